@@ -1,0 +1,174 @@
+/*
+ * pbf.h — C ABI of the GB300 Position Based Fluids step.
+ *
+ * This is the boundary a host (the C++ Particles facade in fluid_gb300/host,
+ * Python through ctypes, or any FFI) binds. It replaces the reference's
+ * in-process simulator struct `Particles` (src/particles.h:105-140) and its
+ * step `Particles::timeStep(double)` (src/particles.cpp:250-297). Signatures
+ * carry plain pointers and sizes only. Every function returns a pbf_status;
+ * no C++ exception crosses the ABI. A handle owns all of its device memory
+ * and one CUDA stream; one host thread may use a handle at a time, distinct
+ * handles are independent.
+ *
+ * Arrays named xyz / vel are row-major (n, 3) float32 in the ORIGINAL particle
+ * order (the order of pbf_create's input, as the reference's `ps` vector).
+ * Functions whose name ends in _device take device pointers and a cudaStream_t
+ * passed as void*; the handle's stream is ordered after that stream on entry
+ * and the caller's stream after the handle's on exit.
+ */
+#ifndef PBF_H
+#define PBF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBF_ABI_VERSION 1
+
+typedef enum pbf_status {
+  PBF_OK = 0,
+  PBF_ERR_INVALID = 1,   /* bad argument or handle state */
+  PBF_ERR_CUDA = 2,      /* a CUDA runtime call failed (see pbf_last_error) */
+  PBF_ERR_TIMEOUT = 3,   /* a bounded device-side wait gave up */
+  PBF_ERR_NONFINITE = 4, /* a position or velocity became NaN/Inf */
+  PBF_ERR_CAPACITY = 5,  /* neighbour list or cell-row capacity exceeded */
+  PBF_ERR_NOMEM = 6      /* device allocation failed */
+} pbf_status;
+
+/* flags */
+#define PBF_FLAG_STATS 1          /* accumulate pbf_stats every step */
+#define PBF_FLAG_GRAPH 2          /* capture the step as a CUDA graph and replay it */
+#define PBF_FLAG_KEEP_PREDICTED 4 /* keep x* after prediction (for pbf_get_predicted) */
+
+/*
+ * Step parameters. pbf_params_default() fills the reference's compile-time
+ * constants (src/particles.cpp:20-44, 151, 180). The reference has implicit
+ * unit particle mass, so rest_density is rho0/m for a fluid of rest density
+ * rho0 and particle mass m.
+ */
+typedef struct pbf_params {
+  double h;               /* kernel radius H (particles.cpp:26) */
+  double h2;              /* neighbour radius squared H2 (particles.cpp:28) */
+  int32_t iters;          /* Jacobi iterations NEWTON_NUM_STEPS (particles.cpp:34) */
+  int32_t scorr_n;        /* tensile exponent N (particles.cpp:40) */
+  double epsilon;         /* constraint relaxation EPSILON (particles.cpp:36) */
+  double scorr_k;         /* tensile coefficient K (particles.cpp:38) */
+  double scorr_dq;        /* tensile reference distance / H, 0.1 (particles.cpp:151) */
+  double vort_eps;        /* VORTICITY_EPSILON (particles.cpp:42) */
+  double xsph_c;          /* XSPH viscosity C (particles.cpp:44) */
+  double dt;              /* DEFAULT_DELTA_T (particles.cpp:24), used by pbf_step(dt <= 0) */
+  double gravity[3];      /* (0, -10, 0) (particles.cpp:180) */
+  double rest_density;    /* Particles(double rest_density = 1000) (particles.h:112) */
+  double box_lo[3];       /* collider: axis-aligned box walls (the reference casts */
+  double box_hi[3];       /*   rays against scene triangles, particles.cpp:51-132) */
+  int32_t box_open_mask;  /* bit 2*axis+side: leave that wall out */
+  int32_t n_clip;         /* clip planes tested before the walls (particles.cpp:57-74) */
+  int32_t clip_axis[2];   /*   default z = 1.0 and y = 1.49 */
+  double clip_value[2];
+  double clamp_lo[3];     /* final clamp box (particles.cpp:81-83) */
+  double clamp_hi[3];
+  int32_t max_neighbors;  /* neighbour capacity per particle (0: 128) */
+  int32_t flags;          /* PBF_FLAG_* */
+} pbf_params;
+
+typedef struct pbf_stats {
+  uint64_t steps;              /* steps taken since create / reset */
+  double mean_density_iter0;   /* mean density after the first lambda pass of the last step
+                                  (the first number of particles.cpp:275-280's print) */
+  double mean_density;         /* mean reported density after the last step (particles.cpp:295) */
+  double max_density_error;    /* max |rho/rho0 - 1| after the last step */
+  double mean_density_error;   /* mean |rho/rho0 - 1| after the last step */
+  uint32_t min_neighbors;      /* over particles, last step */
+  uint32_t max_neighbors;
+  double mean_neighbors;
+  uint64_t low_neighbor_count; /* particles under NUM_NEIGHBOR_ALERT_THRESHOLD=18 (particles.cpp:32) */
+  uint32_t error_flags;        /* sticky device error bits (PBF_ERRBIT_*) */
+} pbf_stats;
+
+#define PBF_ERRBIT_NONFINITE 1u
+#define PBF_ERRBIT_NEIGHBOR_CAPACITY 2u
+#define PBF_ERRBIT_ROW_CAPACITY 4u
+
+typedef struct pbf_handle pbf_handle;
+
+/* Fill *p with the reference's defaults (src/particles.cpp:20-44, 57-83, 180). */
+void pbf_params_default(pbf_params* p);
+
+/* ABI version of the loaded library. */
+int pbf_abi_version(void);
+
+/*
+ * Create a simulator over n particles (replaces `new Particles(rho0)` followed
+ * by n calls of Particles::addParticle, particles.h:112-120). xyz/vel: host,
+ * (n, 3) float32; vel may be NULL (zero). device: CUDA ordinal.
+ */
+pbf_status pbf_create(const pbf_params* params, size_t n, const float* xyz,
+                      const float* vel, int device, pbf_handle** out);
+
+/*
+ * Batched form: n_scenes independent scenes stored back to back (scene s owns
+ * counts[s] particles), each with its own collider box (box_lo/box_hi: host,
+ * (n_scenes, 3); NULL = params->box_lo/hi). All scenes share the remaining
+ * params. One launch per phase covers every scene.
+ */
+pbf_status pbf_batch_create(const pbf_params* params, int n_scenes,
+                            const size_t* counts, const float* box_lo,
+                            const float* box_hi, const float* xyz,
+                            const float* vel, int device, pbf_handle** out);
+
+pbf_status pbf_destroy(pbf_handle* h);
+
+/* Advance nsteps steps of dt each (Particles::timeStep(double),
+ * particles.cpp:250-297; dt <= 0 uses params.dt like Particles::timeStep()). */
+pbf_status pbf_step(pbf_handle* h, double dt, int nsteps);
+
+/* Host accessors, original order (Particle::getPosition, ::velocity,
+ * ::getLatestDensityEstimate; particles.h:36-46). */
+pbf_status pbf_get_positions(pbf_handle* h, float* xyz);
+pbf_status pbf_get_velocities(pbf_handle* h, float* vel);
+pbf_status pbf_get_densities(pbf_handle* h, float* rho);
+/* Replace positions and velocities (host). */
+pbf_status pbf_set_state(pbf_handle* h, const float* xyz, const float* vel);
+
+/* Device-pointer forms of the accessors (see file comment for stream order). */
+pbf_status pbf_set_state_device(pbf_handle* h, const float* xyz,
+                                const float* vel, void* stream);
+pbf_status pbf_get_state_device(pbf_handle* h, float* xyz, float* vel,
+                                float* rho, void* stream);
+
+/* Particles::estimateDensities (particles.cpp:440-444): density of every
+ * particle at its current position, self included; host out[n]. */
+pbf_status pbf_estimate_densities(pbf_handle* h, float* rho);
+
+/* Particles::estimateDensityAt (particles.cpp:446-453) at m query points
+ * (host, (m, 3)); out[m]. */
+pbf_status pbf_estimate_density_at(pbf_handle* h, size_t m, const float* pts,
+                                   float* out);
+
+pbf_status pbf_get_stats(pbf_handle* h, pbf_stats* out);
+
+/* Introspection of the last step, original order. Neighbour sets are those
+ * of the reference's all-pairs search (particles.cpp:258-265) on x*:
+ * counts[n], then ids in ascending original index (capacity cap entries;
+ * *total receives the number needed). cells[n]: linear cell id of x*.
+ * pred: x* after prediction (needs PBF_FLAG_KEEP_PREDICTED). */
+pbf_status pbf_get_neighbors(pbf_handle* h, uint32_t* counts, uint32_t* ids,
+                             size_t cap, size_t* total);
+pbf_status pbf_get_cells(pbf_handle* h, uint32_t* cells);
+pbf_status pbf_get_predicted(pbf_handle* h, float* xyz);
+
+size_t pbf_size(const pbf_handle* h);
+int pbf_num_scenes(const pbf_handle* h);
+
+/* Human-readable description of the last error on this handle (or of the
+ * last failed pbf_create when h is NULL). Never NULL. */
+const char* pbf_last_error(const pbf_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBF_H */

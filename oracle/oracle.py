@@ -1,0 +1,127 @@
+"""ctypes wrapper of the FP64 restatement oracle (oracle/pbf_oracle.c).
+
+TEST INFRASTRUCTURE (the oracle): imported only by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, as the checker or the timed CPU baseline. ``build()``
+compiles the restatement with ``-ffp-contract=off`` so that x86-64 and aarch64 round
+identically; it is called by ``__graft_entry__.build()``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent
+SRC = HERE / "pbf_oracle.c"
+LIB = HERE / "_build" / "libpbf_oracle.so"
+
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+from fluid_gb300.params import PbfParams  # noqa: E402
+
+
+def build(force: bool = False) -> Path:
+    LIB.parent.mkdir(parents=True, exist_ok=True)
+    if not force and LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+           "-fPIC", "-shared", "-Wall", "-o", str(LIB), str(SRC), "-lm"]
+    subprocess.run(cmd, check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        L = ctypes.CDLL(str(LIB))
+        P = ctypes.c_void_p
+        L.orc_step.argtypes = [P, ctypes.c_int64, P, P, P, ctypes.c_int, ctypes.c_double,
+                               P, P, ctypes.c_int64, P, P, ctypes.c_int]
+        L.orc_step.restype = ctypes.c_int
+        L.orc_estimate_densities.argtypes = [P, ctypes.c_int64, P, P, ctypes.c_int]
+        L.orc_estimate_densities.restype = ctypes.c_int
+        L.orc_estimate_density_at.argtypes = [P, ctypes.c_int64, P, ctypes.c_int64, P, P, ctypes.c_int]
+        L.orc_estimate_density_at.restype = ctypes.c_int
+        L.orc_max_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def step(pos, vel, params: PbfParams, steps: int = 1, dt: float | None = None,
+         neighbors: bool = False, predicted: bool = False, threads: int = 0) -> dict:
+    """``steps`` FP64 steps from (pos, vel); returns pos, vel, density (+ neighbour CSR)."""
+    L = lib()
+    pos = np.array(pos, dtype=np.float64, order="C", copy=True)
+    vel = np.array(vel, dtype=np.float64, order="C", copy=True)
+    n = pos.shape[0]
+    rho = np.zeros(n, dtype=np.float64)
+    cp = params.to_c()
+    rho0 = np.zeros(max(steps, 1), dtype=np.float64)
+    pred = np.zeros((n, 3), dtype=np.float64) if predicted else None
+    off = np.zeros(n + 1, dtype=np.int64) if neighbors else None
+    cap = 64 * n if neighbors else 0
+    idx = np.zeros(max(cap, 1), dtype=np.int64) if neighbors else None
+    dtv = params.dt if dt is None else dt
+    pos0, vel0 = pos.copy(), vel.copy()
+    rc = L.orc_step(ctypes.byref(cp), n, _ptr(pos), _ptr(vel), _ptr(rho), steps, dtv,
+                    _ptr(off), _ptr(idx), cap, _ptr(pred), _ptr(rho0), threads)
+    if rc == 1 and neighbors:  # rerun with the exact capacity the last step needed
+        cap = int(off[-1])
+        idx = np.zeros(max(cap, 1), dtype=np.int64)
+        pos, vel = pos0, vel0
+        rc = L.orc_step(ctypes.byref(cp), n, _ptr(pos), _ptr(vel), _ptr(rho), steps, dtv,
+                        _ptr(off), _ptr(idx), cap, _ptr(pred), _ptr(rho0), threads)
+    if rc != 0:
+        raise RuntimeError(f"orc_step failed: {rc}")
+    out = {"pos": pos, "vel": vel, "density": rho, "mean_density_iter0": rho0[:steps]}
+    if neighbors:
+        out["nbr_offsets"] = off
+        out["nbr_idx"] = idx[: off[-1]].copy()
+    if predicted:
+        out["pred"] = pred
+    return out
+
+
+def estimate_densities(pos, params: PbfParams, threads: int = 0) -> np.ndarray:
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    out = np.zeros(pos.shape[0], dtype=np.float64)
+    cp = params.to_c()
+    rc = lib().orc_estimate_densities(ctypes.byref(cp), pos.shape[0], _ptr(pos), _ptr(out), threads)
+    if rc:
+        raise RuntimeError(f"orc_estimate_densities failed: {rc}")
+    return out
+
+
+def estimate_density_at(pos, pts, params: PbfParams, threads: int = 0) -> np.ndarray:
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    out = np.zeros(pts.shape[0], dtype=np.float64)
+    cp = params.to_c()
+    rc = lib().orc_estimate_density_at(ctypes.byref(cp), pos.shape[0], _ptr(pos), pts.shape[0],
+                                       _ptr(pts), _ptr(out), threads)
+    if rc:
+        raise RuntimeError(f"orc_estimate_density_at failed: {rc}")
+    return out
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv))

@@ -1,0 +1,578 @@
+/*
+ * pbf_oracle.c — FP64 CPU restatement of the reference's PBF step.
+ *
+ * TEST INFRASTRUCTURE (the oracle). Only tests/, __graft_entry__.smoke() and
+ * bench.py's CPU-baseline leg load this library, and only as the checker or
+ * the timed CPU baseline; the product path never calls it.
+ *
+ * It restates src/particles.cpp of the reference with the same floating-point
+ * operation order (Vector3D ops of CGL/include/CGL/vector3D.h, intpow of
+ * src/bsdf.h:49-57), so that with -ffp-contract=off it reproduces the
+ * reference's "jacobi" sequence bit for bit. Differences from the reference,
+ * each deliberate:
+ *   - neighbour search uses a uniform grid instead of the all-pairs loop
+ *     (particles.cpp:258-265); lists are sorted by index, which is the order
+ *     the all-pairs loop produces, so every sum runs in the same order;
+ *   - the XSPH/vorticity pass (particles.cpp:285-288) is order-independent:
+ *     every particle sees its neighbours' pre-XSPH velocity;
+ *   - the collider is the reference's triangle box (12 triangles, inward
+ *     normals, built like oracle/ref/ref_driver.cpp) intersected with
+ *     Moller-Trumbore (src/static_scene/marching_triangle.cpp:21-45) by a
+ *     linear scan for the NEAREST hit in both clamp and clamp_response. The
+ *     reference's clamp (particles.cpp:76) uses BVHAccel::intersect(const
+ *     Ray&), which returns the first hit in BVH order (src/bvh.cpp:142-160);
+ *     the two differ only when one displacement crosses two walls.
+ *   - gravity is a 3-vector applied per non-zero component (the reference
+ *     subtracts 10*dt from v.y, particles.cpp:180).
+ * Parallel over particles with OpenMP; every phase is order-independent so the
+ * result does not depend on the thread count.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/pbf.h"
+
+#define EPS_D (0.00000000001) /* CGL/include/CGL/misc.h:11 */
+
+typedef struct { double x, y, z; } v3;
+
+static inline v3 V(double x, double y, double z) { v3 r = {x, y, z}; return r; }
+static inline v3 vadd(v3 a, v3 b) { return V(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 vsub(v3 a, v3 b) { return V(a.x - b.x, a.y - b.y, a.z - b.z); }
+/* Vector3D * double and double * Vector3D: component products. */
+static inline v3 vscale(v3 a, double c) { return V(a.x * c, a.y * c, a.z * c); }
+static inline v3 svmul(double c, v3 a) { return V(c * a.x, c * a.y, c * a.z); }
+/* Vector3D / double: multiply by the reciprocal (vector3D.h operator/). */
+static inline v3 vdiv(v3 a, double c) { const double rc = 1.0 / c; return V(rc * a.x, rc * a.y, rc * a.z); }
+static inline double norm2(v3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+static inline double vnorm(v3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+static inline v3 unit(v3 a) { double r = 1. / sqrt(a.x * a.x + a.y * a.y + a.z * a.z); return V(r * a.x, r * a.y, r * a.z); }
+static inline double dot(v3 u, v3 v) { return u.x * v.x + u.y * v.y + u.z * v.z; }
+static inline v3 cross(v3 u, v3 v) {
+  return V(u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x);
+}
+static inline double comp(v3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+static inline void setcomp(v3* a, int k, double v) { if (k == 0) a->x = v; else if (k == 1) a->y = v; else a->z = v; }
+/* std::max / std::min as <algorithm> defines them. */
+static inline double smax(double a, double b) { return (a < b) ? b : a; }
+static inline double smin(double a, double b) { return (b < a) ? b : a; }
+
+/* intpow<e>(b) = intpow<e-1>(b) * b, intpow<0> = 1 (src/bsdf.h:49-57). */
+static inline double intpow(double b, int e) {
+  double r = 1;
+  for (int i = 0; i < e; i++) r = r * b;
+  return r;
+}
+
+typedef struct {
+  double h, h2, h6, h9, tis;
+  double epsilon, k, vort_eps, xsph_c, rest_density;
+  int iters, scorr_n;
+  v3 gravity;
+  double clamp_lo[3], clamp_hi[3];
+  int n_clip, clip_axis[2];
+  double clip_value[2];
+  int ntri;
+  v3 tp[12][3];
+  v3 tn[12];
+} ctx_t;
+
+/* poly6_kernel, particles.cpp:134-141 */
+static inline double poly6(const ctx_t* c, v3 r) {
+  double r_l_2 = norm2(r);
+  if (r_l_2 >= c->h2) return 0.0;
+  double temp = c->h2 - r_l_2;
+  return 1.56668147106 * intpow(temp, 3) / c->h9;
+}
+
+/* grad_spiky_kernel, particles.cpp:143-149 */
+static inline v3 spiky(const ctx_t* c, v3 r) {
+  double r_l = vnorm(r);
+  if (r_l >= c->h || r_l < EPS_D) return V(0, 0, 0);
+  const double k0 = -3 * 4.774648292756860;
+  return vdiv(svmul(k0 * intpow(c->h - r_l, 2), r), c->h6 * r_l);
+}
+
+/* ---- collider: triangle box + Moller-Trumbore ------------------------------ */
+
+static void build_box(ctx_t* c, const double lo[3], const double hi[3], int open_mask) {
+  c->ntri = 0;
+  for (int axis = 0; axis < 3; axis++) {
+    for (int side = 0; side < 2; side++) {
+      if (open_mask & (1 << (2 * axis + side))) continue;
+      int u = (axis + 1) % 3, w = (axis + 2) % 3;
+      double cc = side ? hi[axis] : lo[axis];
+      double us[4] = {lo[u], hi[u], hi[u], lo[u]};
+      double vs[4] = {lo[w], lo[w], hi[w], hi[w]};
+      v3 corner[4];
+      for (int k = 0; k < 4; k++) {
+        corner[k] = V(0, 0, 0);
+        setcomp(&corner[k], axis, cc);
+        setcomp(&corner[k], u, us[k]);
+        setcomp(&corner[k], w, vs[k]);
+      }
+      v3 n = V(0, 0, 0);
+      setcomp(&n, axis, side ? -1.0 : 1.0);
+      int t = c->ntri;
+      c->tp[t][0] = corner[0]; c->tp[t][1] = corner[1]; c->tp[t][2] = corner[2]; c->tn[t] = n;
+      c->tp[t + 1][0] = corner[0]; c->tp[t + 1][1] = corner[2]; c->tp[t + 1][2] = corner[3]; c->tn[t + 1] = n;
+      c->ntri += 2;
+    }
+  }
+}
+
+typedef struct { v3 o, d; double min_t, max_t; } ray_t;
+
+/* MarchingTriangle::intersect(const Ray&, Intersection*) arithmetic. */
+static int tri_hit(const ctx_t* c, int t, ray_t* r, v3* nrm) {
+  v3 p1 = c->tp[t][0], p2 = c->tp[t][1], p3 = c->tp[t][2];
+  v3 e1 = vsub(p2, p1), e2 = vsub(p3, p1), s = vsub(r->o, p1);
+  v3 s1 = cross(r->d, e2), s2 = cross(s, e1);
+  double d = dot(s1, e1);
+  if (d == 0) return 0;
+  double tt = dot(s2, e2) / d;
+  if ((tt < r->min_t) || (tt > r->max_t)) return 0;
+  double u = dot(s1, s) / d;
+  double v = dot(s2, r->d) / d;
+  double w = 1 - u - v;
+  if ((u < 0) || (u > 1) || (v < 0) || (v > 1) || (w < 0) || (w > 1)) return 0;
+  r->max_t = tt;
+  if (nrm) {
+    v3 n = c->tn[t];
+    *nrm = vadd(vadd(svmul(w, n), svmul(u, n)), svmul(v, n));
+  }
+  return 1;
+}
+
+/* Nearest hit over all triangles; updates r->max_t, *nrm. */
+static int scene_hit(const ctx_t* c, ray_t* r, v3* nrm) {
+  int hit = 0;
+  for (int t = 0; t < c->ntri; t++) hit |= tri_hit(c, t, r, nrm);
+  return hit;
+}
+
+static inline void clamp_box(const ctx_t* c, v3* p) {
+  p->x = smax(c->clamp_lo[0] + EPS_D, smin(c->clamp_hi[0] - EPS_D, p->x));
+  p->y = smax(c->clamp_lo[1] + EPS_D, smin(c->clamp_hi[1] - EPS_D, p->y));
+  p->z = smax(c->clamp_lo[2] + EPS_D, smin(c->clamp_hi[2] - EPS_D, p->z));
+}
+
+static inline int clip_planes(const ctx_t* c, v3 p, v3 d, double* l) {
+  int intersect = 0;
+  for (int i = 0; i < c->n_clip; i++) {
+    int a = c->clip_axis[i];
+    double da = comp(d, a);
+    if (da != 0.0) {
+      double pt = (c->clip_value[i] - comp(p, a)) / da;
+      if (pt > 0.0 && pt < *l) {
+        *l = pt;
+        intersect = 1;
+      }
+    }
+  }
+  return intersect;
+}
+
+/* clamp, particles.cpp:51-84 */
+static void clamp_move(const ctx_t* c, v3* p, v3 delta_p) {
+  double l = vnorm(delta_p);
+  if (l <= EPS_D) return;
+  v3 d = vdiv(delta_p, l);
+  int intersect = clip_planes(c, *p, d, &l);
+  ray_t r = {*p, d, 0.0, l};
+  if (scene_hit(c, &r, NULL) || intersect) {
+    *p = vadd(*p, svmul(r.max_t - EPS_D, d));
+  } else {
+    *p = vadd(*p, delta_p);
+  }
+  clamp_box(c, p);
+}
+
+/* clamp_response, particles.cpp:87-132 */
+static void clamp_response(const ctx_t* c, v3* p, v3 v, double dt) {
+  v3 delta_p = vscale(v, dt);
+  double total_l = vnorm(delta_p), l = total_l;
+  if (l <= EPS_D) return;
+  v3 d = vdiv(delta_p, l);
+  int intersect = clip_planes(c, *p, d, &l);
+  ray_t r = {*p, d, 0.0, l};
+  v3 n = V(0, 0, 0);
+  if (scene_hit(c, &r, &n) || intersect) {
+    *p = vadd(*p, svmul(r.max_t - EPS_D, d));
+    if (dot(d, n) > -1 && !intersect) {
+      d = unit(vsub(delta_p, svmul(dot(delta_p, n), n)));
+      ray_t r2 = {*p, d, 0.0, (total_l - r.max_t) * 0.5};
+      v3 n2 = V(0, 0, 0);
+      scene_hit(c, &r2, &n2);
+      *p = vadd(*p, svmul(r2.max_t - EPS_D, d));
+    }
+  } else {
+    *p = vadd(*p, delta_p);
+  }
+  clamp_box(c, p);
+}
+
+/* ---- neighbour search: uniform grid, lists ascending by index -------------- */
+
+typedef struct {
+  int64_t* off;  /* n+1 */
+  int64_t* idx;  /* off[n] */
+} nbrs_t;
+
+static int cmp_i64(const void* a, const void* b) {
+  int64_t x = *(const int64_t*)a, y = *(const int64_t*)b;
+  return (x > y) - (x < y);
+}
+
+/* N(i) = { j != i : |x*_i - x*_j|^2 <= H2 } (particles.cpp:258-265). */
+static int find_neighbors(const ctx_t* c, int64_t n, const v3* xs, nbrs_t* out) {
+  out->off = (int64_t*)calloc((size_t)n + 1, sizeof(int64_t));
+  out->idx = NULL;
+  if (!out->off) return -1;
+  if (n == 0) return 0;
+  double lo[3] = {xs[0].x, xs[0].y, xs[0].z}, hi[3] = {lo[0], lo[1], lo[2]};
+  for (int64_t i = 1; i < n; i++)
+    for (int k = 0; k < 3; k++) {
+      double v = comp(xs[i], k);
+      if (v < lo[k]) lo[k] = v;
+      if (v > hi[k]) hi[k] = v;
+    }
+  const double cell = sqrt(c->h2) * (1.0 + 1e-6);
+  int64_t dim[3];
+  for (int k = 0; k < 3; k++) {
+    if (!(hi[k] - lo[k] < 1e6 * cell)) return -2; /* non-finite or absurd extent */
+    dim[k] = (int64_t)floor((hi[k] - lo[k]) / cell) + 1;
+  }
+  int64_t ncell = dim[0] * dim[1] * dim[2];
+  if (ncell > ((int64_t)1 << 31)) return -2;
+  int64_t* cell_of = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
+  int64_t* start = (int64_t*)calloc((size_t)ncell + 1, sizeof(int64_t));
+  int64_t* sorted = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
+  if (!cell_of || !start || !sorted) return -1;
+  for (int64_t i = 0; i < n; i++) {
+    int64_t ci[3];
+    for (int k = 0; k < 3; k++) {
+      ci[k] = (int64_t)floor((comp(xs[i], k) - lo[k]) / cell);
+      if (ci[k] < 0) ci[k] = 0;
+      if (ci[k] >= dim[k]) ci[k] = dim[k] - 1;
+    }
+    cell_of[i] = (ci[2] * dim[1] + ci[1]) * dim[0] + ci[0];
+    start[cell_of[i] + 1]++;
+  }
+  for (int64_t q = 0; q < ncell; q++) start[q + 1] += start[q];
+  {
+    int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (size_t)ncell);
+    if (!fill) return -1;
+    memcpy(fill, start, sizeof(int64_t) * (size_t)ncell);
+    for (int64_t i = 0; i < n; i++) sorted[fill[cell_of[i]]++] = i; /* ascending within a cell */
+    free(fill);
+  }
+  for (int pass = 0; pass < 2; pass++) {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; i++) {
+      int64_t q = cell_of[i];
+      int64_t cx = q % dim[0], cy = (q / dim[0]) % dim[1], cz = q / (dim[0] * dim[1]);
+      int64_t cnt = 0;
+      int64_t* dst = pass ? out->idx + out->off[i] : NULL;
+      for (int64_t z = cz - 1; z <= cz + 1; z++) {
+        if (z < 0 || z >= dim[2]) continue;
+        for (int64_t y = cy - 1; y <= cy + 1; y++) {
+          if (y < 0 || y >= dim[1]) continue;
+          for (int64_t x = cx - 1; x <= cx + 1; x++) {
+            if (x < 0 || x >= dim[0]) continue;
+            int64_t qq = (z * dim[1] + y) * dim[0] + x;
+            for (int64_t s = start[qq]; s < start[qq + 1]; s++) {
+              int64_t j = sorted[s];
+              if (j == i) continue;
+              v3 a = xs[i < j ? i : j], b = xs[i < j ? j : i];
+              if (norm2(vsub(a, b)) <= c->h2) {
+                if (dst) dst[cnt] = j;
+                cnt++;
+              }
+            }
+          }
+        }
+      }
+      if (pass == 0) {
+        out->off[i + 1] = cnt;
+      } else {
+        qsort(dst, (size_t)cnt, sizeof(int64_t), cmp_i64);
+      }
+    }
+    if (pass == 0) {
+      for (int64_t i = 0; i < n; i++) out->off[i + 1] += out->off[i];
+      out->idx = (int64_t*)malloc(sizeof(int64_t) * (size_t)(out->off[n] > 0 ? out->off[n] : 1));
+      if (!out->idx) return -1;
+    }
+  }
+  free(cell_of);
+  free(start);
+  free(sorted);
+  return 0;
+}
+
+/* ---- the step ---------------------------------------------------------------- */
+
+static void make_ctx(ctx_t* c, const pbf_params* p) {
+  memset(c, 0, sizeof(*c));
+  c->h = p->h;
+  c->h2 = p->h2;
+  c->h6 = intpow(p->h, 6);
+  c->h9 = intpow(p->h, 9);
+  c->epsilon = p->epsilon;
+  c->k = p->scorr_k;
+  c->vort_eps = p->vort_eps;
+  c->xsph_c = p->xsph_c;
+  c->rest_density = p->rest_density;
+  c->iters = p->iters;
+  c->scorr_n = p->scorr_n;
+  c->gravity = V(p->gravity[0], p->gravity[1], p->gravity[2]);
+  for (int k = 0; k < 3; k++) {
+    c->clamp_lo[k] = p->clamp_lo[k];
+    c->clamp_hi[k] = p->clamp_hi[k];
+  }
+  c->n_clip = p->n_clip < 0 ? 0 : (p->n_clip > 2 ? 2 : p->n_clip);
+  for (int i = 0; i < c->n_clip; i++) {
+    c->clip_axis[i] = p->clip_axis[i];
+    c->clip_value[i] = p->clip_value[i];
+  }
+  build_box(c, p->box_lo, p->box_hi, p->box_open_mask);
+  /* Particle::tensile_instability_scale, particles.cpp:151 */
+  c->tis = 1.0 / poly6(c, V(0, 0, p->scorr_dq * p->h));
+}
+
+typedef struct {
+  double density_iter0_sum;
+} step_info_t;
+
+/*
+ * One step, "jacobi" form (see file comment). pos/vel/rho: n entries (v3 / double).
+ * nb receives the neighbour lists of this step (caller frees).
+ */
+static int step_once(const ctx_t* c, int64_t n, v3* x, v3* v, double* rho, double dt,
+                     nbrs_t* nb, v3* pred_out, step_info_t* info) {
+  v3* xs = (v3*)malloc(sizeof(v3) * (size_t)(n ? n : 1));
+  double* lam = (double*)malloc(sizeof(double) * (size_t)(n ? n : 1));
+  v3* vort = (v3*)malloc(sizeof(v3) * (size_t)(n ? n : 1));
+  v3* vnew = (v3*)malloc(sizeof(v3) * (size_t)(n ? n : 1));
+  if (!xs || !lam || !vort || !vnew) return -1;
+
+  /* applyForceVelocity, particles.cpp:175-183 */
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; i++) {
+    if (c->gravity.x != 0.0) v[i].x -= (-c->gravity.x) * dt;
+    if (c->gravity.y != 0.0) v[i].y -= (-c->gravity.y) * dt;
+    if (c->gravity.z != 0.0) v[i].z -= (-c->gravity.z) * dt;
+    xs[i] = x[i];
+    clamp_response(c, &xs[i], v[i], dt);
+  }
+  if (pred_out) memcpy(pred_out, xs, sizeof(v3) * (size_t)n);
+
+  int rc = find_neighbors(c, n, xs, nb);
+  if (rc) return rc;
+  const int64_t* off = nb->off;
+  const int64_t* idx = nb->idx;
+  int64_t nnz = off[n];
+  double* scorr = (double*)malloc(sizeof(double) * (size_t)(nnz ? nnz : 1));
+  v3* gw = (v3*)malloc(sizeof(v3) * (size_t)(nnz ? nnz : 1));
+  if (!scorr || !gw) return -1;
+
+  for (int it = 0; it < c->iters; it++) {
+    /* newtonStepCalculateLambda, particles.cpp:185-204 */
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+      double density = 0.0, denom = 0.0;
+      v3 grad_i_c_i = V(0, 0, 0);
+      for (int64_t e = off[i]; e < off[i + 1]; e++) {
+        v3 r = vsub(xs[i], xs[idx[e]]);
+        double w = poly6(c, r);
+        v3 g = spiky(c, r);
+        density += w;
+        scorr[e] = -c->k * intpow(w * c->tis, c->scorr_n);
+        gw[e] = g;
+        g = svmul(1. / c->rest_density, g);
+        grad_i_c_i = vadd(grad_i_c_i, g);
+        denom += norm2(g);
+      }
+      double c_i = density / c->rest_density - 1.0;
+      denom += norm2(grad_i_c_i);
+      lam[i] = -c_i / (denom + c->epsilon);
+      rho[i] = density;
+    }
+    if (it == 0 && info) {
+      double s = 0.0;
+      for (int64_t i = 0; i < n; i++) s += rho[i];
+      info->density_iter0_sum = s;
+    }
+    /* newtonStepUpdatePosition, particles.cpp:206-213 */
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+      v3 delta_p = V(0, 0, 0);
+      for (int64_t e = off[i]; e < off[i + 1]; e++) {
+        delta_p = vadd(delta_p, svmul(lam[i] + lam[idx[e]] + scorr[e], gw[e]));
+      }
+      delta_p = svmul(1. / c->rest_density, delta_p);
+      clamp_move(c, &xs[i], delta_p);
+    }
+  }
+
+  /* updateVelocity, particles.cpp:215-217 */
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; i++) v[i] = vdiv(vsub(xs[i], x[i]), dt);
+
+  /* calculateVorticityApplyXSPHViscosity, particles.cpp:219-234 (pre-XSPH neighbour velocities) */
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; i++) {
+    v3 w_acc = V(0, 0, 0), visc = V(0, 0, 0);
+    double density = 0.0;
+    for (int64_t e = off[i]; e < off[i + 1]; e++) {
+      int64_t j = idx[e];
+      v3 v_i_n = vsub(v[j], v[i]);
+      v3 r = vsub(xs[i], xs[j]);
+      v3 g = spiky(c, r);
+      w_acc = vadd(w_acc, cross(v_i_n, g));
+      double w = poly6(c, r);
+      visc = vadd(visc, vscale(v_i_n, w));
+      gw[e] = g;
+      density += w;
+    }
+    vort[i] = w_acc;
+    rho[i] = density;
+    vnew[i] = vadd(v[i], svmul(c->xsph_c, visc));
+  }
+
+  /* applyVorticity + updatePosition, particles.cpp:236-248, 289-294 */
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; i++) {
+    v3 gv = V(0, 0, 0);
+    for (int64_t e = off[i]; e < off[i + 1]; e++) {
+      gv = vadd(gv, svmul(vnorm(vort[idx[e]]), gw[e]));
+    }
+    v3 vi = vnew[i];
+    if (vnorm(gv) > EPS_D) {
+      vi = vadd(vi, svmul(dt * c->vort_eps, cross(unit(gv), vort[i])));
+    }
+    v[i] = vi;
+    x[i] = xs[i];
+  }
+  free(xs);
+  free(lam);
+  free(vort);
+  free(vnew);
+  free(scorr);
+  free(gw);
+  return 0;
+}
+
+/* ---- exported ---------------------------------------------------------------- */
+
+static void set_threads(int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+}
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/*
+ * nsteps steps in place on pos/vel ((n,3) float64); rho[n] receives the
+ * reported densities. If nbr_off (n+1) is given, the last step's neighbour
+ * lists are written to nbr_off / nbr_idx (capacity nbr_cap); returns 1 if the
+ * capacity was too small (nbr_off[n] then holds the needed count). pred
+ * ((n,3) or NULL) receives x* after the last prediction; rho_iter0 (nsteps or
+ * NULL) the mean density after each step's first lambda pass.
+ */
+int orc_step(const pbf_params* prm, int64_t n, double* pos, double* vel, double* rho,
+             int nsteps, double dt, int64_t* nbr_off, int64_t* nbr_idx, int64_t nbr_cap,
+             double* pred, double* rho_iter0, int nthreads) {
+  set_threads(nthreads);
+  ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+  if (!c) return -1;
+  make_ctx(c, prm);
+  int rc = 0;
+  for (int s = 0; s < nsteps && rc == 0; s++) {
+    nbrs_t nb = {NULL, NULL};
+    step_info_t info = {0};
+    rc = step_once(c, n, (v3*)pos, (v3*)vel, rho, dt, &nb,
+                   (pred && s == nsteps - 1) ? (v3*)pred : NULL, &info);
+    if (rc == 0 && rho_iter0) rho_iter0[s] = n ? info.density_iter0_sum / (double)n : 0.0;
+    if (rc == 0 && s == nsteps - 1 && nbr_off) {
+      memcpy(nbr_off, nb.off, sizeof(int64_t) * (size_t)(n + 1));
+      if (nb.off[n] > nbr_cap) {
+        rc = 1;
+      } else if (nb.off[n] > 0) {
+        memcpy(nbr_idx, nb.idx, sizeof(int64_t) * (size_t)nb.off[n]);
+      }
+    }
+    free(nb.off);
+    free(nb.idx);
+  }
+  free(c);
+  return rc;
+}
+
+/* Particles::estimateDensities, particles.cpp:440-444: self included, sum in index order. */
+int orc_estimate_densities(const pbf_params* prm, int64_t n, const double* pos, double* out,
+                           int nthreads) {
+  set_threads(nthreads);
+  ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+  if (!c) return -1;
+  make_ctx(c, prm);
+  const v3* x = (const v3*)pos;
+  nbrs_t nb = {NULL, NULL};
+  int rc = find_neighbors(c, n, x, &nb);
+  if (rc == 0) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+      double d = 0.0;
+      int self_done = 0;
+      for (int64_t e = nb.off[i]; e < nb.off[i + 1]; e++) {
+        int64_t j = nb.idx[e];
+        if (!self_done && j > i) {
+          d += poly6(c, vsub(x[i], x[i]));
+          self_done = 1;
+        }
+        d += poly6(c, vsub(x[j], x[i]));
+      }
+      if (!self_done) d += poly6(c, vsub(x[i], x[i]));
+      out[i] = d;
+    }
+  }
+  free(nb.off);
+  free(nb.idx);
+  free(c);
+  return rc;
+}
+
+/* Particles::estimateDensityAt, particles.cpp:446-453, brute force in index order. */
+int orc_estimate_density_at(const pbf_params* prm, int64_t n, const double* pos, int64_t m,
+                            const double* pts, double* out, int nthreads) {
+  set_threads(nthreads);
+  ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+  if (!c) return -1;
+  make_ctx(c, prm);
+  const v3* x = (const v3*)pos;
+  const v3* q = (const v3*)pts;
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < m; k++) {
+    double d = 0.0;
+    for (int64_t i = 0; i < n; i++) d += poly6(c, vsub(x[i], q[k]));
+    out[k] = d;
+  }
+  free(c);
+  return 0;
+}

@@ -1,0 +1,100 @@
+"""Generate the golden vectors in tests/golden/ by running the reference's own PBF step.
+
+Runs where the reference checkout and its headless build exist (oracle/ref/build_ref.py);
+the GPU machine only reads the committed ``*.npz`` files. Each case stores its inputs,
+its parameters (JSON) and the outputs of the reference step in both orders:
+
+* ``jacobi`` — the reference's Particle methods with an order-independent XSPH pass
+  (oracle/ref/ref_driver.cpp, mode 1): what the oracle restatement and the CUDA path
+  compute;
+* ``literal`` — the reference's unmodified ``Particles::timeStep`` (mode 0).
+
+Usage: ``python tests/golden/make_golden.py [reference_dir]``.
+"""
+from __future__ import annotations
+
+import dataclasses
+import json
+import sys
+import xml.etree.ElementTree as ET
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT))
+
+from fluid_gb300 import scenes  # noqa: E402
+from fluid_gb300.params import PbfParams  # noqa: E402
+from oracle import ref_runner  # noqa: E402
+
+# The reference's Cornell box scene (dae/sky/CBempty.dae): walls x = +-1, floor y = 0,
+# ceiling y = 1.5, back z = -1, open front z = +1 (clipped by particles.cpp:57-65).
+CORNELL = dict(box_lo=(-1.0, 0.0, -1.0), box_hi=(1.0, 1.5, 1.0), box_open_mask=1 << 5)
+
+
+def load_reference_xml(path: Path):
+    """Application::load_particles (application.cpp:302-344): density via stof, pos/v triples."""
+    root = ET.parse(path).getroot()
+    rho0 = float(np.float32(float(root.find("density").text)))
+    pos, vel = [], []
+    for p in root.find("ps").findall("particle"):
+        pos.append([float(t) for t in p.find("pos").text.split()])
+        vel.append([float(t) for t in p.find("v").text.split()])
+    return np.array(pos), np.array(vel), rho0
+
+
+def save_case(name: str, pos, vel, params: PbfParams, steps: int, neighbors: bool = True) -> None:
+    jac = ref_runner.run(pos, vel, params, steps=steps, mode="jacobi", neighbors=neighbors,
+                         load_density=True)
+    lit = ref_runner.run(pos, vel, params, steps=steps, mode="literal")
+    data = dict(
+        params=json.dumps(dataclasses.asdict(params)),
+        steps=np.int64(steps),
+        pos_in=pos, vel_in=vel,
+        pos=jac["pos"], vel=jac["vel"], density=jac["density"],
+        load_density=jac["load_density"],
+        literal_pos=lit["pos"], literal_vel=lit["vel"], literal_density=lit["density"],
+    )
+    if neighbors:
+        data["nbr_offsets"] = jac["nbr_offsets"].astype(np.int32)
+        data["nbr_idx"] = jac["nbr_idx"].astype(np.int32)
+    np.savez_compressed(HERE / f"{name}.npz", **data)
+    print(f"{name}: n={pos.shape[0]} steps={steps}")
+
+
+def params_from_json(text: str) -> PbfParams:
+    d = json.loads(text)
+    for k, v in d.items():
+        if isinstance(v, list):
+            d[k] = tuple(tuple(x) if isinstance(x, list) else x for x in v)
+    return PbfParams(**d)
+
+
+def main(argv):
+    reference = Path(argv[1]) if len(argv) > 1 else Path("/root/reference")
+    if not ref_runner.available():
+        raise SystemExit("build the reference driver first: python oracle/ref/build_ref.py")
+
+    sc = scenes.block4096(1, scale="mass")
+    save_case("block4096_mass_1step", sc.pos, sc.vel, sc.params, 1)
+
+    s = 0.05
+    p = scenes.lattice(8, 8, 8, s)
+    p += scenes.uniform(7, p.size, -0.001, 0.001).reshape(p.shape)
+    # Raw reference constants: the unnormalised XSPH term makes this fluid blow up
+    # within a few steps; 4 steps still run inside the box with wall contacts.
+    save_case("block512_ref_4step", p, np.zeros_like(p), scenes.physical_params(0.1, s, scale="ref"), 4)
+    # Mass-consistent constants: a stable 60-step collapse against the floor and walls.
+    save_case("block512_mass_60step", p, np.zeros_like(p), scenes.physical_params(0.1, s), 60)
+
+    for xml_name, steps in (("p.xml", 1), ("p.xml", 3), ("spheres_p.xml", 1)):
+        pos, vel, rho0 = load_reference_xml(reference / "particles" / xml_name)
+        prm = PbfParams(rest_density=rho0, **CORNELL)
+        stem = xml_name.replace(".xml", "").replace("_p", "p")
+        save_case(f"{stem}_default_{steps}step", pos, vel, prm, steps)
+
+
+if __name__ == "__main__":
+    main(sys.argv)
