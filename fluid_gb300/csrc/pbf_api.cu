@@ -1,0 +1,683 @@
+// C ABI of the PBF step (include/pbf.h): handle lifetime, device memory,
+// stream and CUDA-graph management, host/device transfers, introspection.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "pbf_handle.h"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+double ipow(double b, int e) {
+  double r = 1;
+  for (int i = 0; i < e; ++i) r = r * b;
+  return r;
+}
+
+// poly6 of the reference (particles.cpp:134-141) in FP64, for derived constants.
+double poly6_ref(double r2, double h, double h2) {
+  if (r2 >= h2) return 0.0;
+  const double t = h2 - r2;
+  return 1.56668147106 * ipow(t, 3) / ipow(h, 9);
+}
+
+}  // namespace
+
+namespace pbf {
+
+pbf_status Handle::fail(pbf_status st, const std::string& msg) {
+  err = msg;
+  return st;
+}
+
+pbf_status Handle::cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return PBF_OK;
+  err = std::string(what) + ": " + cudaGetErrorString(e);
+  (void)cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? PBF_ERR_NOMEM : PBF_ERR_CUDA;
+}
+
+DeviceGuard::DeviceGuard(int dev) {
+  if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+  if (prev != dev) cudaSetDevice(dev);
+}
+DeviceGuard::~DeviceGuard() {
+  if (prev >= 0) cudaSetDevice(prev);
+}
+
+bool make_dev_params(const pbf_params& p, DevParams* d, double* cell_out, std::string* why) {
+  if (!(p.h > 0) || !(p.h2 > 0) || !std::isfinite(p.h) || !std::isfinite(p.h2)) {
+    *why = "h and h2 must be positive and finite";
+    return false;
+  }
+  if (p.iters < 0 || p.iters > 1000) {
+    *why = "iters must be in [0, 1000]";
+    return false;
+  }
+  if (p.scorr_n < 1 || p.scorr_n > 16) {
+    *why = "scorr_n must be in [1, 16]";
+    return false;
+  }
+  if (!(p.rest_density > 0) || !std::isfinite(p.rest_density)) {
+    *why = "rest_density must be positive";
+    return false;
+  }
+  if (p.n_clip < 0 || p.n_clip > 2) {
+    *why = "n_clip must be 0, 1 or 2";
+    return false;
+  }
+  for (int c = 0; c < p.n_clip; ++c)
+    if (p.clip_axis[c] < 0 || p.clip_axis[c] > 2) {
+      *why = "clip_axis must be 0, 1 or 2";
+      return false;
+    }
+  const int max_nbr = p.max_neighbors == 0 ? 128 : p.max_neighbors;
+  if (max_nbr < 4 || max_nbr > 255) {
+    *why = "max_neighbors must be in [4, 255]";
+    return false;
+  }
+  std::memset(d, 0, sizeof(*d));
+  const double cell = std::sqrt(p.h2) * 1.001;
+  d->h = static_cast<float>(p.h);
+  d->h2 = static_cast<float>(p.h2);
+  d->cell = static_cast<float>(cell);
+  d->inv_cell = static_cast<float>(1.0 / cell);
+  d->poly6_c = static_cast<float>(1.56668147106 / ipow(p.h, 9));
+  d->spiky_c = static_cast<float>(-3 * 4.774648292756860 / ipow(p.h, 6));
+  const double dq = p.scorr_dq * p.h;
+  d->tis = static_cast<float>(1.0 / poly6_ref(dq * dq, p.h, p.h2));
+  d->scorr_k = static_cast<float>(p.scorr_k);
+  d->epsilon = static_cast<float>(p.epsilon);
+  d->rest_density = static_cast<float>(p.rest_density);
+  d->inv_rho0 = static_cast<float>(1.0 / p.rest_density);
+  d->xsph_c = static_cast<float>(p.xsph_c);
+  d->vort_eps = static_cast<float>(p.vort_eps);
+  for (int k = 0; k < 3; ++k) {
+    d->g[k] = static_cast<float>(p.gravity[k]);
+    d->clamp_lo[k] = static_cast<float>(p.clamp_lo[k]);
+    d->clamp_hi[k] = static_cast<float>(p.clamp_hi[k]);
+  }
+  d->n_clip = p.n_clip;
+  for (int c = 0; c < p.n_clip; ++c) {
+    d->clip_axis[c] = p.clip_axis[c];
+    d->clip_value[c] = static_cast<float>(p.clip_value[c]);
+  }
+  d->scorr_n = p.scorr_n;
+  d->open_mask = p.box_open_mask;
+  d->max_words = (max_nbr + 3) / 4;
+  d->stats = (p.flags & PBF_FLAG_STATS) ? 1 : 0;
+  *cell_out = cell;
+  return true;
+}
+
+// Grid of one scene: the collider box (extended to the clamp box across open
+// faces) plus one margin cell on each side.
+bool make_scene(const pbf_params& p, double cell, const float* lo, const float* hi, SceneDesc* sc,
+                std::string* why) {
+  std::memset(sc, 0, sizeof(*sc));
+  for (int a = 0; a < 3; ++a) {
+    if (!(hi[a] > lo[a])) {
+      *why = "box_hi must exceed box_lo on every axis";
+      return false;
+    }
+    double e0 = lo[a], e1 = hi[a];
+    if (p.box_open_mask & (1 << (2 * a))) e0 = std::min(e0, p.clamp_lo[a]);
+    if (p.box_open_mask & (1 << (2 * a + 1))) e1 = std::max(e1, p.clamp_hi[a]);
+    sc->lo[a] = lo[a];
+    sc->hi[a] = hi[a];
+    sc->origin[a] = static_cast<float>(e0 - cell);
+    const double dim = std::ceil((e1 - e0) / cell) + 2.0;
+    const double lim = a == 0 ? 1024.0 : 2048.0;
+    if (!(dim <= lim)) {
+      *why = "grid too fine for the box: at most 1024 x 2048 x 2048 cells of size h";
+      return false;
+    }
+    sc->dim[a] = static_cast<int>(dim);
+  }
+  return true;
+}
+
+void Handle::free_all() {
+  DeviceGuard g(device);
+  for (int k = 0; k < 2; ++k) {
+    if (graph[k]) cudaGraphExecDestroy(graph[k]);
+    graph[k] = nullptr;
+  }
+  void* ptrs[] = {b.pos[0], b.pos[1], b.disp[0], b.disp[1], b.xs[0], b.xs[1], b.vel[0], b.vel[1],
+                  b.omega, b.pred, b.lam, b.rho, b.rho_iter0, b.id[0], b.id[1], b.key, b.rank,
+                  b.perm, b.nbr_hdr, b.nbr_w, b.cell_count, b.cell_start, b.scan_tmp, b.scenes,
+                  b.stats, b.err, b.io, b.io2, scratch};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  b = Buffers();
+  scratch = nullptr;
+  scratch_bytes = 0;
+  if (stream) cudaStreamDestroy(stream);
+  stream = nullptr;
+}
+
+pbf_status Handle::alloc_all() {
+  const size_t n = b.n ? b.n : 1;
+  const size_t f4 = sizeof(float4) * n, u4 = sizeof(uint32_t) * n;
+  struct A {
+    void** p;
+    size_t bytes;
+  } list[] = {
+      {(void**)&b.pos[0], f4}, {(void**)&b.pos[1], f4}, {(void**)&b.disp[0], f4}, {(void**)&b.disp[1], f4},
+      {(void**)&b.xs[0], f4}, {(void**)&b.xs[1], f4}, {(void**)&b.vel[0], f4}, {(void**)&b.vel[1], f4},
+      {(void**)&b.omega, f4}, {(void**)&b.lam, u4}, {(void**)&b.rho, u4}, {(void**)&b.rho_iter0, u4},
+      {(void**)&b.id[0], u4}, {(void**)&b.id[1], u4}, {(void**)&b.key, u4}, {(void**)&b.rank, u4},
+      {(void**)&b.perm, u4}, {(void**)&b.nbr_hdr, sizeof(uint4) * n},
+      {(void**)&b.nbr_w, u4 * static_cast<size_t>(b.max_words)},
+      {(void**)&b.cell_count, sizeof(uint32_t) * b.n_cells},
+      {(void**)&b.cell_start, sizeof(uint32_t) * (b.n_cells + 1)},
+      {(void**)&b.scan_tmp, sizeof(uint32_t) * ((b.n_cells + 1023) / 1024 + 1)},
+      {(void**)&b.scenes, sizeof(SceneDesc) * b.n_scenes}, {(void**)&b.stats, sizeof(DevStats)},
+      {(void**)&b.err, sizeof(unsigned)}, {(void**)&b.io, 3 * sizeof(float) * n},
+      {(void**)&b.io2, 3 * sizeof(float) * n},
+  };
+  for (auto& a : list) {
+    pbf_status st = cuda(cudaMalloc(a.p, a.bytes), "cudaMalloc");
+    if (st != PBF_OK) return st;
+  }
+  if (params.flags & PBF_FLAG_KEEP_PREDICTED) {
+    pbf_status st = cuda(cudaMalloc((void**)&b.pred, f4), "cudaMalloc");
+    if (st != PBF_OK) return st;
+  }
+  return cuda(cudaMemsetAsync(b.err, 0, sizeof(unsigned), stream), "cudaMemsetAsync");
+}
+
+pbf_status Handle::ensure_scratch(size_t bytes) {
+  if (bytes <= scratch_bytes) return PBF_OK;
+  if (scratch) cudaFree(scratch);
+  scratch = nullptr;
+  scratch_bytes = 0;
+  pbf_status st = cuda(cudaMalloc(&scratch, bytes), "cudaMalloc(scratch)");
+  if (st == PBF_OK) scratch_bytes = bytes;
+  return st;
+}
+
+pbf_status Handle::sync_and_check() {
+  pbf_status st = cuda(cudaMemcpyAsync(&host_err_word, b.err, sizeof(unsigned), cudaMemcpyDeviceToHost, stream),
+                       "read error word");
+  if (st != PBF_OK) return st;
+  st = cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+  if (st != PBF_OK) return st;
+  if (host_err_word & PBF_ERRBIT_NONFINITE) return fail(PBF_ERR_NONFINITE, "a position or velocity became non-finite");
+  if (host_err_word & PBF_ERRBIT_NEIGHBOR_CAPACITY)
+    return fail(PBF_ERR_CAPACITY, "a particle had more neighbours than max_neighbors");
+  if (host_err_word & PBF_ERRBIT_ROW_CAPACITY)
+    return fail(PBF_ERR_CAPACITY, "more than 256 particles in one 3-cell row");
+  return PBF_OK;
+}
+
+pbf_status Handle::enqueue_steps(float dt, int nsteps) {
+  const bool use_graph = (params.flags & PBF_FLAG_GRAPH) != 0;
+  const bool keep_pred = b.pred != nullptr;
+  for (int k = 0; k < nsteps; ++k) {
+    if (use_graph) {
+      if (graph_dt != dt) {
+        for (int q = 0; q < 2; ++q) {
+          if (graph[q]) cudaGraphExecDestroy(graph[q]);
+          graph[q] = nullptr;
+        }
+        graph_dt = dt;
+      }
+      if (!graph[cur]) {
+        cudaGraph_t g = nullptr;
+        pbf_status st = cuda(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        if (st != PBF_OK) return st;
+        cudaError_t le = launch_step(b, dp, tune, cur, dt, params.iters, keep_pred, stream);
+        cudaError_t ee = cudaStreamEndCapture(stream, &g);
+        if (le != cudaSuccess) {
+          if (g) cudaGraphDestroy(g);
+          return cuda(le, "capture step");
+        }
+        st = cuda(ee, "end capture");
+        if (st != PBF_OK) return st;
+        st = cuda(cudaGraphInstantiate(&graph[cur], g, 0), "instantiate graph");
+        cudaGraphDestroy(g);
+        if (st != PBF_OK) return st;
+      }
+      pbf_status st = cuda(cudaGraphLaunch(graph[cur], stream), "cudaGraphLaunch");
+      if (st != PBF_OK) return st;
+    } else {
+      pbf_status st = cuda(launch_step(b, dp, tune, cur, dt, params.iters, keep_pred, stream), "launch step");
+      if (st != PBF_OK) return st;
+    }
+    cur ^= 1;
+    ++steps;
+  }
+  nbr_valid = nsteps > 0 || nbr_valid;
+  return PBF_OK;
+}
+
+void Handle::drop_graphs() {
+  for (int q = 0; q < 2; ++q) {
+    if (graph[q]) cudaGraphExecDestroy(graph[q]);
+    graph[q] = nullptr;
+  }
+  graph_dt = -1.f;
+}
+
+}  // namespace pbf
+
+using pbf::Handle;
+
+extern "C" {
+
+void pbf_params_default(pbf_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->h = 0.3;
+  p->h2 = 0.09;
+  p->iters = 12;
+  p->scorr_n = 4;
+  p->epsilon = 2;
+  p->scorr_k = 0.0001;
+  p->scorr_dq = 0.1;
+  p->vort_eps = 0.001;
+  p->xsph_c = 0.001;
+  p->dt = 0.016;
+  p->gravity[0] = 0;
+  p->gravity[1] = -10;
+  p->gravity[2] = 0;
+  p->rest_density = 1000.0;
+  p->box_lo[0] = -1; p->box_lo[1] = 0; p->box_lo[2] = -1;
+  p->box_hi[0] = 1; p->box_hi[1] = 1.5; p->box_hi[2] = 1;
+  p->box_open_mask = 0;
+  p->n_clip = 2;
+  p->clip_axis[0] = 2; p->clip_value[0] = 1.0;
+  p->clip_axis[1] = 1; p->clip_value[1] = 1.49;
+  p->clamp_lo[0] = -1; p->clamp_lo[1] = 0; p->clamp_lo[2] = -1;
+  p->clamp_hi[0] = 1; p->clamp_hi[1] = 1.49; p->clamp_hi[2] = 1;
+  p->max_neighbors = 128;
+  p->flags = PBF_FLAG_STATS;
+}
+
+int pbf_abi_version(void) { return PBF_ABI_VERSION; }
+
+pbf_status pbf_batch_create(const pbf_params* params, int n_scenes, const size_t* counts,
+                            const float* box_lo, const float* box_hi, const float* xyz, const float* vel,
+                            int device, pbf_handle** out) {
+  g_create_error.clear();
+  if (!out) {
+    g_create_error = "out is NULL";
+    return PBF_ERR_INVALID;
+  }
+  *out = nullptr;
+  if (!params || n_scenes < 1 || !counts) {
+    g_create_error = "params, counts and n_scenes >= 1 are required";
+    return PBF_ERR_INVALID;
+  }
+  size_t n = 0;
+  for (int s = 0; s < n_scenes; ++s) n += counts[s];
+  if (n > 0 && !xyz) {
+    g_create_error = "xyz is NULL";
+    return PBF_ERR_INVALID;
+  }
+  if (n >= (size_t(1) << 31)) {
+    g_create_error = "at most 2^31 - 1 particles";
+    return PBF_ERR_INVALID;
+  }
+  pbf::DevParams dp;
+  double cell;
+  std::string why;
+  if (!pbf::make_dev_params(*params, &dp, &cell, &why)) {
+    g_create_error = why;
+    return PBF_ERR_INVALID;
+  }
+  std::vector<pbf::SceneDesc> scenes(n_scenes);
+  uint64_t cells = 0, poff = 0;
+  for (int s = 0; s < n_scenes; ++s) {
+    float lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = box_lo ? box_lo[3 * s + a] : static_cast<float>(params->box_lo[a]);
+      hi[a] = box_hi ? box_hi[3 * s + a] : static_cast<float>(params->box_hi[a]);
+    }
+    if (!pbf::make_scene(*params, cell, lo, hi, &scenes[s], &why)) {
+      g_create_error = "scene " + std::to_string(s) + ": " + why;
+      return PBF_ERR_INVALID;
+    }
+    scenes[s].cell_off = static_cast<uint32_t>(cells);
+    scenes[s].p_off = static_cast<uint32_t>(poff);
+    scenes[s].p_cnt = static_cast<uint32_t>(counts[s]);
+    cells += static_cast<uint64_t>(scenes[s].dim[0]) * scenes[s].dim[1] * scenes[s].dim[2];
+    poff += counts[s];
+    if (cells >= (uint64_t(1) << 31)) {
+      g_create_error = "too many grid cells over all scenes";
+      return PBF_ERR_INVALID;
+    }
+  }
+  Handle* h = new (std::nothrow) Handle();
+  if (!h) {
+    g_create_error = "out of host memory";
+    return PBF_ERR_NOMEM;
+  }
+  h->device = device;
+  h->params = *params;
+  if (h->params.max_neighbors == 0) h->params.max_neighbors = 128;
+  h->dp = dp;
+  h->scenes_host = scenes;
+  h->b.n = n;
+  h->b.n_scenes = n_scenes;
+  h->b.n_cells = static_cast<uint32_t>(cells);
+  h->b.max_words = dp.max_words;
+  pbf::DeviceGuard g(device);
+  pbf_status st = h->cuda(cudaSetDevice(device), "cudaSetDevice");
+  if (st == PBF_OK) st = h->cuda(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
+  if (st == PBF_OK) st = h->alloc_all();
+  if (st == PBF_OK)
+    st = h->cuda(cudaMemcpyAsync(h->b.scenes, scenes.data(), sizeof(pbf::SceneDesc) * n_scenes,
+                                 cudaMemcpyHostToDevice, h->stream),
+                 "upload scenes");
+  if (st == PBF_OK && n > 0) {
+    st = h->cuda(cudaMemcpyAsync(h->b.io, xyz, 3 * sizeof(float) * n, cudaMemcpyHostToDevice, h->stream),
+                 "upload positions");
+    if (st == PBF_OK && vel)
+      st = h->cuda(cudaMemcpyAsync(h->b.io2, vel, 3 * sizeof(float) * n, cudaMemcpyHostToDevice, h->stream),
+                   "upload velocities");
+    if (st == PBF_OK)
+      st = h->cuda(pbf::launch_upload(h->b, 0, h->b.io, vel ? h->b.io2 : nullptr, nullptr, h->stream),
+                   "upload kernel");
+    if (st == PBF_OK)
+      st = h->cuda(cudaMemsetAsync(h->b.rho, 0, sizeof(float) * n, h->stream), "memset");
+  }
+  if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+  if (st != PBF_OK) {
+    g_create_error = h->err;
+    h->free_all();
+    delete h;
+    return st;
+  }
+  *out = reinterpret_cast<pbf_handle*>(h);
+  return PBF_OK;
+}
+
+pbf_status pbf_create(const pbf_params* params, size_t n, const float* xyz, const float* vel, int device,
+                      pbf_handle** out) {
+  return pbf_batch_create(params, 1, &n, nullptr, nullptr, xyz, vel, device, out);
+}
+
+pbf_status pbf_destroy(pbf_handle* hh) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  h->free_all();
+  delete h;
+  return PBF_OK;
+}
+
+pbf_status pbf_step(pbf_handle* hh, double dt, int nsteps) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (nsteps < 0) return h->fail(PBF_ERR_INVALID, "nsteps must be >= 0");
+  const double d = dt > 0 ? dt : h->params.dt;
+  if (!(d > 0) || !std::isfinite(d)) return h->fail(PBF_ERR_INVALID, "dt must be positive");
+  pbf::DeviceGuard g(h->device);
+  pbf_status st = h->enqueue_steps(static_cast<float>(d), nsteps);
+  if (st != PBF_OK) return st;
+  h->simulate_time += d * nsteps;
+  return h->sync_and_check();
+}
+
+pbf_status pbf_step_async(pbf_handle* hh, double dt, int nsteps) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (nsteps < 0) return h->fail(PBF_ERR_INVALID, "nsteps must be >= 0");
+  const double d = dt > 0 ? dt : h->params.dt;
+  if (!(d > 0) || !std::isfinite(d)) return h->fail(PBF_ERR_INVALID, "dt must be positive");
+  pbf::DeviceGuard g(h->device);
+  pbf_status st = h->enqueue_steps(static_cast<float>(d), nsteps);
+  if (st == PBF_OK) h->simulate_time += d * nsteps;
+  return st;
+}
+
+pbf_status pbf_sync(pbf_handle* hh) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  pbf::DeviceGuard g(h->device);
+  return h->sync_and_check();
+}
+
+void* pbf_stream(pbf_handle* hh) {
+  return hh ? reinterpret_cast<void*>(reinterpret_cast<Handle*>(hh)->stream) : nullptr;
+}
+
+static pbf_status download(Handle* h, float* xyz, float* vel, float* rho) {
+  pbf::DeviceGuard g(h->device);
+  const size_t n = h->b.n;
+  if (n == 0) return PBF_OK;
+  pbf_status st = PBF_OK;
+  if (xyz) {
+    st = h->cuda(pbf::launch_download(h->b, h->cur, h->b.io, nullptr, nullptr, h->stream), "download");
+    if (st == PBF_OK)
+      st = h->cuda(cudaMemcpyAsync(xyz, h->b.io, 3 * sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
+  }
+  if (st == PBF_OK && vel) {
+    st = h->cuda(pbf::launch_download(h->b, h->cur, nullptr, h->b.io2, nullptr, h->stream), "download");
+    if (st == PBF_OK)
+      st = h->cuda(cudaMemcpyAsync(vel, h->b.io2, 3 * sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
+  }
+  if (st == PBF_OK && rho) {
+    float* tmp = reinterpret_cast<float*>(h->b.disp[0]);  // scratch between steps
+    st = h->cuda(pbf::launch_download(h->b, h->cur, nullptr, nullptr, tmp, h->stream), "download");
+    if (st == PBF_OK)
+      st = h->cuda(cudaMemcpyAsync(rho, tmp, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
+  }
+  if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+  return st;
+}
+
+pbf_status pbf_get_positions(pbf_handle* hh, float* xyz) {
+  if (!hh || !xyz) return PBF_ERR_INVALID;
+  return download(reinterpret_cast<Handle*>(hh), xyz, nullptr, nullptr);
+}
+
+pbf_status pbf_get_velocities(pbf_handle* hh, float* vel) {
+  if (!hh || !vel) return PBF_ERR_INVALID;
+  return download(reinterpret_cast<Handle*>(hh), nullptr, vel, nullptr);
+}
+
+pbf_status pbf_get_densities(pbf_handle* hh, float* rho) {
+  if (!hh || !rho) return PBF_ERR_INVALID;
+  return download(reinterpret_cast<Handle*>(hh), nullptr, nullptr, rho);
+}
+
+pbf_status pbf_set_state(pbf_handle* hh, const float* xyz, const float* vel) {
+  if (!hh || (!xyz && reinterpret_cast<Handle*>(hh)->b.n)) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  pbf::DeviceGuard g(h->device);
+  const size_t n = h->b.n;
+  if (n == 0) return PBF_OK;
+  pbf_status st = h->cuda(cudaMemcpyAsync(h->b.io, xyz, 3 * sizeof(float) * n, cudaMemcpyHostToDevice, h->stream),
+                          "H2D");
+  if (st == PBF_OK && vel)
+    st = h->cuda(cudaMemcpyAsync(h->b.io2, vel, 3 * sizeof(float) * n, cudaMemcpyHostToDevice, h->stream), "H2D");
+  if (st == PBF_OK)
+    st = h->cuda(pbf::launch_upload(h->b, h->cur, h->b.io, vel ? h->b.io2 : nullptr, nullptr, h->stream), "upload");
+  if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+  h->nbr_valid = false;
+  return st;
+}
+
+pbf_status pbf_set_state_device(pbf_handle* hh, const float* xyz, const float* vel, void* stream) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!xyz && h->b.n) return h->fail(PBF_ERR_INVALID, "xyz is NULL");
+  pbf::DeviceGuard g(h->device);
+  pbf_status st = h->join_from(static_cast<cudaStream_t>(stream));
+  if (st == PBF_OK)
+    st = h->cuda(pbf::launch_upload(h->b, h->cur, xyz, vel, nullptr, h->stream), "upload");
+  if (st == PBF_OK) st = h->join_to(static_cast<cudaStream_t>(stream));
+  h->nbr_valid = false;
+  return st;
+}
+
+pbf_status pbf_get_state_device(pbf_handle* hh, float* xyz, float* vel, float* rho, void* stream) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  pbf::DeviceGuard g(h->device);
+  pbf_status st = h->join_from(static_cast<cudaStream_t>(stream));
+  if (st == PBF_OK)
+    st = h->cuda(pbf::launch_download(h->b, h->cur, xyz, vel, rho, h->stream), "download");
+  if (st == PBF_OK) st = h->join_to(static_cast<cudaStream_t>(stream));
+  return st;
+}
+
+pbf_status pbf_estimate_densities(pbf_handle* hh, float* rho) {
+  if (!hh || !rho) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  pbf::DeviceGuard g(h->device);
+  if (h->b.n == 0) return PBF_OK;
+  pbf_status st = h->cuda(pbf::launch_resort(h->b, h->dp, h->tune, h->cur, h->stream), "resort");
+  if (st != PBF_OK) return st;
+  h->cur ^= 1;
+  h->nbr_valid = false;
+  h->drop_graphs();
+  st = h->cuda(pbf::launch_density_self(h->b, h->dp, h->tune, h->cur, h->b.rho, h->stream), "density");
+  if (st != PBF_OK) return st;
+  return download(h, nullptr, nullptr, rho);
+}
+
+pbf_status pbf_estimate_density_at(pbf_handle* hh, size_t m, const float* pts, float* out) {
+  if (!hh || (m && (!pts || !out))) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (h->b.n_scenes != 1) return h->fail(PBF_ERR_INVALID, "density queries need a single-scene handle");
+  if (m == 0) return PBF_OK;
+  pbf::DeviceGuard g(h->device);
+  pbf_status st = h->ensure_scratch(2 * 3 * sizeof(float) * m);
+  if (st != PBF_OK) return st;
+  float* dpts = static_cast<float*>(h->scratch);
+  float* dout = dpts + 3 * m;
+  if (h->b.n) {
+    st = h->cuda(pbf::launch_resort(h->b, h->dp, h->tune, h->cur, h->stream), "resort");
+    if (st != PBF_OK) return st;
+    h->cur ^= 1;
+    h->nbr_valid = false;
+    h->drop_graphs();
+  }
+  st = h->cuda(cudaMemcpyAsync(dpts, pts, 3 * sizeof(float) * m, cudaMemcpyHostToDevice, h->stream), "H2D");
+  if (st != PBF_OK) return st;
+  if (h->b.n) {
+    st = h->cuda(pbf::launch_density_at(h->b, h->dp, h->cur, m, dpts, dout, h->stream), "density_at");
+  } else {
+    st = h->cuda(cudaMemsetAsync(dout, 0, sizeof(float) * m, h->stream), "memset");
+  }
+  if (st == PBF_OK)
+    st = h->cuda(cudaMemcpyAsync(out, dout, sizeof(float) * m, cudaMemcpyDeviceToHost, h->stream), "D2H");
+  if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+  return st;
+}
+
+pbf_status pbf_get_stats(pbf_handle* hh, pbf_stats* out) {
+  if (!hh || !out) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  pbf::DeviceGuard g(h->device);
+  std::memset(out, 0, sizeof(*out));
+  out->steps = h->steps;
+  pbf::DevStats ds;
+  std::memset(&ds, 0, sizeof(ds));
+  unsigned errw = 0;
+  pbf_status st = h->cuda(cudaMemcpyAsync(&ds, h->b.stats, sizeof(ds), cudaMemcpyDeviceToHost, h->stream), "D2H");
+  if (st == PBF_OK)
+    st = h->cuda(cudaMemcpyAsync(&errw, h->b.err, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream), "D2H");
+  if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+  if (st != PBF_OK) return st;
+  out->error_flags = errw;
+  if (!h->dp.stats || h->steps == 0 || h->b.n == 0) return PBF_OK;
+  const double n = static_cast<double>(h->b.n);
+  out->mean_density_iter0 = ds.rho_iter0_sum / n;
+  out->mean_density = ds.rho_sum / n;
+  out->mean_density_error = ds.err_sum / n;
+  float em;
+  std::memcpy(&em, &ds.err_max_bits, sizeof(em));
+  out->max_density_error = em;
+  out->min_neighbors = ds.nbr_min;
+  out->max_neighbors = ds.nbr_max;
+  out->mean_neighbors = static_cast<double>(ds.nbr_sum) / n;
+  out->low_neighbor_count = ds.low_cnt;
+  return PBF_OK;
+}
+
+pbf_status pbf_get_neighbors(pbf_handle* hh, uint32_t* counts, uint32_t* ids, size_t cap, size_t* total) {
+  if (!hh || !counts) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h->nbr_valid) return h->fail(PBF_ERR_INVALID, "no neighbour lists: step first");
+  pbf::DeviceGuard g(h->device);
+  const size_t n = h->b.n;
+  if (n == 0) {
+    if (total) *total = 0;
+    return PBF_OK;
+  }
+  pbf_status st = h->ensure_scratch(sizeof(uint32_t) * (2 * n + 1));
+  if (st != PBF_OK) return st;
+  uint32_t* dcounts = static_cast<uint32_t*>(h->scratch);
+  st = h->cuda(pbf::launch_neighbor_counts(h->b, h->cur, dcounts, h->stream), "counts");
+  if (st == PBF_OK)
+    st = h->cuda(cudaMemcpyAsync(counts, dcounts, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
+  if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "sync");
+  if (st != PBF_OK) return st;
+  std::vector<uint32_t> off(n + 1, 0);
+  for (size_t i = 0; i < n; ++i) off[i + 1] = off[i] + counts[i];
+  if (total) *total = off[n];
+  if (!ids) return PBF_OK;
+  if (off[n] > cap) return h->fail(PBF_ERR_INVALID, "ids capacity too small");
+  st = h->ensure_scratch(sizeof(uint32_t) * (n + 1 + static_cast<size_t>(off[n])));
+  if (st != PBF_OK) return st;
+  uint32_t* doff = static_cast<uint32_t*>(h->scratch);
+  uint32_t* dids = doff + n + 1;
+  st = h->cuda(cudaMemcpyAsync(doff, off.data(), sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, h->stream), "H2D");
+  if (st == PBF_OK) st = h->cuda(pbf::launch_neighbor_ids(h->b, h->cur, doff, dids, h->stream), "ids");
+  if (st == PBF_OK && off[n])
+    st = h->cuda(cudaMemcpyAsync(ids, dids, sizeof(uint32_t) * off[n], cudaMemcpyDeviceToHost, h->stream), "D2H");
+  if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "sync");
+  if (st != PBF_OK) return st;
+  for (size_t i = 0; i < n; ++i) std::sort(ids + off[i], ids + off[i + 1]);
+  return PBF_OK;
+}
+
+pbf_status pbf_get_cells(pbf_handle* hh, uint32_t* cells) {
+  if (!hh || !cells) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h->nbr_valid || !h->b.pred) return h->fail(PBF_ERR_INVALID, "needs a step taken with PBF_FLAG_KEEP_PREDICTED");
+  pbf::DeviceGuard g(h->device);
+  const size_t n = h->b.n;
+  if (n == 0) return PBF_OK;
+  pbf_status st = h->ensure_scratch(sizeof(uint32_t) * n);
+  if (st != PBF_OK) return st;
+  uint32_t* d = static_cast<uint32_t*>(h->scratch);
+  st = h->cuda(pbf::launch_cells_of(h->b, h->dp, h->cur, d, h->stream), "cells");
+  if (st == PBF_OK) st = h->cuda(cudaMemcpyAsync(cells, d, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
+  if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "sync");
+  return st;
+}
+
+pbf_status pbf_get_predicted(pbf_handle* hh, float* xyz) {
+  if (!hh || !xyz) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h->nbr_valid || !h->b.pred) return h->fail(PBF_ERR_INVALID, "needs a step taken with PBF_FLAG_KEEP_PREDICTED");
+  pbf::DeviceGuard g(h->device);
+  const size_t n = h->b.n;
+  if (n == 0) return PBF_OK;
+  pbf_status st = h->cuda(pbf::launch_unsort_f4(h->b, h->cur, h->b.pred, h->b.io, h->stream), "unsort");
+  if (st == PBF_OK) st = h->cuda(cudaMemcpyAsync(xyz, h->b.io, 3 * sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
+  if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "sync");
+  return st;
+}
+
+size_t pbf_size(const pbf_handle* hh) { return hh ? reinterpret_cast<const Handle*>(hh)->b.n : 0; }
+
+int pbf_num_scenes(const pbf_handle* hh) { return hh ? reinterpret_cast<const Handle*>(hh)->b.n_scenes : 0; }
+
+const char* pbf_last_error(const pbf_handle* hh) {
+  if (!hh) return g_create_error.c_str();
+  return reinterpret_cast<const Handle*>(hh)->err.c_str();
+}
+
+}  // extern "C"

@@ -1,0 +1,201 @@
+// Device-side building blocks of the PBF step: vector helpers, the SPH
+// kernels of the reference, the box collider and the compressed neighbour
+// iteration. Included by every PBF translation unit.
+#pragma once
+
+#include <cstdint>
+
+#include "pbf_internal.h"
+
+namespace pbf {
+
+__device__ __forceinline__ float3 f3(const float4& a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float c) { return make_float3(a.x * c, a.y * c, a.z * c); }
+__device__ __forceinline__ float3 operator*(float c, float3 a) { return make_float3(a.x * c, a.y * c, a.z * c); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross3(float3 u, float3 v) {
+  return make_float3(u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x);
+}
+__device__ __forceinline__ float cmp3(const float3& v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
+__device__ __forceinline__ void set3(float3& v, int a, float x) {
+  if (a == 0) v.x = x; else if (a == 1) v.y = x; else v.z = x;
+}
+
+// Exactly rounded |a - b|^2 with no contraction: the neighbour predicate of
+// particles.cpp:260 evaluated in FP32 (a host check can repeat it bit for bit).
+__device__ __forceinline__ float dist2_rn(const float4& a, const float4& b) {
+  const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// Cell of x* within its scene's grid: floor((x - origin) * inv_cell), clamped.
+struct CellCoord {
+  int x, y, z;
+};
+__device__ __forceinline__ CellCoord cell_of(const float3 p, const SceneDesc& sc, float inv_cell) {
+  float c[3] = {p.x, p.y, p.z};
+  int out[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float f = floorf(__fmul_rn(__fsub_rn(c[a], sc.origin[a]), inv_cell));
+    f = fminf(fmaxf(f, 0.0f), static_cast<float>(sc.dim[a] - 1));
+    out[a] = static_cast<int>(f);
+  }
+  return CellCoord{out[0], out[1], out[2]};
+}
+__device__ __forceinline__ uint32_t cell_key(const CellCoord& c, const SceneDesc& sc) {
+  return sc.cell_off + static_cast<uint32_t>((c.z * sc.dim[1] + c.y) * sc.dim[0] + c.x);
+}
+__device__ __forceinline__ uint32_t pack_coord(const CellCoord& c) {
+  return static_cast<uint32_t>(c.x) | (static_cast<uint32_t>(c.y) << 10) |
+         (static_cast<uint32_t>(c.z) << 21);
+}
+
+// ---- collider ------------------------------------------------------------------
+// Nearest wall of the scene box hit by the segment p + t*dir, t in [0, l]
+// (walls facing the motion only; a point already outside a wall it moves
+// away from is stopped at once). Returns t; *wall = 2*axis+side or -1.
+__device__ __forceinline__ float wall_hit(const float3 p, const float3 dir, float l,
+                                          const SceneDesc& sc, int open_mask, int* wall) {
+  float t = l;
+  int w = -1;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float da = cmp3(dir, a);
+    const float pa = cmp3(p, a);
+    if (da < 0.0f) {
+      if (!(open_mask & (1 << (2 * a)))) {
+        const float tt = fmaxf((sc.lo[a] - pa) / da, 0.0f);
+        if (tt <= t) { t = tt; w = 2 * a; }
+      }
+    } else if (da > 0.0f) {
+      if (!(open_mask & (1 << (2 * a + 1)))) {
+        const float tt = fmaxf((sc.hi[a] - pa) / da, 0.0f);
+        if (tt <= t) { t = tt; w = 2 * a + 1; }
+      }
+    }
+  }
+  *wall = w;
+  return t;
+}
+
+__device__ __forceinline__ float wall_value(const SceneDesc& sc, int wall) {
+  return (wall & 1) ? sc.hi[wall >> 1] : sc.lo[wall >> 1];
+}
+
+// Move x* = x + d by `delta` against the collider, in displacement form: d is
+// updated, x is fixed. Follows clamp (slide = false, particles.cpp:51-84) and
+// clamp_response (slide = true, particles.cpp:87-132): clip planes first, the
+// nearest wall stops the move (the stopped coordinate is placed exactly on
+// the wall), the predict move slides once along the wall for half the
+// remaining length unless a clip plane was crossed, then the clamp box.
+__device__ __forceinline__ void collide(const float3 x, float3& d, const float3 delta, bool slide,
+                                        const SceneDesc& sc, const DevParams& P) {
+  const float3 p = x + d;
+  float l = sqrtf(delta.x * delta.x + delta.y * delta.y + delta.z * delta.z);
+  if (!(l > kEps)) return;  // particles.cpp:53-55 / 90-92: no move, no clamp
+  const float3 dir = delta * (1.0f / l);
+  const float total = l;
+  bool intersect = false;
+  for (int c = 0; c < P.n_clip; ++c) {
+    const int a = P.clip_axis[c];
+    const float da = cmp3(dir, a);
+    if (da != 0.0f) {
+      const float pt = (P.clip_value[c] - cmp3(p, a)) / da;
+      if (pt > 0.0f && pt < l) { l = pt; intersect = true; }
+    }
+  }
+  int wall;
+  const float t = wall_hit(p, dir, l, sc, P.open_mask, &wall);
+  if (wall >= 0 || intersect) {
+    float3 nd = d + dir * t;
+    if (wall >= 0) set3(nd, wall >> 1, wall_value(sc, wall) - cmp3(x, wall >> 1));
+    if (slide && wall >= 0 && !intersect) {
+      const int a = wall >> 1;
+      const float n_dot = (wall & 1) ? -cmp3(dir, a) : cmp3(dir, a);  // dot(dir, inward normal)
+      if (n_dot > -1.0f) {
+        float3 tan = delta;
+        set3(tan, a, 0.0f);
+        const float tl = sqrtf(dot3(tan, tan));
+        if (tl > 0.0f) {
+          const float3 dir2 = tan * (1.0f / tl);
+          const float l2 = (total - t) * 0.5f;
+          int wall2;
+          const float t2 = wall_hit(x + nd, dir2, l2, sc, P.open_mask, &wall2);
+          nd = nd + dir2 * t2;
+          if (wall2 >= 0) set3(nd, wall2 >> 1, wall_value(sc, wall2) - cmp3(x, wall2 >> 1));
+        }
+      }
+    }
+    d = nd;
+  } else {
+    d = d + delta;
+  }
+  const float3 q = x + d;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float qa = cmp3(q, a);
+    if (qa < P.clamp_lo[a]) set3(d, a, P.clamp_lo[a] - cmp3(x, a));
+    else if (qa > P.clamp_hi[a]) set3(d, a, P.clamp_hi[a] - cmp3(x, a));
+  }
+}
+
+// ---- neighbour lists -----------------------------------------------------------
+// A particle's neighbours lie in the 9 rows (dz, dy) of 3 consecutive cells
+// (cx-1..cx+1) around its cell; each row is a contiguous slot range of the
+// cell-sorted arrays. A neighbour is stored as a u8 offset from its row's first
+// slot; hdr holds the 9 row counts (bytes), the total (hdr.z bits 8-15) and the
+// packed cell coordinates (hdr.w).
+__device__ __forceinline__ int row_count(const uint4& h, int r) {
+  const uint32_t w = r < 4 ? h.x : (r < 8 ? h.y : h.z);
+  return static_cast<int>((w >> (8 * (r & 3))) & 0xffu);
+}
+__device__ __forceinline__ int nbr_total(const uint4& h) { return static_cast<int>((h.z >> 8) & 0xffu); }
+
+// Calls f(j) for every neighbour slot j of slot i, ascending.
+template <typename F>
+__device__ __forceinline__ void for_each_neighbor(int i, int n, const uint4 h,
+                                                  const uint32_t* __restrict__ words,
+                                                  const uint32_t* __restrict__ cell_start,
+                                                  const SceneDesc& sc, F&& f) {
+  const int cx = static_cast<int>(h.w & 1023u);
+  const int cy = static_cast<int>((h.w >> 10) & 2047u);
+  const int cz = static_cast<int>(h.w >> 21);
+  const int x0 = cx > 0 ? cx - 1 : 0;
+  uint32_t base[9];
+#pragma unroll
+  for (int r = 0; r < 9; ++r) {
+    const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
+    base[r] = row_count(h, r)
+                  ? __ldg(&cell_start[sc.cell_off + static_cast<uint32_t>((z * sc.dim[1] + y) * sc.dim[0] + x0)])
+                  : 0u;
+  }
+  int k = 0;
+  uint32_t word = 0;
+#pragma unroll
+  for (int r = 0; r < 9; ++r) {
+    const int c = row_count(h, r);
+    for (int t = 0; t < c; ++t, ++k) {
+      if ((k & 3) == 0) word = __ldg(&words[static_cast<size_t>(k >> 2) * n + i]);
+      const uint32_t j = base[r] + ((word >> ((k & 3) * 8)) & 0xffu);
+      f(j);
+    }
+  }
+}
+
+// Spiky gradient factor s with grad W(r) = spiky_c * s * r (particles.cpp:143-149);
+// returns false outside [EPS_D, h).
+__device__ __forceinline__ bool spiky_s(float r2, float h, float* s) {
+  const float rinv = rsqrtf(r2);
+  const float rl = r2 * rinv;
+  if (!(rl < h && rl >= kEps)) return false;
+  const float hr = h - rl;
+  *s = hr * hr * rinv;
+  return true;
+}
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+}  // namespace pbf

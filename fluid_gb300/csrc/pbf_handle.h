@@ -1,0 +1,71 @@
+// The object behind a pbf_handle*: parameters, device buffers, stream, graphs.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "pbf_internal.h"
+
+namespace pbf {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev);
+  ~DeviceGuard();
+};
+
+bool make_dev_params(const pbf_params& p, DevParams* d, double* cell_out, std::string* why);
+bool make_scene(const pbf_params& p, double cell, const float* lo, const float* hi, SceneDesc* sc,
+                std::string* why);
+
+struct Handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  pbf_params params{};
+  DevParams dp{};
+  Buffers b;
+  Tuning tune;
+  std::vector<SceneDesc> scenes_host;
+  int cur = 0;               // buffers holding the current state
+  uint64_t steps = 0;
+  double simulate_time = 0;  // Particles::simulate_time
+  bool nbr_valid = false;    // neighbour lists / x* copy describe the current order
+  std::string err;
+  unsigned host_err_word = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one step starting from buffers 0 / 1
+  float graph_dt = -1.f;
+  void* scratch = nullptr;   // grow-only scratch for introspection and queries
+  size_t scratch_bytes = 0;
+
+  pbf_status fail(pbf_status st, const std::string& msg);
+  pbf_status cuda(cudaError_t e, const char* what);
+  pbf_status alloc_all();
+  void free_all();
+  pbf_status ensure_scratch(size_t bytes);
+  pbf_status enqueue_steps(float dt, int nsteps);
+  pbf_status sync_and_check();
+  void drop_graphs();
+
+  // Order the handle's stream after `other` (or the legacy default stream
+  // when other is null), and back.
+  pbf_status join_from(cudaStream_t other) {
+    cudaEvent_t ev;
+    pbf_status st = cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+    if (st != PBF_OK) return st;
+    st = cuda(cudaEventRecord(ev, other), "event record");
+    if (st == PBF_OK) st = cuda(cudaStreamWaitEvent(stream, ev, 0), "stream wait");
+    cudaEventDestroy(ev);
+    return st;
+  }
+  pbf_status join_to(cudaStream_t other) {
+    cudaEvent_t ev;
+    pbf_status st = cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+    if (st != PBF_OK) return st;
+    st = cuda(cudaEventRecord(ev, stream), "event record");
+    if (st == PBF_OK) st = cuda(cudaStreamWaitEvent(other, ev, 0), "stream wait");
+    cudaEventDestroy(ev);
+    return st;
+  }
+};
+
+}  // namespace pbf

@@ -1,0 +1,132 @@
+// Internal types shared by the PBF CUDA translation units.
+//
+// Data layout in HBM (N particles, C cells over all scenes), all arrays in the
+// cell-sorted order of the current step unless noted:
+//   pos    float4  x (w: scene id as int bits)             16 B
+//   disp   float4  delta = x* - x (displacement form)       16 B
+//   xs[2]  float4  x* ping-pong over the Jacobi iterations  16 B each
+//   vel    float4  v                                        16 B
+//   omega  float4  vorticity (w: |omega|)                   16 B
+//   lam    float   lambda                                    4 B
+//   rho    float   reported density                          4 B
+//   id     u32     original particle index                   4 B
+//   nbr_hdr uint4  9 row counts (u8), total (u8), packed cell coords
+//   nbr_w   u32    [words][N] neighbour offsets, 4 x u8 per word, word-major
+//   cell_count / cell_start u32 [C] / [C+1]
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "../../include/pbf.h"
+
+namespace pbf {
+
+constexpr int kMaxRowCandidates = 256;  // u8 offsets within one 3-cell row
+constexpr int kNeighborAlert = 18;      // NUM_NEIGHBOR_ALERT_THRESHOLD, particles.cpp:32
+constexpr float kEps = 1e-11f;          // EPS_D, CGL/include/CGL/misc.h:11
+
+// Per-scene collider and grid (device table, one entry per scene).
+struct SceneDesc {
+  float lo[3], hi[3];       // collider walls
+  float origin[3];          // grid origin
+  int dim[3];               // grid cells per axis
+  uint32_t cell_off;        // first global cell id
+  uint32_t p_off, p_cnt;    // particle range in original order
+  uint32_t pad;
+};
+
+// Uniform physics parameters in FP32, derived on the host from pbf_params.
+struct DevParams {
+  float h, h2, inv_cell, cell;
+  float poly6_c;     // 1.56668147106 / h^9            (particles.cpp:140)
+  float spiky_c;     // -3 * 4.774648292756860 / h^6  (particles.cpp:148)
+  float tis;         // 1 / W(scorr_dq * h)           (particles.cpp:151)
+  float scorr_k, epsilon, rest_density, inv_rho0;
+  float xsph_c, vort_eps;
+  float g[3];
+  float clip_value[2];
+  float clamp_lo[3], clamp_hi[3];
+  int scorr_n, n_clip, clip_axis[2], open_mask, max_words;
+  int stats;
+};
+
+// Step statistics accumulated on the device (reset every step).
+struct DevStats {
+  double rho_iter0_sum;
+  double rho_sum;
+  double err_sum;
+  unsigned int err_max_bits;   // float bits of max |rho/rho0 - 1| (non-negative)
+  unsigned int nbr_min;
+  unsigned int nbr_max;
+  unsigned int pad;
+  unsigned long long nbr_sum;
+  unsigned long long low_cnt;
+};
+
+struct Buffers {
+  size_t n = 0;
+  int n_scenes = 0;
+  uint32_t n_cells = 0;
+  int max_words = 0;
+  float4* pos[2] = {nullptr, nullptr};
+  float4* disp[2] = {nullptr, nullptr};
+  float4* xs[2] = {nullptr, nullptr};
+  float4* vel[2] = {nullptr, nullptr};
+  float4* omega = nullptr;
+  float4* pred = nullptr;  // optional copy of x* after prediction (sorted order)
+  float* lam = nullptr;
+  float* rho = nullptr;
+  float* rho_iter0 = nullptr;  // density after the first lambda pass (stats)
+  uint32_t* id[2] = {nullptr, nullptr};
+  uint32_t* key = nullptr;
+  uint32_t* rank = nullptr;
+  uint32_t* perm = nullptr;
+  uint4* nbr_hdr = nullptr;
+  uint32_t* nbr_w = nullptr;
+  uint32_t* cell_count = nullptr;
+  uint32_t* cell_start = nullptr;  // n_cells + 1
+  uint32_t* scan_tmp = nullptr;    // block sums
+  SceneDesc* scenes = nullptr;
+  DevStats* stats = nullptr;
+  unsigned int* err = nullptr;     // sticky PBF_ERRBIT_* word
+  float* io = nullptr;             // (n, 3) staging for host/device packed transfers
+  float* io2 = nullptr;
+};
+
+// Launch shapes picked by the autotuner (threads per block per kernel family).
+struct Tuning {
+  int block_predict = 256;
+  int block_nbr = 128;
+  int block_solve = 128;
+  int block_misc = 256;
+};
+
+// ---- launchers (pbf_kernels.cu) ----
+// cur: index of the buffers holding the current (sorted) state; the step
+// writes the next state into 1 - cur.
+cudaError_t launch_step(const Buffers& b, const DevParams& p, const Tuning& t, int cur,
+                        float dt, int iters, bool keep_pred, cudaStream_t s);
+cudaError_t launch_resort(const Buffers& b, const DevParams& p, const Tuning& t, int cur,
+                          cudaStream_t s);
+cudaError_t launch_upload(const Buffers& b, int cur, const float* xyz, const float* vel,
+                          const uint32_t* scene_of, cudaStream_t s);
+cudaError_t launch_download(const Buffers& b, int cur, float* xyz, float* vel, float* rho,
+                            cudaStream_t s);
+cudaError_t launch_unsort_u32(const Buffers& b, int cur, const uint32_t* src, uint32_t* dst,
+                              cudaStream_t s);
+cudaError_t launch_unsort_f4(const Buffers& b, int cur, const float4* src, float* dst_xyz,
+                             cudaStream_t s);
+cudaError_t launch_cells_of(const Buffers& b, const DevParams& p, int cur, uint32_t* cells,
+                            cudaStream_t s);
+cudaError_t launch_neighbor_ids(const Buffers& b, int cur, const uint32_t* offsets,
+                                uint32_t* ids, cudaStream_t s);
+cudaError_t launch_neighbor_counts(const Buffers& b, int cur, uint32_t* counts, cudaStream_t s);
+cudaError_t launch_density_self(const Buffers& b, const DevParams& p, const Tuning& t, int cur,
+                                float* rho_sorted, cudaStream_t s);
+cudaError_t launch_density_at(const Buffers& b, const DevParams& p, int cur, size_t m,
+                              const float* pts, float* out, cudaStream_t s);
+
+}  // namespace pbf

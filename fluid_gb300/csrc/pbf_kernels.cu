@@ -1,0 +1,779 @@
+// PBF step kernels for sm_103a (FP32 on CUDA cores; the step is a sparse
+// stencil with no dense contraction, so no tensor cores).
+//
+// One step (Particles::timeStep, particles.cpp:250-297) is this launch chain
+// on one stream; every phase covers all scenes of a batch in one launch:
+//   k_predict     gravity + predicted move + collision, cell key, per-cell
+//                 count and rank (particles.cpp:175-183, 87-132)
+//   k_scan_*      exclusive prefix sum of the cell counts
+//   k_scatter     slot = cell start + rank
+//   k_cellsort    order each cell's slots by original index (determinism)
+//   k_gather      reorder x, delta, id into cell order; x* = x + delta
+//   k_nbr_build   neighbour sets |x*_i - x*_j|^2 <= H2 over the 27 cells,
+//                 stored row-compressed (particles.cpp:258-265)
+//   k_lambda      density + lambda            (particles.cpp:185-204)   x iters
+//   k_deltap      delta p + collision         (particles.cpp:206-213)   x iters
+//   k_xsph        velocity, vorticity, XSPH, reported density
+//                 (particles.cpp:215-234, order-independent form)
+//   k_vort        vorticity confinement, x <- x* (particles.cpp:236-248)
+#include <cfloat>
+#include <climits>
+#include <cstdint>
+
+#include "pbf_device.cuh"
+
+namespace pbf {
+namespace {
+
+constexpr int kScanItems = 4;
+constexpr int kScanThreads = 256;
+constexpr int kScanTile = kScanItems * kScanThreads;
+constexpr uint32_t kMaxSortedCell = 256;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ int scene_of_slot(const float4& p) { return __float_as_int(p.w); }
+
+// ---------------------------------------------------------------------------
+// prediction + cell count
+// ---------------------------------------------------------------------------
+__global__ void k_predict(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                          float4* __restrict__ disp_out, uint32_t* __restrict__ key_out,
+                          uint32_t* __restrict__ rank_out, uint32_t* __restrict__ cell_count,
+                          const SceneDesc* __restrict__ scenes, DevParams P, float dt, int move,
+                          int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i < n;
+  uint32_t key = 0xffffffffu;
+  if (live) {
+    const float4 x4 = pos[i];
+    const SceneDesc& sc = scenes[scene_of_slot(x4)];
+    const float3 x = f3(x4);
+    float3 d = make_float3(0.f, 0.f, 0.f);
+    if (move) {
+      const float4 v4 = vel[i];
+      // applyForceVelocity, particles.cpp:180: v += g dt
+      const float3 v = make_float3(v4.x + P.g[0] * dt, v4.y + P.g[1] * dt, v4.z + P.g[2] * dt);
+      collide(x, d, v * dt, true, sc, P);
+      disp_out[i] = make_float4(d.x, d.y, d.z, 0.f);
+    }
+    key = cell_key(cell_of(x + d, sc, P.inv_cell), sc);
+    key_out[i] = key;
+  }
+  // warp-aggregated per-cell rank
+  const unsigned active = __ballot_sync(0xffffffffu, live);
+  if (!live) return;
+  const unsigned peers = __match_any_sync(active, key);
+  const int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (static_cast<int>(lane_id()) == leader) base = atomicAdd(&cell_count[key], __popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  rank_out[i] = base + __popc(peers & lanemask_lt());
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan of cell counts (three phases)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t warp_sums[32];
+  const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= static_cast<unsigned>(o)) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    uint32_t w = lane < static_cast<unsigned>(nw) ? warp_sums[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= static_cast<unsigned>(o)) w += y;
+    }
+    if (lane < static_cast<unsigned>(nw)) warp_sums[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t warp_off = warp ? warp_sums[warp - 1] : 0u;
+  *total = warp_sums[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return warp_off + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* __restrict__ count,
+                                                              uint32_t* __restrict__ start,
+                                                              uint32_t* __restrict__ tile_sum,
+                                                              uint32_t m) {
+  const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = (base + k < m) ? count[base + k] : 0u;
+    s += v[k];
+  }
+  uint32_t total;
+  uint32_t off = block_exclusive_scan(s, &total);
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < m) start[base + k] = off;
+    off += v[k];
+  }
+  if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(uint32_t* __restrict__ tile_sum, uint32_t tiles,
+                                                     uint32_t* __restrict__ start, uint32_t m) {
+  uint32_t carry = 0;
+  for (uint32_t b = 0; b < tiles; b += blockDim.x) {
+    const uint32_t idx = b + threadIdx.x;
+    const uint32_t v = idx < tiles ? tile_sum[idx] : 0u;
+    uint32_t total;
+    const uint32_t ex = block_exclusive_scan(v, &total);
+    if (idx < tiles) tile_sum[idx] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) start[m] = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_add(uint32_t* __restrict__ start,
+                                                            const uint32_t* __restrict__ tile_sum,
+                                                            uint32_t m) {
+  const uint32_t add = tile_sum[blockIdx.x];
+  const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k)
+    if (base + k < m) start[base + k] += add;
+}
+
+// ---------------------------------------------------------------------------
+// reorder
+// ---------------------------------------------------------------------------
+__global__ void k_scatter(const uint32_t* __restrict__ key, const uint32_t* __restrict__ rank,
+                          const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ perm, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) perm[cell_start[key[i]] + rank[i]] = static_cast<uint32_t>(i);
+}
+
+// Insertion sort of each cell's slots by original particle index, so the
+// cell order (hence every neighbour sum) is independent of atomic timing.
+// Cells above kMaxSortedCell particles keep the atomic order (bounded time).
+__global__ void k_cellsort(const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ perm,
+                           const uint32_t* __restrict__ id, uint32_t m) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m) return;
+  const uint32_t b = cell_start[c], e = cell_start[c + 1];
+  if (e - b < 2 || e - b > kMaxSortedCell) return;
+  for (uint32_t x = b + 1; x < e; ++x) {
+    const uint32_t v = perm[x];
+    const uint32_t kv = id[v];
+    uint32_t y = x;
+    while (y > b && id[perm[y - 1]] > kv) {
+      perm[y] = perm[y - 1];
+      --y;
+    }
+    perm[y] = v;
+  }
+}
+
+__global__ void k_gather(const uint32_t* __restrict__ perm, const float4* __restrict__ pos_a,
+                         const float4* __restrict__ disp_a, const float4* __restrict__ vel_a,
+                         const uint32_t* __restrict__ id_a, float4* __restrict__ pos_b,
+                         float4* __restrict__ disp_b, float4* __restrict__ xs_b,
+                         float4* __restrict__ vel_b, uint32_t* __restrict__ id_b, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint32_t i = perm[s];
+  const float4 x = pos_a[i];
+  pos_b[s] = x;
+  id_b[s] = id_a[i];
+  if (disp_a) {
+    const float4 d = disp_a[i];
+    disp_b[s] = d;
+    xs_b[s] = make_float4(x.x + d.x, x.y + d.y, x.z + d.z, 0.f);
+  }
+  if (vel_a) vel_b[s] = vel_a[i];
+}
+
+// ---------------------------------------------------------------------------
+// neighbour sets
+// ---------------------------------------------------------------------------
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ xs,
+                                                     const float4* __restrict__ pos,
+                                                     const uint32_t* __restrict__ cell_start,
+                                                     const SceneDesc* __restrict__ scenes,
+                                                     uint4* __restrict__ hdr, uint32_t* __restrict__ words,
+                                                     unsigned* __restrict__ err, DevParams P, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = xs[i];
+  const SceneDesc& sc = scenes[scene_of_slot(pos[i])];
+  const CellCoord cc = cell_of(f3(xi), sc, P.inv_cell);
+  const int cap = min(P.max_words * 4, 255);
+  uint32_t cnt[3] = {0u, 0u, 0u};
+  int total = 0;
+  uint32_t word = 0;
+  unsigned flags = 0;
+  const int x0 = cc.x > 0 ? cc.x - 1 : 0;
+  const int x1 = cc.x + 1 < sc.dim[0] ? cc.x + 1 : sc.dim[0] - 1;
+#pragma unroll 1
+  for (int r = 0; r < 9; ++r) {
+    const int z = cc.z + r / 3 - 1, y = cc.y + r % 3 - 1;
+    if (z < 0 || z >= sc.dim[2] || y < 0 || y >= sc.dim[1]) continue;
+    const uint32_t row = sc.cell_off + static_cast<uint32_t>((z * sc.dim[1] + y) * sc.dim[0]);
+    const uint32_t start = __ldg(&cell_start[row + x0]);
+    uint32_t end = __ldg(&cell_start[row + x1 + 1]);
+    if (end - start > static_cast<uint32_t>(kMaxRowCandidates)) {
+      flags |= PBF_ERRBIT_ROW_CAPACITY;
+      end = start + kMaxRowCandidates;
+    }
+    uint32_t c = 0;
+    for (uint32_t j = start; j < end; ++j) {
+      if (j == static_cast<uint32_t>(i)) continue;
+      const float4 xj = __ldg(&xs[j]);
+      if (dist2_rn(xi, xj) <= P.h2) {
+        if (total < cap) {
+          word |= (j - start) << (8 * (total & 3));
+          ++total;
+          ++c;
+          if ((total & 3) == 0) {
+            words[static_cast<size_t>((total >> 2) - 1) * n + i] = word;
+            word = 0;
+          }
+        } else {
+          flags |= PBF_ERRBIT_NEIGHBOR_CAPACITY;
+        }
+      }
+    }
+    cnt[r >> 2] |= c << (8 * (r & 3));
+  }
+  if (total & 3) words[static_cast<size_t>(total >> 2) * n + i] = word;
+  hdr[i] = make_uint4(cnt[0], cnt[1], cnt[2] | (static_cast<uint32_t>(total) << 8), pack_coord(cc));
+  if (flags) atomicOr(err, flags);
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi density-constraint iterations
+// ---------------------------------------------------------------------------
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_lambda(const float4* __restrict__ xs,
+                                                  const float4* __restrict__ pos,
+                                                  const uint4* __restrict__ hdr,
+                                                  const uint32_t* __restrict__ words,
+                                                  const uint32_t* __restrict__ cell_start,
+                                                  const SceneDesc* __restrict__ scenes,
+                                                  float* __restrict__ lam, float* __restrict__ rho_iter0,
+                                                  DevParams P, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = xs[i];
+  const SceneDesc& sc = scenes[scene_of_slot(pos[i])];
+  float qsum = 0.f, g2 = 0.f;
+  float3 gs = make_float3(0.f, 0.f, 0.f);
+  for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) {
+    const float4 xj = __ldg(&xs[j]);
+    const float3 r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+    const float r2 = dot3(r, r);
+    if (r2 < P.h2) {
+      const float q = P.h2 - r2;
+      qsum += q * q * q;
+    }
+    float s;
+    if (spiky_s(r2, P.h, &s)) {
+      gs = gs + r * s;
+      g2 += s * s * r2;
+    }
+  });
+  const float rho = P.poly6_c * qsum;
+  const float kg = P.spiky_c * P.inv_rho0;
+  const float denom = kg * kg * (g2 + dot3(gs, gs)) + P.epsilon;
+  lam[i] = -(rho * P.inv_rho0 - 1.0f) / denom;
+  if (rho_iter0) rho_iter0[i] = rho;
+}
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
+                                                  const float4* __restrict__ pos,
+                                                  const uint4* __restrict__ hdr,
+                                                  const uint32_t* __restrict__ words,
+                                                  const uint32_t* __restrict__ cell_start,
+                                                  const SceneDesc* __restrict__ scenes,
+                                                  const float* __restrict__ lam,
+                                                  float4* __restrict__ disp, float4* __restrict__ xs_next,
+                                                  DevParams P, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = xs[i];
+  const float4 x4 = pos[i];
+  const SceneDesc& sc = scenes[scene_of_slot(x4)];
+  const float li = lam[i];
+  float3 dp = make_float3(0.f, 0.f, 0.f);
+  for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) {
+    const float4 xj = __ldg(&xs[j]);
+    const float lj = __ldg(&lam[j]);
+    const float3 r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+    const float r2 = dot3(r, r);
+    float w = 0.f;
+    if (r2 < P.h2) {
+      const float q = P.h2 - r2;
+      w = P.poly6_c * (q * q * q);
+    }
+    const float a = w * P.tis;
+    float an = a;
+    for (int e = 1; e < P.scorr_n; ++e) an *= a;
+    const float scorr = -P.scorr_k * an;
+    float s;
+    if (spiky_s(r2, P.h, &s)) dp = dp + r * ((li + lj + scorr) * s);
+  });
+  dp = dp * (P.spiky_c * P.inv_rho0);
+  const float4 d4 = disp[i];
+  float3 d = f3(d4);
+  const float3 x = f3(x4);
+  collide(x, d, dp, false, sc, P);
+  disp[i] = make_float4(d.x, d.y, d.z, 0.f);
+  xs_next[i] = make_float4(x.x + d.x, x.y + d.y, x.z + d.z, 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// velocity, vorticity, XSPH, reported density; then vorticity confinement
+// ---------------------------------------------------------------------------
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_xsph(const float4* __restrict__ xs,
+                                                const float4* __restrict__ pos,
+                                                const float4* __restrict__ disp,
+                                                const uint4* __restrict__ hdr,
+                                                const uint32_t* __restrict__ words,
+                                                const uint32_t* __restrict__ cell_start,
+                                                const SceneDesc* __restrict__ scenes,
+                                                float4* __restrict__ vel_out, float4* __restrict__ omega,
+                                                float* __restrict__ rho_out, DevParams P, float inv_dt,
+                                                int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const float4 xi = xs[i];
+    const SceneDesc& sc = scenes[scene_of_slot(pos[i])];
+    const float3 vi = f3(disp[i]) * inv_dt;  // updateVelocity, particles.cpp:215-217
+    float qsum = 0.f;
+    float3 visc = make_float3(0.f, 0.f, 0.f), w = make_float3(0.f, 0.f, 0.f);
+    for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) {
+      const float4 xj = __ldg(&xs[j]);
+      const float3 vij = f3(__ldg(&disp[j])) * inv_dt - vi;
+      const float3 r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+      const float r2 = dot3(r, r);
+      if (r2 < P.h2) {
+        const float q = P.h2 - r2;
+        const float q3 = q * q * q;
+        visc = visc + vij * q3;
+        qsum += q3;
+      }
+      float s;
+      if (spiky_s(r2, P.h, &s)) w = w + cross3(vij, r * s);
+    });
+    const float rho = P.poly6_c * qsum;
+    w = w * P.spiky_c;
+    const float3 v = vi + visc * (P.xsph_c * P.poly6_c);
+    vel_out[i] = make_float4(v.x, v.y, v.z, 0.f);
+    omega[i] = make_float4(w.x, w.y, w.z, sqrtf(dot3(w, w)));
+    rho_out[i] = rho;
+  }
+}
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
+                                                float4* __restrict__ pos,
+                                                const float4* __restrict__ omega,
+                                                const uint4* __restrict__ hdr,
+                                                const uint32_t* __restrict__ words,
+                                                const uint32_t* __restrict__ cell_start,
+                                                const SceneDesc* __restrict__ scenes,
+                                                float4* __restrict__ vel, unsigned* __restrict__ err,
+                                                DevParams P, float dt, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = xs[i];
+  const float4 p4 = pos[i];
+  const SceneDesc& sc = scenes[scene_of_slot(p4)];
+  float3 eta = make_float3(0.f, 0.f, 0.f);
+  for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) {
+    const float4 xj = __ldg(&xs[j]);
+    const float wj = __ldg(&omega[j].w);
+    const float3 r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+    float s;
+    if (spiky_s(dot3(r, r), P.h, &s)) eta = eta + r * (wj * s);
+  });
+  eta = eta * P.spiky_c;
+  float3 v = f3(vel[i]);
+  const float en = sqrtf(dot3(eta, eta));
+  if (en > kEps) {
+    const float4 wi = omega[i];
+    v = v + cross3(eta * (1.0f / en), f3(wi)) * (dt * P.vort_eps);
+  }
+  vel[i] = make_float4(v.x, v.y, v.z, 0.f);
+  pos[i] = make_float4(xi.x, xi.y, xi.z, p4.w);  // updatePosition, particles.cpp:246-248
+  if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(xi.x) && isfinite(xi.y) &&
+        isfinite(xi.z)))
+    atomicOr(err, PBF_ERRBIT_NONFINITE);
+}
+
+// Step statistics (the prints of particles.cpp:267-295 and the neighbour
+// alert of :168-172, as numbers): one pass over densities and list headers.
+__global__ void __launch_bounds__(256) k_stats(const float* __restrict__ rho, const float* __restrict__ rho0,
+                                               const uint4* __restrict__ hdr, DevStats* __restrict__ st,
+                                               float inv_rho0, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i < n;
+  double r = 0.0, r0 = 0.0, es = 0.0;
+  float em = 0.f;
+  unsigned cmin = 0xffffffffu, cmax = 0u;
+  unsigned long long csum = 0ull, low = 0ull;
+  if (live) {
+    const float x = rho[i];
+    r = x;
+    r0 = rho0[i];
+    const float e = fabsf(x * inv_rho0 - 1.0f);
+    es = e;
+    em = e;
+    const unsigned c = static_cast<unsigned>(nbr_total(hdr[i]));
+    cmin = cmax = c;
+    csum = c;
+    low = c < static_cast<unsigned>(kNeighborAlert) ? 1ull : 0ull;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    r += __shfl_down_sync(0xffffffffu, r, o);
+    r0 += __shfl_down_sync(0xffffffffu, r0, o);
+    es += __shfl_down_sync(0xffffffffu, es, o);
+    em = fmaxf(em, __shfl_down_sync(0xffffffffu, em, o));
+    cmin = min(cmin, __shfl_down_sync(0xffffffffu, cmin, o));
+    cmax = max(cmax, __shfl_down_sync(0xffffffffu, cmax, o));
+    csum += __shfl_down_sync(0xffffffffu, csum, o);
+    low += __shfl_down_sync(0xffffffffu, low, o);
+  }
+  if (lane_id() == 0 && live) {  // live threads form a prefix: lane 0 live iff any lane is
+    atomicAdd(&st->rho_sum, r);
+    atomicAdd(&st->rho_iter0_sum, r0);
+    atomicAdd(&st->err_sum, es);
+    atomicMax(&st->err_max_bits, __float_as_uint(em));
+    atomicMin(&st->nbr_min, cmin);
+    atomicMax(&st->nbr_max, cmax);
+    atomicAdd(&st->nbr_sum, csum);
+    atomicAdd(&st->low_cnt, low);
+  }
+}
+
+__global__ void k_stats_init(DevStats* st) {
+  st->rho_iter0_sum = 0.0;
+  st->rho_sum = 0.0;
+  st->err_sum = 0.0;
+  st->err_max_bits = 0u;
+  st->nbr_min = 0xffffffffu;
+  st->nbr_max = 0u;
+  st->nbr_sum = 0ull;
+  st->low_cnt = 0ull;
+}
+
+// ---------------------------------------------------------------------------
+// transfers between original order and cell order
+// ---------------------------------------------------------------------------
+__global__ void k_upload(const float* __restrict__ xyz, const float* __restrict__ v,
+                         const SceneDesc* __restrict__ scenes, int n_scenes, float4* __restrict__ pos,
+                         float4* __restrict__ vel, uint32_t* __restrict__ id, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int lo = 0, hi = n_scenes - 1;  // scene whose particle range holds s
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (scenes[mid].p_off <= static_cast<uint32_t>(s)) lo = mid; else hi = mid - 1;
+  }
+  pos[s] = make_float4(xyz[3 * s], xyz[3 * s + 1], xyz[3 * s + 2], __int_as_float(lo));
+  vel[s] = v ? make_float4(v[3 * s], v[3 * s + 1], v[3 * s + 2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+  id[s] = static_cast<uint32_t>(s);
+}
+
+__global__ void k_download(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                           const float* __restrict__ rho, const uint32_t* __restrict__ id,
+                           float* __restrict__ xyz, float* __restrict__ v, float* __restrict__ r, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint32_t o = id[s];
+  if (xyz) {
+    const float4 p = pos[s];
+    xyz[3 * o] = p.x;
+    xyz[3 * o + 1] = p.y;
+    xyz[3 * o + 2] = p.z;
+  }
+  if (v) {
+    const float4 q = vel[s];
+    v[3 * o] = q.x;
+    v[3 * o + 1] = q.y;
+    v[3 * o + 2] = q.z;
+  }
+  if (r) r[o] = rho[s];
+}
+
+__global__ void k_unsort_u32(const uint32_t* __restrict__ src, const uint32_t* __restrict__ id,
+                             uint32_t* __restrict__ dst, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) dst[id[s]] = src[s];
+}
+
+__global__ void k_unsort_f4(const float4* __restrict__ src, const uint32_t* __restrict__ id,
+                            float* __restrict__ dst, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const float4 p = src[s];
+  const uint32_t o = id[s];
+  dst[3 * o] = p.x;
+  dst[3 * o + 1] = p.y;
+  dst[3 * o + 2] = p.z;
+}
+
+__global__ void k_cells_of(const float4* __restrict__ xs, const float4* __restrict__ pos,
+                           const SceneDesc* __restrict__ scenes, const uint32_t* __restrict__ id,
+                           uint32_t* __restrict__ cells, DevParams P, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const SceneDesc& sc = scenes[scene_of_slot(pos[s])];
+  cells[id[s]] = cell_key(cell_of(f3(xs[s]), sc, P.inv_cell), sc);
+}
+
+__global__ void k_nbr_counts(const uint4* __restrict__ hdr, const uint32_t* __restrict__ id,
+                             uint32_t* __restrict__ counts, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) counts[id[s]] = static_cast<uint32_t>(nbr_total(hdr[s]));
+}
+
+// ids[offsets[id[i]] ...] = original ids of i's neighbours (cell order).
+__global__ void k_nbr_ids(const float4* __restrict__ pos, const uint4* __restrict__ hdr,
+                          const uint32_t* __restrict__ words, const uint32_t* __restrict__ cell_start,
+                          const SceneDesc* __restrict__ scenes, const uint32_t* __restrict__ id,
+                          const uint32_t* __restrict__ offsets, uint32_t* __restrict__ ids, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const SceneDesc& sc = scenes[scene_of_slot(pos[i])];
+  uint32_t o = offsets[id[i]];
+  for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) { ids[o++] = id[j]; });
+}
+
+// Particles::estimateDensities (particles.cpp:440-444) on cell-sorted x: self included.
+__global__ void k_density_self(const float4* __restrict__ pos, const uint32_t* __restrict__ cell_start,
+                               const SceneDesc* __restrict__ scenes, float* __restrict__ rho,
+                               DevParams P, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = pos[i];
+  const SceneDesc& sc = scenes[scene_of_slot(xi)];
+  const CellCoord cc = cell_of(f3(xi), sc, P.inv_cell);
+  float qsum = 0.f;
+  for (int r = 0; r < 9; ++r) {
+    const int z = cc.z + r / 3 - 1, y = cc.y + r % 3 - 1;
+    if (z < 0 || z >= sc.dim[2] || y < 0 || y >= sc.dim[1]) continue;
+    const uint32_t row = sc.cell_off + static_cast<uint32_t>((z * sc.dim[1] + y) * sc.dim[0]);
+    const int x0 = cc.x > 0 ? cc.x - 1 : 0;
+    const int x1 = cc.x + 1 < sc.dim[0] ? cc.x + 1 : sc.dim[0] - 1;
+    for (uint32_t j = cell_start[row + x0]; j < cell_start[row + x1 + 1]; ++j) {
+      const float4 xj = __ldg(&pos[j]);
+      const float3 d = make_float3(xj.x - xi.x, xj.y - xi.y, xj.z - xi.z);
+      const float r2 = dot3(d, d);
+      if (r2 < P.h2) {
+        const float q = P.h2 - r2;
+        qsum += q * q * q;
+      }
+    }
+  }
+  rho[i] = P.poly6_c * qsum;
+}
+
+// Particles::estimateDensityAt (particles.cpp:446-453) at query points, scene 0.
+__global__ void k_density_at(const float4* __restrict__ pos, const uint32_t* __restrict__ cell_start,
+                             const SceneDesc* __restrict__ scenes, const float* __restrict__ pts,
+                             float* __restrict__ out, DevParams P, int m) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  const SceneDesc& sc = scenes[0];
+  const float3 p = make_float3(pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]);
+  const CellCoord cc = cell_of(p, sc, P.inv_cell);
+  float qsum = 0.f;
+  for (int r = 0; r < 9; ++r) {
+    const int z = cc.z + r / 3 - 1, y = cc.y + r % 3 - 1;
+    if (z < 0 || z >= sc.dim[2] || y < 0 || y >= sc.dim[1]) continue;
+    const uint32_t row = sc.cell_off + static_cast<uint32_t>((z * sc.dim[1] + y) * sc.dim[0]);
+    const int x0 = cc.x > 0 ? cc.x - 1 : 0;
+    const int x1 = cc.x + 1 < sc.dim[0] ? cc.x + 1 : sc.dim[0] - 1;
+    for (uint32_t j = cell_start[row + x0]; j < cell_start[row + x1 + 1]; ++j) {
+      const float4 xj = __ldg(&pos[j]);
+      const float3 d = make_float3(xj.x - p.x, xj.y - p.y, xj.z - p.z);
+      const float r2 = dot3(d, d);
+      if (r2 < P.h2) {
+        const float qq = P.h2 - r2;
+        qsum += qq * qq * qq;
+      }
+    }
+  }
+  out[q] = P.poly6_c * qsum;
+}
+
+inline unsigned blocks_for(size_t n, int block) { return static_cast<unsigned>((n + block - 1) / block); }
+
+// Shared front half of a step and of a resort: keys, counts, scan, slots.
+cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& t, int cur, float dt,
+                            bool move, cudaStream_t s) {
+  const int n = static_cast<int>(b.n);
+  const uint32_t m = b.n_cells;
+  cudaError_t e = cudaMemsetAsync(b.cell_count, 0, sizeof(uint32_t) * m, s);
+  if (e != cudaSuccess) return e;
+  k_predict<<<blocks_for(n, t.block_predict), t.block_predict, 0, s>>>(
+      b.pos[cur], b.vel[cur], b.disp[0], b.key, b.rank, b.cell_count, b.scenes, P, dt, move ? 1 : 0, n);
+  const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
+  k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(b.cell_count, b.cell_start, b.scan_tmp, m);
+  k_scan_sums<<<1, 1024, 0, s>>>(b.scan_tmp, tiles, b.cell_start, m);
+  k_scan_add<<<tiles, kScanThreads, 0, s>>>(b.cell_start, b.scan_tmp, m);
+  k_scatter<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(b.key, b.rank, b.cell_start, b.perm, n);
+  k_cellsort<<<blocks_for(m, t.block_misc), t.block_misc, 0, s>>>(b.cell_start, b.perm, b.id[cur], m);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+#define PBF_BLOCK_SWITCH(block, ...)                          \
+  switch (block) {                                            \
+    case 64: { constexpr int BLOCK = 64; __VA_ARGS__; } break;   \
+    case 128: { constexpr int BLOCK = 128; __VA_ARGS__; } break; \
+    case 512: { constexpr int BLOCK = 512; __VA_ARGS__; } break; \
+    default: { constexpr int BLOCK = 256; __VA_ARGS__; } break;  \
+  }
+
+cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, int cur, float dt,
+                        int iters, bool keep_pred, cudaStream_t s) {
+  const int n = static_cast<int>(b.n);
+  if (n == 0) return cudaSuccess;
+  const int A = cur, B = 1 - cur;
+  if (P.stats) k_stats_init<<<1, 1, 0, s>>>(b.stats);
+  cudaError_t e = sort_into_cells(b, P, t, A, dt, true, s);
+  if (e != cudaSuccess) return e;
+  k_gather<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(
+      b.perm, b.pos[A], b.disp[0], nullptr, b.id[A], b.pos[B], b.disp[1], b.xs[0], nullptr, b.id[B], n);
+  if (keep_pred && b.pred) {
+    e = cudaMemcpyAsync(b.pred, b.xs[0], sizeof(float4) * b.n, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  }
+  PBF_BLOCK_SWITCH(t.block_nbr,
+                   k_nbr_build<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                       b.xs[0], b.pos[B], b.cell_start, b.scenes, b.nbr_hdr, b.nbr_w, b.err, P, n));
+  for (int it = 0; it < iters; ++it) {
+    const float4* xcur = b.xs[it & 1];
+    float4* xnext = b.xs[(it + 1) & 1];
+    PBF_BLOCK_SWITCH(t.block_solve,
+                     k_lambda<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                         xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.lam,
+                         (it == 0 && P.stats) ? b.rho_iter0 : nullptr, P, n));
+    PBF_BLOCK_SWITCH(t.block_solve,
+                     k_deltap<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                         xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.lam, b.disp[1],
+                         xnext, P, n));
+  }
+  const float4* fin = b.xs[iters & 1];
+  PBF_BLOCK_SWITCH(t.block_solve,
+                   k_xsph<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                       fin, b.pos[B], b.disp[1], b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.vel[B],
+                       b.omega, b.rho, P, 1.0f / dt, n));
+  PBF_BLOCK_SWITCH(t.block_solve,
+                   k_vort<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                       fin, b.pos[B], b.omega, b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.vel[B],
+                       b.err, P, dt, n));
+  if (P.stats)
+    k_stats<<<blocks_for(n, 256), 256, 0, s>>>(b.rho, b.rho_iter0, b.nbr_hdr, b.stats, P.inv_rho0, n);
+  return cudaGetLastError();
+}
+
+// Reorder the state into cells of the current positions (no motion); the
+// result lands in buffers 1 - cur.
+cudaError_t launch_resort(const Buffers& b, const DevParams& P, const Tuning& t, int cur, cudaStream_t s) {
+  const int n = static_cast<int>(b.n);
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = sort_into_cells(b, P, t, cur, 0.f, false, s);
+  if (e != cudaSuccess) return e;
+  k_gather<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(
+      b.perm, b.pos[cur], nullptr, b.vel[cur], b.id[cur], b.pos[1 - cur], nullptr, nullptr, b.vel[1 - cur],
+      b.id[1 - cur], n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_upload(const Buffers& b, int cur, const float* xyz, const float* vel,
+                          const uint32_t* /*scene_of*/, cudaStream_t s) {
+  const int n = static_cast<int>(b.n);
+  if (n == 0) return cudaSuccess;
+  k_upload<<<blocks_for(n, 256), 256, 0, s>>>(xyz, vel, b.scenes, b.n_scenes, b.pos[cur], b.vel[cur],
+                                              b.id[cur], n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_download(const Buffers& b, int cur, float* xyz, float* vel, float* rho, cudaStream_t s) {
+  const int n = static_cast<int>(b.n);
+  if (n == 0) return cudaSuccess;
+  k_download<<<blocks_for(n, 256), 256, 0, s>>>(b.pos[cur], b.vel[cur], b.rho, b.id[cur], xyz, vel, rho, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unsort_u32(const Buffers& b, int cur, const uint32_t* src, uint32_t* dst, cudaStream_t s) {
+  const int n = static_cast<int>(b.n);
+  if (n == 0) return cudaSuccess;
+  k_unsort_u32<<<blocks_for(n, 256), 256, 0, s>>>(src, b.id[cur], dst, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unsort_f4(const Buffers& b, int cur, const float4* src, float* dst_xyz, cudaStream_t s) {
+  const int n = static_cast<int>(b.n);
+  if (n == 0) return cudaSuccess;
+  k_unsort_f4<<<blocks_for(n, 256), 256, 0, s>>>(src, b.id[cur], dst_xyz, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cells_of(const Buffers& b, const DevParams& P, int cur, uint32_t* cells, cudaStream_t s) {
+  const int n = static_cast<int>(b.n);
+  if (n == 0) return cudaSuccess;
+  k_cells_of<<<blocks_for(n, 256), 256, 0, s>>>(b.pred, b.pos[cur], b.scenes, b.id[cur], cells, P, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_neighbor_counts(const Buffers& b, int cur, uint32_t* counts, cudaStream_t s) {
+  const int n = static_cast<int>(b.n);
+  if (n == 0) return cudaSuccess;
+  k_nbr_counts<<<blocks_for(n, 256), 256, 0, s>>>(b.nbr_hdr, b.id[cur], counts, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_neighbor_ids(const Buffers& b, int cur, const uint32_t* offsets, uint32_t* ids,
+                                cudaStream_t s) {
+  const int n = static_cast<int>(b.n);
+  if (n == 0) return cudaSuccess;
+  k_nbr_ids<<<blocks_for(n, 256), 256, 0, s>>>(b.pos[cur], b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes,
+                                               b.id[cur], offsets, ids, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_density_self(const Buffers& b, const DevParams& P, const Tuning& t, int cur,
+                                float* rho_sorted, cudaStream_t s) {
+  const int n = static_cast<int>(b.n);
+  if (n == 0) return cudaSuccess;
+  k_density_self<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(b.pos[cur], b.cell_start, b.scenes,
+                                                                       rho_sorted, P, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_density_at(const Buffers& b, const DevParams& P, int cur, size_t m, const float* pts,
+                              float* out, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  k_density_at<<<blocks_for(m, 256), 256, 0, s>>>(b.pos[cur], b.cell_start, b.scenes, pts, out, P,
+                                                  static_cast<int>(m));
+  return cudaGetLastError();
+}
+
+}  // namespace pbf

@@ -1,0 +1,248 @@
+"""Python binding of the C ABI (include/pbf.h) over ctypes.
+
+``Simulator`` mirrors the reference's ``Particles`` (src/particles.h:105-140): construct
+from positions/velocities and a parameter set, ``time_step(dt)``, position / velocity /
+density accessors, ``estimate_densities()`` and ``estimate_density_at()``. Every call
+goes to libpbf.so; there is no Python or CPU fallback, and loading fails loudly when
+the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from .params import CParams, PbfParams
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpbf.so"
+
+PBF_OK = 0
+STATUS = {0: "PBF_OK", 1: "PBF_ERR_INVALID", 2: "PBF_ERR_CUDA", 3: "PBF_ERR_TIMEOUT",
+          4: "PBF_ERR_NONFINITE", 5: "PBF_ERR_CAPACITY", 6: "PBF_ERR_NOMEM"}
+
+
+class PbfError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class CStats(ctypes.Structure):
+    _fields_ = [
+        ("steps", ctypes.c_uint64),
+        ("mean_density_iter0", ctypes.c_double),
+        ("mean_density", ctypes.c_double),
+        ("max_density_error", ctypes.c_double),
+        ("mean_density_error", ctypes.c_double),
+        ("min_neighbors", ctypes.c_uint32),
+        ("max_neighbors", ctypes.c_uint32),
+        ("mean_neighbors", ctypes.c_double),
+        ("low_neighbor_count", ctypes.c_uint64),
+        ("error_flags", ctypes.c_uint32),
+    ]
+
+
+_lib = None
+P = ctypes.c_void_p
+
+
+def _declare(L):
+    st = ctypes.c_int
+    sz = ctypes.c_size_t
+    sigs = {
+        "pbf_params_default": (None, [P]),
+        "pbf_abi_version": (ctypes.c_int, []),
+        "pbf_create": (st, [P, sz, P, P, ctypes.c_int, P]),
+        "pbf_batch_create": (st, [P, ctypes.c_int, P, P, P, P, P, ctypes.c_int, P]),
+        "pbf_destroy": (st, [P]),
+        "pbf_step": (st, [P, ctypes.c_double, ctypes.c_int]),
+        "pbf_step_async": (st, [P, ctypes.c_double, ctypes.c_int]),
+        "pbf_sync": (st, [P]),
+        "pbf_stream": (P, [P]),
+        "pbf_get_positions": (st, [P, P]),
+        "pbf_get_velocities": (st, [P, P]),
+        "pbf_get_densities": (st, [P, P]),
+        "pbf_set_state": (st, [P, P, P]),
+        "pbf_set_state_device": (st, [P, P, P, P]),
+        "pbf_get_state_device": (st, [P, P, P, P, P]),
+        "pbf_estimate_densities": (st, [P, P]),
+        "pbf_estimate_density_at": (st, [P, sz, P, P]),
+        "pbf_get_stats": (st, [P, P]),
+        "pbf_get_neighbors": (st, [P, P, P, sz, P]),
+        "pbf_get_cells": (st, [P, P]),
+        "pbf_get_predicted": (st, [P, P]),
+        "pbf_size": (sz, [P]),
+        "pbf_num_scenes": (ctypes.c_int, [P]),
+        "pbf_last_error": (ctypes.c_char_p, [P]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
+def lib():
+    """Load libpbf.so (built by ``fluid_gb300.build``); raise if it is missing."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise FileNotFoundError(
+                f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        _lib = _declare(ctypes.CDLL(str(LIB_PATH)))
+    return _lib
+
+
+def default_params_c() -> CParams:
+    c = CParams()
+    lib().pbf_params_default(ctypes.byref(c))
+    return c
+
+
+def _f32(a, shape_last=3):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.ndim != 2 or a.shape[1] != shape_last:
+        raise ValueError(f"expected an (n, {shape_last}) array")
+    return a
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(P)
+
+
+class Simulator:
+    """A GPU PBF simulator over one scene or a batch of independent scenes."""
+
+    def __init__(self, pos, vel=None, params: PbfParams | None = None, device: int = 0,
+                 counts=None, boxes=None):
+        L = lib()
+        self._h = P()
+        self.params = params or PbfParams()
+        cp = self.params.to_c()
+        pos = _f32(pos)
+        vel = None if vel is None else _f32(vel)
+        if vel is not None and vel.shape != pos.shape:
+            raise ValueError("vel must match pos")
+        self.n = pos.shape[0]
+        if counts is None:
+            rc = L.pbf_create(ctypes.byref(cp), self.n, _ptr(pos), _ptr(vel), device, ctypes.byref(self._h))
+        else:
+            cnt = np.ascontiguousarray(counts, dtype=np.uint64)
+            if int(cnt.sum()) != self.n:
+                raise ValueError("counts must sum to the number of particles")
+            lo = hi = None
+            if boxes is not None:
+                lo = np.ascontiguousarray([b[0] for b in boxes], dtype=np.float32)
+                hi = np.ascontiguousarray([b[1] for b in boxes], dtype=np.float32)
+            rc = L.pbf_batch_create(ctypes.byref(cp), len(cnt), _ptr(cnt), _ptr(lo), _ptr(hi), _ptr(pos),
+                                    _ptr(vel), device, ctypes.byref(self._h))
+        if rc != PBF_OK:
+            raise PbfError(rc, L.pbf_last_error(None).decode())
+
+    # -- lifetime ---------------------------------------------------------------
+    def close(self):
+        if self._h:
+            lib().pbf_destroy(self._h)
+            self._h = P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        if rc != PBF_OK:
+            raise PbfError(rc, lib().pbf_last_error(self._h).decode())
+
+    # -- stepping -----------------------------------------------------------------
+    def time_step(self, dt: float = 0.0, steps: int = 1):
+        """Particles::timeStep(dt) (particles.cpp:250-297); dt <= 0 uses params.dt."""
+        self._check(lib().pbf_step(self._h, float(dt), int(steps)))
+
+    def step_async(self, dt: float = 0.0, steps: int = 1):
+        self._check(lib().pbf_step_async(self._h, float(dt), int(steps)))
+
+    def sync(self):
+        self._check(lib().pbf_sync(self._h))
+
+    @property
+    def stream(self) -> int:
+        return lib().pbf_stream(self._h) or 0
+
+    # -- accessors ------------------------------------------------------------------
+    def positions(self) -> np.ndarray:
+        out = np.empty((self.n, 3), dtype=np.float32)
+        self._check(lib().pbf_get_positions(self._h, _ptr(out)))
+        return out
+
+    def velocities(self) -> np.ndarray:
+        out = np.empty((self.n, 3), dtype=np.float32)
+        self._check(lib().pbf_get_velocities(self._h, _ptr(out)))
+        return out
+
+    def densities(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.float32)
+        self._check(lib().pbf_get_densities(self._h, _ptr(out)))
+        return out
+
+    def set_state(self, pos, vel=None):
+        pos = _f32(pos)
+        vel = None if vel is None else _f32(vel)
+        self._check(lib().pbf_set_state(self._h, _ptr(pos), _ptr(vel)))
+
+    def set_state_device(self, pos_ptr: int, vel_ptr: int | None, stream: int = 0):
+        self._check(lib().pbf_set_state_device(self._h, P(pos_ptr), P(vel_ptr) if vel_ptr else None,
+                                               P(stream) if stream else None))
+
+    def get_state_device(self, pos_ptr: int | None, vel_ptr: int | None, rho_ptr: int | None,
+                         stream: int = 0):
+        self._check(lib().pbf_get_state_device(self._h, P(pos_ptr) if pos_ptr else None,
+                                               P(vel_ptr) if vel_ptr else None,
+                                               P(rho_ptr) if rho_ptr else None, P(stream) if stream else None))
+
+    def estimate_densities(self) -> np.ndarray:
+        """Particles::estimateDensities (particles.cpp:440-444): self term included."""
+        out = np.empty(self.n, dtype=np.float32)
+        self._check(lib().pbf_estimate_densities(self._h, _ptr(out)))
+        return out
+
+    def estimate_density_at(self, pts) -> np.ndarray:
+        """Particles::estimateDensityAt (particles.cpp:446-453) at each row of pts."""
+        pts = _f32(pts)
+        out = np.empty(pts.shape[0], dtype=np.float32)
+        self._check(lib().pbf_estimate_density_at(self._h, pts.shape[0], _ptr(pts), _ptr(out)))
+        return out
+
+    def stats(self) -> dict:
+        s = CStats()
+        self._check(lib().pbf_get_stats(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in CStats._fields_}
+
+    def neighbors(self):
+        """Neighbour sets of the last step in original ids: (offsets[n+1], ids), ascending."""
+        counts = np.zeros(self.n, dtype=np.uint32)
+        total = ctypes.c_size_t(0)
+        self._check(lib().pbf_get_neighbors(self._h, _ptr(counts), None, 0, ctypes.byref(total)))
+        ids = np.zeros(max(total.value, 1), dtype=np.uint32)
+        self._check(lib().pbf_get_neighbors(self._h, _ptr(counts), _ptr(ids), ids.size, ctypes.byref(total)))
+        off = np.zeros(self.n + 1, dtype=np.int64)
+        off[1:] = np.cumsum(counts)
+        return off, ids[: total.value]
+
+    def cells(self) -> np.ndarray:
+        out = np.zeros(self.n, dtype=np.uint32)
+        self._check(lib().pbf_get_cells(self._h, _ptr(out)))
+        return out
+
+    def predicted(self) -> np.ndarray:
+        out = np.empty((self.n, 3), dtype=np.float32)
+        self._check(lib().pbf_get_predicted(self._h, _ptr(out)))
+        return out

@@ -28,6 +28,12 @@ extern "C" {
 
 #define PBF_ABI_VERSION 1
 
+#if defined(__GNUC__)
+#define PBF_API __attribute__((visibility("default")))
+#else
+#define PBF_API
+#endif
+
 typedef enum pbf_status {
   PBF_OK = 0,
   PBF_ERR_INVALID = 1,   /* bad argument or handle state */
@@ -95,17 +101,17 @@ typedef struct pbf_stats {
 typedef struct pbf_handle pbf_handle;
 
 /* Fill *p with the reference's defaults (src/particles.cpp:20-44, 57-83, 180). */
-void pbf_params_default(pbf_params* p);
+PBF_API void pbf_params_default(pbf_params* p);
 
 /* ABI version of the loaded library. */
-int pbf_abi_version(void);
+PBF_API int pbf_abi_version(void);
 
 /*
  * Create a simulator over n particles (replaces `new Particles(rho0)` followed
  * by n calls of Particles::addParticle, particles.h:112-120). xyz/vel: host,
  * (n, 3) float32; vel may be NULL (zero). device: CUDA ordinal.
  */
-pbf_status pbf_create(const pbf_params* params, size_t n, const float* xyz,
+PBF_API pbf_status pbf_create(const pbf_params* params, size_t n, const float* xyz,
                       const float* vel, int device, pbf_handle** out);
 
 /*
@@ -114,58 +120,65 @@ pbf_status pbf_create(const pbf_params* params, size_t n, const float* xyz,
  * (n_scenes, 3); NULL = params->box_lo/hi). All scenes share the remaining
  * params. One launch per phase covers every scene.
  */
-pbf_status pbf_batch_create(const pbf_params* params, int n_scenes,
+PBF_API pbf_status pbf_batch_create(const pbf_params* params, int n_scenes,
                             const size_t* counts, const float* box_lo,
                             const float* box_hi, const float* xyz,
                             const float* vel, int device, pbf_handle** out);
 
-pbf_status pbf_destroy(pbf_handle* h);
+PBF_API pbf_status pbf_destroy(pbf_handle* h);
 
 /* Advance nsteps steps of dt each (Particles::timeStep(double),
  * particles.cpp:250-297; dt <= 0 uses params.dt like Particles::timeStep()). */
-pbf_status pbf_step(pbf_handle* h, double dt, int nsteps);
+PBF_API pbf_status pbf_step(pbf_handle* h, double dt, int nsteps);
+
+/* Enqueue nsteps steps on the handle's stream and return without waiting
+ * (no error check); pbf_sync waits and reports device-side errors. */
+PBF_API pbf_status pbf_step_async(pbf_handle* h, double dt, int nsteps);
+PBF_API pbf_status pbf_sync(pbf_handle* h);
+/* The handle's cudaStream_t (as void*), for ordering and event timing. */
+PBF_API void* pbf_stream(pbf_handle* h);
 
 /* Host accessors, original order (Particle::getPosition, ::velocity,
  * ::getLatestDensityEstimate; particles.h:36-46). */
-pbf_status pbf_get_positions(pbf_handle* h, float* xyz);
-pbf_status pbf_get_velocities(pbf_handle* h, float* vel);
-pbf_status pbf_get_densities(pbf_handle* h, float* rho);
+PBF_API pbf_status pbf_get_positions(pbf_handle* h, float* xyz);
+PBF_API pbf_status pbf_get_velocities(pbf_handle* h, float* vel);
+PBF_API pbf_status pbf_get_densities(pbf_handle* h, float* rho);
 /* Replace positions and velocities (host). */
-pbf_status pbf_set_state(pbf_handle* h, const float* xyz, const float* vel);
+PBF_API pbf_status pbf_set_state(pbf_handle* h, const float* xyz, const float* vel);
 
 /* Device-pointer forms of the accessors (see file comment for stream order). */
-pbf_status pbf_set_state_device(pbf_handle* h, const float* xyz,
+PBF_API pbf_status pbf_set_state_device(pbf_handle* h, const float* xyz,
                                 const float* vel, void* stream);
-pbf_status pbf_get_state_device(pbf_handle* h, float* xyz, float* vel,
+PBF_API pbf_status pbf_get_state_device(pbf_handle* h, float* xyz, float* vel,
                                 float* rho, void* stream);
 
 /* Particles::estimateDensities (particles.cpp:440-444): density of every
  * particle at its current position, self included; host out[n]. */
-pbf_status pbf_estimate_densities(pbf_handle* h, float* rho);
+PBF_API pbf_status pbf_estimate_densities(pbf_handle* h, float* rho);
 
 /* Particles::estimateDensityAt (particles.cpp:446-453) at m query points
  * (host, (m, 3)); out[m]. */
-pbf_status pbf_estimate_density_at(pbf_handle* h, size_t m, const float* pts,
+PBF_API pbf_status pbf_estimate_density_at(pbf_handle* h, size_t m, const float* pts,
                                    float* out);
 
-pbf_status pbf_get_stats(pbf_handle* h, pbf_stats* out);
+PBF_API pbf_status pbf_get_stats(pbf_handle* h, pbf_stats* out);
 
 /* Introspection of the last step, original order. Neighbour sets are those
  * of the reference's all-pairs search (particles.cpp:258-265) on x*:
  * counts[n], then ids in ascending original index (capacity cap entries;
  * *total receives the number needed). cells[n]: linear cell id of x*.
  * pred: x* after prediction (needs PBF_FLAG_KEEP_PREDICTED). */
-pbf_status pbf_get_neighbors(pbf_handle* h, uint32_t* counts, uint32_t* ids,
+PBF_API pbf_status pbf_get_neighbors(pbf_handle* h, uint32_t* counts, uint32_t* ids,
                              size_t cap, size_t* total);
-pbf_status pbf_get_cells(pbf_handle* h, uint32_t* cells);
-pbf_status pbf_get_predicted(pbf_handle* h, float* xyz);
+PBF_API pbf_status pbf_get_cells(pbf_handle* h, uint32_t* cells);
+PBF_API pbf_status pbf_get_predicted(pbf_handle* h, float* xyz);
 
-size_t pbf_size(const pbf_handle* h);
-int pbf_num_scenes(const pbf_handle* h);
+PBF_API size_t pbf_size(const pbf_handle* h);
+PBF_API int pbf_num_scenes(const pbf_handle* h);
 
 /* Human-readable description of the last error on this handle (or of the
  * last failed pbf_create when h is NULL). Never NULL. */
-const char* pbf_last_error(const pbf_handle* h);
+PBF_API const char* pbf_last_error(const pbf_handle* h);
 
 #ifdef __cplusplus
 }
