@@ -1,0 +1,418 @@
+#!/usr/bin/env python
+"""PBF particle-updates/s on one GB300 (one JSON line on stdout).
+
+Workload (default): the 1,048,576-particle colliding-blocks scene (two 64x128x64
+lattices, h = 0.0125, 4 Jacobi iterations, FP32), synthetic and seeded. A step is one
+full PBF time step of every particle (Particles::timeStep, particles.cpp:250-297).
+
+* ``value``: particle-updates/s with the state resident in HBM, device time of exactly
+  K steps from CUDA events on the simulator's stream. Every timed step advances the
+  configured initial state (cell-sorted once, then restored from a device snapshot
+  between steps), so each step does the full work of one PBF step over the configured
+  input; the reference's formulas are not stable for long rollouts at this resolution.
+  Snapshot restore and an L2 flush (256 MiB write) run between steps, outside the events.
+* ``e2e``: the same metric through the C ABI with host buffers: per step
+  pbf_set_state (H2D of positions and velocities from pinned memory), pbf_step, and
+  pbf_get_positions + pbf_get_velocities (D2H), wall-clocked.
+* ``roofline``: the dominant kernel's algorithmic bytes per launch over its average
+  event-timed launch duration, against the measured HBM copy bandwidth.
+* ``cpu_baseline``: the reference's own step (built from its sources) on a bounded
+  sample of the workload on the host cores, else the FP64 restatement.
+* ``--impl reference``: the reference CPU step alone, on the same config and metric.
+
+Multi-GPU: replicas only (every rank runs the same scene; weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "PBF particle-updates/s at 1M (4 iters); batched & adjoint vs plain, 1 GB300"
+UNIT = "particle-updates/s"
+
+# Algorithmic HBM bytes per particle for each phase (FP32 SoA; each phase reads and
+# writes its unique per-particle data once): B(I) = 340 + 56 I + 8 C/N.
+ALGO_BYTES = {"predict": 64 + 24, "sort": 104, "gather": 0, "lambda": 20, "deltap": 36,
+              "xsph": 84, "vorticity": 64, "neighbors": 16, "scan": 0, "stats": 0}
+# DRAM bytes per particle per launch measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum) on the 1M colliding-blocks scene; see profiles/.
+NCU_TRAFFIC_PER_PARTICLE: dict[str, float] = {}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(gpu_index)], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def sample_block(scene, side=16):
+    """A side^3 sub-lattice of the first block (bottom corner): the CPU baseline's sample."""
+    nx, ny = 64, 128
+    idx = [(k * ny + j) * nx + i for k in range(side) for j in range(side) for i in range(side)]
+    idx = np.asarray(idx)
+    return scene.pos[idx], scene.vel[idx]
+
+
+def run_reference_sample(scene, steps, procs, side=16):
+    """The reference step (oracle/_ref) on `procs` disjoint side^3 samples in parallel."""
+    from oracle import ref_runner
+
+    if not ref_runner.available():
+        return None
+    pos, vel = sample_block(scene, side)
+    # disjoint samples: shift each copy's lattice window along z inside block A
+    samples = []
+    for p in range(procs):
+        k0 = (p * side) % 64
+        nx, ny = 64, 128
+        idx = np.asarray([((k0 + k) % 64 * ny + j) * nx + i for k in range(side) for j in range(side)
+                          for i in range(side)])
+        samples.append((scene.pos[idx], scene.vel[idx]))
+    from concurrent.futures import ThreadPoolExecutor
+
+    with ThreadPoolExecutor(max_workers=procs) as ex:
+        outs = list(ex.map(lambda s: ref_runner.run(s[0], s[1], scene.params, steps=steps, mode="literal"), samples))
+    secs = max(o["seconds"] for o in outs)
+    n = samples[0][0].shape[0]
+    return {"value": procs * n * steps / secs, "seconds": secs, "n": n, "steps": steps, "procs": procs}
+
+
+def cpu_baseline(scene, budget_s: float):
+    """Reference step on one core, sized to roughly budget_s of CPU work."""
+    from oracle import ref_runner
+
+    if ref_runner.available():
+        probe = run_reference_sample(scene, 2, 1)
+        per_step = probe["seconds"] / 2
+        steps = max(2, min(400, int(budget_s / max(per_step, 1e-4))))
+        r = run_reference_sample(scene, steps, 1)
+        return {"value": r["value"], "unit": UNIT, "cores": 1, "kind": "reference",
+                "sample": f"reference particles.cpp step (FP64, O(N^2) all-pairs) on a {r['n']}-particle "
+                          f"16^3 sub-lattice of the workload, {steps} steps, 1 thread; the reference's cost "
+                          f"per particle grows with N, so this sample overstates its speed on the full scene"}
+    from oracle import oracle
+
+    pos, vel = sample_block(scene, 32)
+    t = time.perf_counter()
+    oracle.step(pos, vel, scene.params, steps=2, threads=1)
+    dt = (time.perf_counter() - t) / 2
+    steps = max(1, int(budget_s / max(dt, 1e-4)))
+    t = time.perf_counter()
+    oracle.step(pos, vel, scene.params, steps=steps, threads=1)
+    secs = time.perf_counter() - t
+    return {"value": pos.shape[0] * steps / secs, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"FP64 restatement (uniform grid) on a {pos.shape[0]}-particle sub-lattice, {steps} steps, "
+                      f"1 thread (reference build unavailable)"}
+
+
+def cpu_port_all_cores(scene, budget_s: float):
+    from oracle import oracle
+
+    pos, vel = sample_block(scene, 48)
+    threads = oracle.max_threads()
+    t = time.perf_counter()
+    oracle.step(pos, vel, scene.params, steps=1, threads=threads)
+    dt = time.perf_counter() - t
+    steps = max(1, int(budget_s / max(dt, 1e-4)))
+    t = time.perf_counter()
+    oracle.step(pos, vel, scene.params, steps=steps, threads=threads)
+    secs = time.perf_counter() - t
+    return {"value": pos.shape[0] * steps / secs, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"FP64 restatement (uniform grid, OpenMP) on a {pos.shape[0]}-particle sub-lattice, "
+                      f"{steps} steps"}
+
+
+def workload_config(scene, extra=None):
+    cfg = {"workload": scene.name, "particles": int(scene.n), "iters": scene.params.iters, "h": scene.params.h,
+           "dt": scene.params.dt, "seed": scene.seed, "l2": "flushed between timed steps (256 MiB write, untimed)",
+           "protocol": "each timed step advances the configured initial state (device snapshot restored between "
+                       "steps, untimed)",
+           "parallelism": "replicas", "notes": scene.notes}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def bench_reference(args, scene, world, rank):
+    if rank != 0:
+        return 0
+    procs = max(1, min(os.cpu_count() or 1, 64))
+    from oracle import ref_runner
+
+    if not ref_runner.available():
+        # fall back to the FP64 restatement (the oracle port) on all host threads
+        from oracle import oracle
+
+        pos, vel = sample_block(scene, 48)
+        threads = oracle.max_threads()
+        oracle.step(pos, vel, scene.params, steps=max(args.warmup, 1), threads=threads)
+        t = time.perf_counter()
+        oracle.step(pos, vel, scene.params, steps=args.steps, threads=threads)
+        secs = time.perf_counter() - t
+        value = pos.shape[0] * args.steps / secs
+        kind, cores = "port", threads
+        sample = f"FP64 restatement (OpenMP) on a {pos.shape[0]}-particle sub-lattice, {args.steps} steps"
+        ms = secs / args.steps * 1e3
+    else:
+        run_reference_sample(scene, max(args.warmup, 1), procs)  # warm-up
+        r = run_reference_sample(scene, args.steps, procs)
+        value, kind, cores = r["value"], "reference", procs
+        sample = (f"reference particles.cpp step (unmodified but for the parameter block), {procs} processes x "
+                  f"{r['n']}-particle disjoint 16^3 sub-lattices of the workload, {args.steps} steps each; "
+                  f"its all-pairs search makes the full {scene.n}-particle step far slower than this sample")
+        ms = r["seconds"] / args.steps * 1e3
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(scene),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def bench_ours(args, scene, world, rank, local):
+    import torch
+
+    from fluid_gb300 import pbf
+    from fluid_gb300.params import PBF_FLAG_STATS
+
+    torch.cuda.set_device(local)
+    prm = scene.params.with_(flags=PBF_FLAG_STATS)
+    sim = pbf.Simulator(scene.pos, scene.vel, prm, device=local)
+    n = sim.n
+    dt = prm.dt
+    stream = torch.cuda.ExternalStream(sim.stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    sim.sort()
+    sim.snapshot()
+    for _ in range(args.warmup):
+        sim.restore()
+        sim.step_async(dt, 1)
+    sim.sync()
+
+    gpu_index = local
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        try:
+            gpu_index = int(vis.split(",")[local])
+        except ValueError:
+            pass
+    clocks = ClockSampler(gpu_index)
+    time.sleep(0.3)
+    sim.set_profiling(True)
+    sim.reset_phase_times()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            sim.restore()
+            flush.zero_()
+            starts[k].record(stream)
+            sim.step_async(dt, 1)
+            ends[k].record(stream)
+    sim.sync()
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    phases = sim.phase_times()
+    sim.set_profiling(False)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = reduce_max(sum(step_ms), world)
+    value = world * n * args.steps / (total_ms / 1e3)
+    stats = sim.stats()
+
+    # dominant kernel (by device time in the timed region) and its roofline
+    peak, peak_kind = peaks()
+    dom = max((k for k in phases if ALGO_BYTES.get(k, 0) > 0), key=lambda k: phases[k][0])
+    dom_ms, dom_launches = phases[dom]
+    per_launch_s = dom_ms / max(dom_launches, 1) / 1e3
+    algo = ALGO_BYTES[dom] * n
+    achieved = algo / per_launch_s / 1e9
+    traffic = NCU_TRAFFIC_PER_PARTICLE.get(dom)
+    step_bytes = (340 + 56 * prm.iters) * n
+    launches = int(sum(v[1] for v in phases.values()))
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        xh = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+        vh = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+        x0 = scene.pos.astype(np.float32)
+        v0 = scene.vel.astype(np.float32)
+        L = pbf.lib()
+        xp, vp = xh.ctypes.data_as(pbf.P), vh.ctypes.data_as(pbf.P)
+        tot = 0.0
+        e2e_steps = max(1, args.steps)
+        for k in range(e2e_steps + 1):
+            xh[:] = x0  # the configured input, as a host caller would hand it over
+            vh[:] = v0
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rc = L.pbf_set_state(sim._h, xp, vp)
+            rc |= L.pbf_step(sim._h, dt, 1)
+            rc |= L.pbf_get_positions(sim._h, xp)
+            rc |= L.pbf_get_velocities(sim._h, vp)
+            t1 = time.perf_counter()
+            if rc:
+                raise RuntimeError(L.pbf_last_error(sim._h).decode())
+            if k > 0:  # the first iteration warms the unsorted-input path
+                tot += t1 - t0
+        tot = reduce_max(tot, world)
+        e2e = {"value": world * n * e2e_steps / tot, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 12,
+               "d2h_bytes_per_step": 2 * n * 12, "ms_per_step": tot / e2e_steps * 1e3,
+               "path": "pbf_set_state + pbf_step + pbf_get_positions + pbf_get_velocities, pinned host buffers"}
+    sim.close()
+
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(scene),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": None if traffic is None else traffic * n,
+                     "algo_bytes_per_launch": algo, "avg_launch_ms": per_launch_s * 1e3,
+                     "step_frac": step_bytes / (total_ms / args.steps / 1e3) / 1e9 / peak},
+        "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items()},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "stats": {"mean_density_over_rho0": stats["mean_density"] / prm.rest_density,
+                  "mean_neighbors": stats["mean_neighbors"], "max_neighbors": stats["max_neighbors"]},
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
+        line["cpu_port_all_cores"] = cpu_port_all_cores(scene, min(args.cpu_seconds, 10.0))
+    print(json.dumps(line))
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="colliding_blocks_1m")
+    ap.add_argument("--seed", type=int, default=None)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    from fluid_gb300 import scenes
+
+    world, rank, local = dist_setup()
+    if world > 1 and args.impl == "ours":
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    build = scenes.SCENES[args.workload]
+    scene = build() if args.seed is None else build(args.seed)
+    try:
+        if args.impl == "reference":
+            return bench_reference(args, scene, world, rank)
+        return bench_ours(args, scene, world, rank, local)
+    finally:
+        if world > 1 and args.impl == "ours":
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -152,10 +152,14 @@ void Handle::free_all() {
   void* ptrs[] = {b.pos[0], b.pos[1], b.disp[0], b.disp[1], b.xs[0], b.xs[1], b.vel[0], b.vel[1],
                   b.omega, b.pred, b.lam, b.rho, b.rho_iter0, b.id[0], b.id[1], b.key, b.rank,
                   b.perm, b.nbr_hdr, b.nbr_w, b.cell_count, b.cell_start, b.scan_tmp, b.scenes,
-                  b.stats, b.err, b.io, b.io2, scratch};
+                  b.stats, b.err, b.io, b.io2, scratch, snap_pos, snap_vel, snap_id};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   b = Buffers();
+  snap_pos = snap_vel = nullptr;
+  snap_id = nullptr;
+  snap_valid = false;
+  free_profiling();
   scratch = nullptr;
   scratch_bytes = 0;
   if (stream) cudaStreamDestroy(stream);
@@ -217,8 +221,51 @@ pbf_status Handle::sync_and_check() {
   return PBF_OK;
 }
 
+PhaseMarks Handle::next_marks() {
+  const int cap = 8 + 2 * params.iters + 4;
+  if (prof_used == prof_events.size()) {
+    std::vector<cudaEvent_t> ev(cap, nullptr);
+    for (auto& e : ev) cudaEventCreate(&e);
+    prof_events.push_back(ev);
+    prof_phase.push_back(std::vector<int>(cap, -1));
+    prof_count.push_back(0);
+  }
+  PhaseMarks m;
+  m.ev = prof_events[prof_used].data();
+  m.phase = prof_phase[prof_used].data();
+  m.cap = static_cast<int>(prof_events[prof_used].size());
+  return m;
+}
+
+pbf_status Handle::collect_phase_times() {
+  if (prof_used == 0) return PBF_OK;
+  pbf_status st = cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+  if (st != PBF_OK) return st;
+  for (size_t k = 0; k < prof_used; ++k) {
+    for (int q = 1; q < prof_count[k]; ++q) {
+      float ms = 0.f;
+      st = cuda(cudaEventElapsedTime(&ms, prof_events[k][q - 1], prof_events[k][q]), "cudaEventElapsedTime");
+      if (st != PBF_OK) return st;
+      const int ph = prof_phase[k][q];
+      if (ph >= 0 && ph < kNumPhases) phase_ms[ph] += ms;
+    }
+  }
+  prof_used = 0;
+  return PBF_OK;
+}
+
+void Handle::free_profiling() {
+  for (auto& set : prof_events)
+    for (auto& e : set)
+      if (e) cudaEventDestroy(e);
+  prof_events.clear();
+  prof_phase.clear();
+  prof_count.clear();
+  prof_used = 0;
+}
+
 pbf_status Handle::enqueue_steps(float dt, int nsteps) {
-  const bool use_graph = (params.flags & PBF_FLAG_GRAPH) != 0;
+  const bool use_graph = (params.flags & PBF_FLAG_GRAPH) != 0 && !profiling;
   const bool keep_pred = b.pred != nullptr;
   for (int k = 0; k < nsteps; ++k) {
     if (use_graph) {
@@ -247,6 +294,20 @@ pbf_status Handle::enqueue_steps(float dt, int nsteps) {
       }
       pbf_status st = cuda(cudaGraphLaunch(graph[cur], stream), "cudaGraphLaunch");
       if (st != PBF_OK) return st;
+    } else if (profiling) {
+      PhaseMarks m = next_marks();
+      pbf_status st =
+          cuda(launch_step(b, dp, tune, cur, dt, params.iters, keep_pred, stream, &m), "launch step");
+      if (st != PBF_OK) return st;
+      prof_count[prof_used++] = m.count;
+      const int it = params.iters;
+      const uint64_t per_step[kNumPhases] = {1, 3, 2, 1, 1, static_cast<uint64_t>(it), static_cast<uint64_t>(it),
+                                             1, 1, dp.stats ? 2u : 0u};
+      for (int q = 0; q < kNumPhases; ++q) phase_launches[q] += per_step[q];
+      if (prof_used >= 256) {
+        st = collect_phase_times();
+        if (st != PBF_OK) return st;
+      }
     } else {
       pbf_status st = cuda(launch_step(b, dp, tune, cur, dt, params.iters, keep_pred, stream), "launch step");
       if (st != PBF_OK) return st;
@@ -668,6 +729,104 @@ pbf_status pbf_get_predicted(pbf_handle* hh, float* xyz) {
   pbf_status st = h->cuda(pbf::launch_unsort_f4(h->b, h->cur, h->b.pred, h->b.io, h->stream), "unsort");
   if (st == PBF_OK) st = h->cuda(cudaMemcpyAsync(xyz, h->b.io, 3 * sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
   if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "sync");
+  return st;
+}
+
+pbf_status pbf_sort(pbf_handle* hh) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  pbf::DeviceGuard g(h->device);
+  if (h->b.n == 0) return PBF_OK;
+  pbf_status st = h->cuda(pbf::launch_resort(h->b, h->dp, h->tune, h->cur, h->stream), "resort");
+  if (st != PBF_OK) return st;
+  h->cur ^= 1;
+  h->nbr_valid = false;
+  return h->cuda(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+}
+
+pbf_status pbf_snapshot(pbf_handle* hh) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  pbf::DeviceGuard g(h->device);
+  const size_t n = h->b.n ? h->b.n : 1;
+  pbf_status st = PBF_OK;
+  if (!h->snap_pos) st = h->cuda(cudaMalloc((void**)&h->snap_pos, sizeof(float4) * n), "cudaMalloc");
+  if (st == PBF_OK && !h->snap_vel) st = h->cuda(cudaMalloc((void**)&h->snap_vel, sizeof(float4) * n), "cudaMalloc");
+  if (st == PBF_OK && !h->snap_id) st = h->cuda(cudaMalloc((void**)&h->snap_id, sizeof(uint32_t) * n), "cudaMalloc");
+  if (st != PBF_OK) return st;
+  const size_t m = h->b.n;
+  st = h->cuda(cudaMemcpyAsync(h->snap_pos, h->b.pos[h->cur], sizeof(float4) * m, cudaMemcpyDeviceToDevice, h->stream), "copy");
+  if (st == PBF_OK)
+    st = h->cuda(cudaMemcpyAsync(h->snap_vel, h->b.vel[h->cur], sizeof(float4) * m, cudaMemcpyDeviceToDevice, h->stream), "copy");
+  if (st == PBF_OK)
+    st = h->cuda(cudaMemcpyAsync(h->snap_id, h->b.id[h->cur], sizeof(uint32_t) * m, cudaMemcpyDeviceToDevice, h->stream), "copy");
+  if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+  if (st == PBF_OK) {
+    h->snap_valid = true;
+    h->snap_steps = h->steps;
+    h->snap_time = h->simulate_time;
+  }
+  return st;
+}
+
+pbf_status pbf_restore(pbf_handle* hh) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h->snap_valid) return h->fail(PBF_ERR_INVALID, "no snapshot taken");
+  pbf::DeviceGuard g(h->device);
+  const size_t m = h->b.n;
+  pbf_status st =
+      h->cuda(cudaMemcpyAsync(h->b.pos[h->cur], h->snap_pos, sizeof(float4) * m, cudaMemcpyDeviceToDevice, h->stream), "copy");
+  if (st == PBF_OK)
+    st = h->cuda(cudaMemcpyAsync(h->b.vel[h->cur], h->snap_vel, sizeof(float4) * m, cudaMemcpyDeviceToDevice, h->stream), "copy");
+  if (st == PBF_OK)
+    st = h->cuda(cudaMemcpyAsync(h->b.id[h->cur], h->snap_id, sizeof(uint32_t) * m, cudaMemcpyDeviceToDevice, h->stream), "copy");
+  h->nbr_valid = false;
+  h->steps = h->snap_steps;
+  h->simulate_time = h->snap_time;
+  return st;
+}
+
+static const char* kPhaseNames[pbf::kNumPhases] = {"predict", "scan", "sort", "gather", "neighbors",
+                                                    "lambda", "deltap", "xsph", "vorticity", "stats"};
+
+const char* pbf_phase_name(int phase) {
+  return (phase >= 0 && phase < pbf::kNumPhases) ? kPhaseNames[phase] : "";
+}
+
+int pbf_num_phases(void) { return pbf::kNumPhases; }
+
+pbf_status pbf_set_profiling(pbf_handle* hh, int enable) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  pbf::DeviceGuard g(h->device);
+  pbf_status st = h->collect_phase_times();
+  h->profiling = enable != 0;
+  return st;
+}
+
+pbf_status pbf_get_phase_times(pbf_handle* hh, double* ms, uint64_t* launches, int max_phases) {
+  if (!hh || max_phases < 0) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  pbf::DeviceGuard g(h->device);
+  pbf_status st = h->collect_phase_times();
+  if (st != PBF_OK) return st;
+  for (int q = 0; q < max_phases && q < pbf::kNumPhases; ++q) {
+    if (ms) ms[q] = h->phase_ms[q];
+    if (launches) launches[q] = h->phase_launches[q];
+  }
+  return PBF_OK;
+}
+
+pbf_status pbf_reset_phase_times(pbf_handle* hh) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  pbf::DeviceGuard g(h->device);
+  pbf_status st = h->collect_phase_times();
+  for (int q = 0; q < pbf::kNumPhases; ++q) {
+    h->phase_ms[q] = 0;
+    h->phase_launches[q] = 0;
+  }
   return st;
 }
 

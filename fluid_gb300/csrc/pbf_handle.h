@@ -36,6 +36,21 @@ struct Handle {
   float graph_dt = -1.f;
   void* scratch = nullptr;   // grow-only scratch for introspection and queries
   size_t scratch_bytes = 0;
+  // per-phase CUDA-event timing (pbf_set_profiling)
+  bool profiling = false;
+  std::vector<std::vector<cudaEvent_t>> prof_events;  // one set per step in flight
+  std::vector<std::vector<int>> prof_phase;
+  std::vector<int> prof_count;
+  size_t prof_used = 0;
+  // device-side snapshot (pbf_snapshot / pbf_restore)
+  float4* snap_pos = nullptr;
+  float4* snap_vel = nullptr;
+  uint32_t* snap_id = nullptr;
+  bool snap_valid = false;
+  uint64_t snap_steps = 0;
+  double snap_time = 0;
+  double phase_ms[kNumPhases] = {};
+  uint64_t phase_launches[kNumPhases] = {};
 
   pbf_status fail(pbf_status st, const std::string& msg);
   pbf_status cuda(cudaError_t e, const char* what);
@@ -45,6 +60,9 @@ struct Handle {
   pbf_status enqueue_steps(float dt, int nsteps);
   pbf_status sync_and_check();
   void drop_graphs();
+  PhaseMarks next_marks();
+  pbf_status collect_phase_times();
+  void free_profiling();
 
   // Order the handle's stream after `other` (or the legacy default stream
   // when other is null), and back.

@@ -104,11 +104,42 @@ struct Tuning {
   int block_misc = 256;
 };
 
+// Phases of a step for CUDA-event timing (pbf_get_phase_times).
+enum Phase {
+  kPhasePredict = 0,
+  kPhaseScan,
+  kPhaseSort,
+  kPhaseGather,
+  kPhaseNeighbors,
+  kPhaseLambda,
+  kPhaseDeltaP,
+  kPhaseXsph,
+  kPhaseVorticity,
+  kPhaseStats,
+  kNumPhases
+};
+
+// Events recorded between phases of one step (optional).
+struct PhaseMarks {
+  cudaEvent_t* ev = nullptr;
+  int* phase = nullptr;
+  int count = 0;
+  int cap = 0;
+  void mark(int ph, cudaStream_t s) {
+    if (ev && count < cap) {
+      cudaEventRecord(ev[count], s);
+      phase[count] = ph;
+      ++count;
+    }
+  }
+};
+
 // ---- launchers (pbf_kernels.cu) ----
 // cur: index of the buffers holding the current (sorted) state; the step
 // writes the next state into 1 - cur.
 cudaError_t launch_step(const Buffers& b, const DevParams& p, const Tuning& t, int cur,
-                        float dt, int iters, bool keep_pred, cudaStream_t s);
+                        float dt, int iters, bool keep_pred, cudaStream_t s,
+                        PhaseMarks* marks = nullptr);
 cudaError_t launch_resort(const Buffers& b, const DevParams& p, const Tuning& t, int cur,
                           cudaStream_t s);
 cudaError_t launch_upload(const Buffers& b, int cur, const float* xyz, const float* vel,

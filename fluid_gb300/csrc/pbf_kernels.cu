@@ -624,19 +624,22 @@ inline unsigned blocks_for(size_t n, int block) { return static_cast<unsigned>((
 
 // Shared front half of a step and of a resort: keys, counts, scan, slots.
 cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& t, int cur, float dt,
-                            bool move, cudaStream_t s) {
+                            bool move, cudaStream_t s, PhaseMarks* mk = nullptr) {
   const int n = static_cast<int>(b.n);
   const uint32_t m = b.n_cells;
   cudaError_t e = cudaMemsetAsync(b.cell_count, 0, sizeof(uint32_t) * m, s);
   if (e != cudaSuccess) return e;
   k_predict<<<blocks_for(n, t.block_predict), t.block_predict, 0, s>>>(
       b.pos[cur], b.vel[cur], b.disp[0], b.key, b.rank, b.cell_count, b.scenes, P, dt, move ? 1 : 0, n);
+  if (mk) mk->mark(kPhasePredict, s);
   const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
   k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(b.cell_count, b.cell_start, b.scan_tmp, m);
   k_scan_sums<<<1, 1024, 0, s>>>(b.scan_tmp, tiles, b.cell_start, m);
   k_scan_add<<<tiles, kScanThreads, 0, s>>>(b.cell_start, b.scan_tmp, m);
+  if (mk) mk->mark(kPhaseScan, s);
   k_scatter<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(b.key, b.rank, b.cell_start, b.perm, n);
   k_cellsort<<<blocks_for(m, t.block_misc), t.block_misc, 0, s>>>(b.cell_start, b.perm, b.id[cur], m);
+  if (mk) mk->mark(kPhaseSort, s);
   return cudaGetLastError();
 }
 
@@ -651,12 +654,14 @@ cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& 
   }
 
 cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, int cur, float dt,
-                        int iters, bool keep_pred, cudaStream_t s) {
+                        int iters, bool keep_pred, cudaStream_t s, PhaseMarks* mk) {
   const int n = static_cast<int>(b.n);
   if (n == 0) return cudaSuccess;
   const int A = cur, B = 1 - cur;
+  if (mk) mk->mark(-1, s);
   if (P.stats) k_stats_init<<<1, 1, 0, s>>>(b.stats);
-  cudaError_t e = sort_into_cells(b, P, t, A, dt, true, s);
+  if (mk) mk->mark(kPhaseStats, s);
+  cudaError_t e = sort_into_cells(b, P, t, A, dt, true, s, mk);
   if (e != cudaSuccess) return e;
   k_gather<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(
       b.perm, b.pos[A], b.disp[0], nullptr, b.id[A], b.pos[B], b.disp[1], b.xs[0], nullptr, b.id[B], n);
@@ -664,9 +669,11 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
     e = cudaMemcpyAsync(b.pred, b.xs[0], sizeof(float4) * b.n, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return e;
   }
+  if (mk) mk->mark(kPhaseGather, s);
   PBF_BLOCK_SWITCH(t.block_nbr,
                    k_nbr_build<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
                        b.xs[0], b.pos[B], b.cell_start, b.scenes, b.nbr_hdr, b.nbr_w, b.err, P, n));
+  if (mk) mk->mark(kPhaseNeighbors, s);
   for (int it = 0; it < iters; ++it) {
     const float4* xcur = b.xs[it & 1];
     float4* xnext = b.xs[(it + 1) & 1];
@@ -674,22 +681,27 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
                      k_lambda<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
                          xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.lam,
                          (it == 0 && P.stats) ? b.rho_iter0 : nullptr, P, n));
+    if (mk) mk->mark(kPhaseLambda, s);
     PBF_BLOCK_SWITCH(t.block_solve,
                      k_deltap<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
                          xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.lam, b.disp[1],
                          xnext, P, n));
+    if (mk) mk->mark(kPhaseDeltaP, s);
   }
   const float4* fin = b.xs[iters & 1];
   PBF_BLOCK_SWITCH(t.block_solve,
                    k_xsph<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
                        fin, b.pos[B], b.disp[1], b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.vel[B],
                        b.omega, b.rho, P, 1.0f / dt, n));
+  if (mk) mk->mark(kPhaseXsph, s);
   PBF_BLOCK_SWITCH(t.block_solve,
                    k_vort<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
                        fin, b.pos[B], b.omega, b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.vel[B],
                        b.err, P, dt, n));
+  if (mk) mk->mark(kPhaseVorticity, s);
   if (P.stats)
     k_stats<<<blocks_for(n, 256), 256, 0, s>>>(b.rho, b.rho_iter0, b.nbr_hdr, b.stats, P.inv_rho0, n);
+  if (mk) mk->mark(kPhaseStats, s);
   return cudaGetLastError();
 }
 

@@ -72,6 +72,14 @@ def _declare(L):
         "pbf_get_neighbors": (st, [P, P, P, sz, P]),
         "pbf_get_cells": (st, [P, P]),
         "pbf_get_predicted": (st, [P, P]),
+        "pbf_sort": (st, [P]),
+        "pbf_snapshot": (st, [P]),
+        "pbf_restore": (st, [P]),
+        "pbf_set_profiling": (st, [P, ctypes.c_int]),
+        "pbf_get_phase_times": (st, [P, P, P, ctypes.c_int]),
+        "pbf_reset_phase_times": (st, [P]),
+        "pbf_num_phases": (ctypes.c_int, []),
+        "pbf_phase_name": (ctypes.c_char_p, [ctypes.c_int]),
         "pbf_size": (sz, [P]),
         "pbf_num_scenes": (ctypes.c_int, [P]),
         "pbf_last_error": (ctypes.c_char_p, [P]),
@@ -241,6 +249,29 @@ class Simulator:
         out = np.zeros(self.n, dtype=np.uint32)
         self._check(lib().pbf_get_cells(self._h, _ptr(out)))
         return out
+
+    def sort(self):
+        self._check(lib().pbf_sort(self._h))
+
+    def snapshot(self):
+        self._check(lib().pbf_snapshot(self._h))
+
+    def restore(self):
+        self._check(lib().pbf_restore(self._h))
+
+    def set_profiling(self, on: bool = True):
+        self._check(lib().pbf_set_profiling(self._h, 1 if on else 0))
+
+    def reset_phase_times(self):
+        self._check(lib().pbf_reset_phase_times(self._h))
+
+    def phase_times(self) -> dict:
+        """{phase: (device ms, kernel launches)} accumulated since the last reset."""
+        k = lib().pbf_num_phases()
+        ms = np.zeros(k, dtype=np.float64)
+        cnt = np.zeros(k, dtype=np.uint64)
+        self._check(lib().pbf_get_phase_times(self._h, _ptr(ms), _ptr(cnt), k))
+        return {lib().pbf_phase_name(q).decode(): (float(ms[q]), int(cnt[q])) for q in range(k)}
 
     def predicted(self) -> np.ndarray:
         out = np.empty((self.n, 3), dtype=np.float32)

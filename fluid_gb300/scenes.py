@@ -5,12 +5,11 @@ is a pure function of (name, seed) on every machine. Positions and velocities ar
 FP64 here; the CUDA path receives them rounded to FP32.
 
 Mass convention. The reference step has implicit unit particle mass
-(src/particles.cpp:185-204 sums W without a mass factor). A scene quoted with a
-physical rest density rho0 and lattice spacing s has particle mass m = rho0*s^3, and
-the reference formulas reproduce that fluid with ``rest_density = rho0/m = 1/s^3``.
-XSPH (particles.cpp:233) and vorticity (particles.cpp:242) carry no m/rho factor in
-the reference; ``physical_params(..., scale="mass")`` folds m/rho0 = s^3 into the
-coefficients so long rollouts stay stable, ``scale="ref"`` keeps the raw constants.
+(src/particles.cpp:185-204 sums W without a mass factor and without the self term).
+A scene quoted with a physical rest density and lattice spacing s is expressed in the
+reference's formulas by ``physical_params``: the rest density is the lattice's own
+density, and the dimensional constants the reference tuned at H = 0.3 are carried to
+the scene's resolution (see ``physical_params``).
 """
 from __future__ import annotations
 
@@ -64,29 +63,53 @@ def lattice(nx: int, ny: int, nz: int, spacing: float, corner=(0.0, 0.0, 0.0)) -
     return (pts + 0.5) * spacing + np.asarray(corner, dtype=np.float64)
 
 
-def physical_params(h: float, spacing: float, rho0: float = 1000.0, scale: str = "mass", **kw) -> PbfParams:
-    """Reference-formula parameters for a fluid of physical rest density ``rho0``.
+def lattice_density(h: float, h2: float, spacing: float) -> float:
+    """Density the reference's formula gives a particle inside a perfect cubic lattice.
 
-    The reference's unit-mass formulas need ``rest_density = rho0 / m = 1/s^3``.
-    ``scale="mass"`` multiplies the XSPH and vorticity coefficients by m/rho0 = s^3.
+    particles.cpp:185-204 sums poly6 over neighbours only (no self term), so a lattice of
+    spacing s has density sum_{j != i} W(x_i - x_j) = 0.814/s^3 for h = 2s, not 1/s^3.
+    """
+    m = int(math.ceil(h / spacing)) + 1
+    r = np.arange(-m, m + 1) * spacing
+    X, Y, Z = np.meshgrid(r, r, r, indexing="ij")
+    r2 = X * X + Y * Y + Z * Z
+    r2[m, m, m] = np.inf
+    w = np.where(r2 < h2, 1.56668147106 * (h2 - r2) ** 3 / h ** 9, 0.0)
+    return float(w.sum())
+
+
+REFERENCE_H = 0.3   # particles.cpp:26: the resolution the reference's constants were tuned at
+PAPER_H = 0.1       # Macklin & Mueller (2013) scenes, where tensile k = 0.1 is quoted
+
+
+def physical_params(h: float, spacing: float, scale: str = "mass", *, xsph_c: float = 0.001,
+                    vort_eps: float = 0.001, epsilon: float = 2.0, scorr_k: float = 0.0001,
+                    scorr_k_h: float = REFERENCE_H, **kw) -> PbfParams:
+    """Reference-formula parameters for a fluid sampled at lattice spacing ``spacing``.
+
+    The reference's formulas are kept exactly; only the constants are chosen here.
+    ``scale="mass"`` transfers the reference's dimensional constants to resolution h:
+    rest density = the lattice's own density (the configured fluid starts at rest),
+    EPSILON (units of |grad C|^2 ~ 1/h^2) times (0.3/h)^2, the tensile K (added to
+    lambda ~ h^2) times (h/h_K)^2 where h_K is the resolution K was quoted at, and the
+    XSPH / vorticity coefficients (multiplying sums of W ~ number density) divided by
+    the rest density. ``scale="ref"`` uses the raw constants with rest density 1/s^3.
     Unspecified parameters take the reference defaults except g = -9.8 y, dt = 1/60
     and a [0,1]^3 collider box.
     """
-    vol = spacing ** 3
-    base = dict(
-        h=h, h2=decimal_square(h), iters=4, dt=1.0 / 60.0, gravity=(0.0, -9.8, 0.0),
-        rest_density=1.0 / vol, box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0),
-    )
-    xsph_c = kw.pop("xsph_c", 0.001)
-    vort_eps = kw.pop("vort_eps", 0.001)
+    h2 = decimal_square(h)
+    base = dict(h=h, h2=h2, iters=4, dt=1.0 / 60.0, gravity=(0.0, -9.8, 0.0),
+                box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0))
     if scale == "mass":
-        xsph_c *= vol
-        vort_eps *= vol
-    elif scale != "ref":
+        rho0 = lattice_density(h, h2, spacing)
+        base.update(rest_density=rho0, epsilon=epsilon * (REFERENCE_H / h) ** 2,
+                    scorr_k=scorr_k * (h / scorr_k_h) ** 2, xsph_c=xsph_c / rho0, vort_eps=vort_eps / rho0)
+    elif scale == "ref":
+        base.update(rest_density=1.0 / spacing ** 3, epsilon=epsilon, scorr_k=scorr_k, xsph_c=xsph_c,
+                    vort_eps=vort_eps)
+    else:
         raise ValueError(f"unknown scale {scale!r}")
-    base.update(xsph_c=xsph_c, vort_eps=vort_eps)
     base.update(kw)
-    del rho0  # the physical density only fixes the particle mass, which cancels
     return PbfParams(**base)
 
 
@@ -138,7 +161,7 @@ def colliding_blocks_1m(seed: int = 3) -> Scene:
     v = normal(seed, p.size, 0.01, stream=1).reshape(p.shape)
     v[: a.shape[0], 0] += 1.0
     v[a.shape[0]:, 0] -= 1.0
-    prm = physical_params(h, s, scorr_k=0.1, scorr_n=4)
+    prm = physical_params(h, s, scorr_k=0.1, scorr_k_h=PAPER_H, scorr_n=4)
     return Scene("colliding_blocks_1m", p, v, prm, 200, seed,
                  notes="blocks 0.4x0.8x0.4 m at x in [0,0.4) and [0.6,1.0); position jitter +-0.8% of s")
 

@@ -152,6 +152,16 @@ PBF_API pbf_status pbf_set_state_device(pbf_handle* h, const float* xyz,
 PBF_API pbf_status pbf_get_state_device(pbf_handle* h, float* xyz, float* vel,
                                 float* rho, void* stream);
 
+/* Reorder the current state into cell order without moving it (the step
+ * does this every step; a fresh handle holds the input order). */
+PBF_API pbf_status pbf_sort(pbf_handle* h);
+
+/* Device-side checkpoint of the state (positions, velocities, particle order,
+ * step count, simulate_time); pbf_restore rolls back to it, enqueued on the
+ * handle's stream without waiting. The reference has no checkpointing. */
+PBF_API pbf_status pbf_snapshot(pbf_handle* h);
+PBF_API pbf_status pbf_restore(pbf_handle* h);
+
 /* Particles::estimateDensities (particles.cpp:440-444): density of every
  * particle at its current position, self included; host out[n]. */
 PBF_API pbf_status pbf_estimate_densities(pbf_handle* h, float* rho);
@@ -172,6 +182,20 @@ PBF_API pbf_status pbf_get_neighbors(pbf_handle* h, uint32_t* counts, uint32_t* 
                              size_t cap, size_t* total);
 PBF_API pbf_status pbf_get_cells(pbf_handle* h, uint32_t* cells);
 PBF_API pbf_status pbf_get_predicted(pbf_handle* h, float* xyz);
+
+/*
+ * Per-phase CUDA-event timing (the reference times nothing on this path; it
+ * prints progress, particles.cpp:251-295). While enabled, steps run without
+ * graph replay and record an event after each phase on the handle's stream.
+ * pbf_get_phase_times waits and returns, per phase, the accumulated device
+ * milliseconds and the number of kernel launches since the last reset.
+ */
+PBF_API pbf_status pbf_set_profiling(pbf_handle* h, int enable);
+PBF_API pbf_status pbf_get_phase_times(pbf_handle* h, double* ms,
+                                       uint64_t* launches, int max_phases);
+PBF_API pbf_status pbf_reset_phase_times(pbf_handle* h);
+PBF_API int pbf_num_phases(void);
+PBF_API const char* pbf_phase_name(int phase);
 
 PBF_API size_t pbf_size(const pbf_handle* h);
 PBF_API int pbf_num_scenes(const pbf_handle* h);

@@ -49,6 +49,9 @@ def lib():
         L.orc_step.argtypes = [P, ctypes.c_int64, P, P, P, ctypes.c_int, ctypes.c_double,
                                P, P, ctypes.c_int64, P, P, ctypes.c_int]
         L.orc_step.restype = ctypes.c_int
+        L.orc_step2.argtypes = [P, ctypes.c_int64, P, P, P, ctypes.c_int, ctypes.c_double,
+                                P, P, ctypes.c_int64, P, P, P, P, ctypes.c_int]
+        L.orc_step2.restype = ctypes.c_int
         L.orc_estimate_densities.argtypes = [P, ctypes.c_int64, P, P, ctypes.c_int]
         L.orc_estimate_densities.restype = ctypes.c_int
         L.orc_estimate_density_at.argtypes = [P, ctypes.c_int64, P, ctypes.c_int64, P, P, ctypes.c_int]
@@ -63,8 +66,12 @@ def _ptr(a):
 
 
 def step(pos, vel, params: PbfParams, steps: int = 1, dt: float | None = None,
-         neighbors: bool = False, predicted: bool = False, threads: int = 0) -> dict:
-    """``steps`` FP64 steps from (pos, vel); returns pos, vel, density (+ neighbour CSR)."""
+         neighbors: bool = False, predicted: bool = False, threads: int = 0,
+         given_neighbors=None) -> dict:
+    """``steps`` FP64 steps from (pos, vel); returns pos, vel, density (+ neighbour CSR).
+
+    ``given_neighbors=(offsets, ids)`` replaces the first step's neighbour search.
+    """
     L = lib()
     pos = np.array(pos, dtype=np.float64, order="C", copy=True)
     vel = np.array(vel, dtype=np.float64, order="C", copy=True)
@@ -78,14 +85,24 @@ def step(pos, vel, params: PbfParams, steps: int = 1, dt: float | None = None,
     idx = np.zeros(max(cap, 1), dtype=np.int64) if neighbors else None
     dtv = params.dt if dt is None else dt
     pos0, vel0 = pos.copy(), vel.copy()
-    rc = L.orc_step(ctypes.byref(cp), n, _ptr(pos), _ptr(vel), _ptr(rho), steps, dtv,
-                    _ptr(off), _ptr(idx), cap, _ptr(pred), _ptr(rho0), threads)
+    g_off = g_idx = None
+    if given_neighbors is not None:
+        g_off = np.ascontiguousarray(given_neighbors[0], dtype=np.int64)
+        g_idx = np.ascontiguousarray(given_neighbors[1], dtype=np.int64)
+        if g_idx.size == 0:
+            g_idx = np.zeros(1, dtype=np.int64)
+
+    def call():
+        return L.orc_step2(ctypes.byref(cp), n, _ptr(pos), _ptr(vel), _ptr(rho), steps, dtv,
+                           _ptr(off), _ptr(idx), cap, _ptr(pred), _ptr(rho0), _ptr(g_off), _ptr(g_idx),
+                           threads)
+
+    rc = call()
     if rc == 1 and neighbors:  # rerun with the exact capacity the last step needed
         cap = int(off[-1])
         idx = np.zeros(max(cap, 1), dtype=np.int64)
-        pos, vel = pos0, vel0
-        rc = L.orc_step(ctypes.byref(cp), n, _ptr(pos), _ptr(vel), _ptr(rho), steps, dtv,
-                        _ptr(off), _ptr(idx), cap, _ptr(pred), _ptr(rho0), threads)
+        pos, vel = pos0, vel0.copy()
+        rc = call()
     if rc != 0:
         raise RuntimeError(f"orc_step failed: {rc}")
     out = {"pos": pos, "vel": vel, "density": rho, "mean_density_iter0": rho0[:steps]}

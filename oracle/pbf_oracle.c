@@ -356,7 +356,7 @@ typedef struct {
  * nb receives the neighbour lists of this step (caller frees).
  */
 static int step_once(const ctx_t* c, int64_t n, v3* x, v3* v, double* rho, double dt,
-                     nbrs_t* nb, v3* pred_out, step_info_t* info) {
+                     nbrs_t* nb, const nbrs_t* given, v3* pred_out, step_info_t* info) {
   v3* xs = (v3*)malloc(sizeof(v3) * (size_t)(n ? n : 1));
   double* lam = (double*)malloc(sizeof(double) * (size_t)(n ? n : 1));
   v3* vort = (v3*)malloc(sizeof(v3) * (size_t)(n ? n : 1));
@@ -374,8 +374,18 @@ static int step_once(const ctx_t* c, int64_t n, v3* x, v3* v, double* rho, doubl
   }
   if (pred_out) memcpy(pred_out, xs, sizeof(v3) * (size_t)n);
 
-  int rc = find_neighbors(c, n, xs, nb);
-  if (rc) return rc;
+  int rc = 0;
+  if (given) {
+    /* caller-supplied neighbour sets (ascending per particle) replace the search */
+    nb->off = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n + 1));
+    nb->idx = (int64_t*)malloc(sizeof(int64_t) * (size_t)(given->off[n] > 0 ? given->off[n] : 1));
+    if (!nb->off || !nb->idx) return -1;
+    memcpy(nb->off, given->off, sizeof(int64_t) * (size_t)(n + 1));
+    if (given->off[n] > 0) memcpy(nb->idx, given->idx, sizeof(int64_t) * (size_t)given->off[n]);
+  } else {
+    rc = find_neighbors(c, n, xs, nb);
+    if (rc) return rc;
+  }
   const int64_t* off = nb->off;
   const int64_t* idx = nb->idx;
   int64_t nnz = off[n];
@@ -494,11 +504,14 @@ int orc_max_threads(void) {
  * lists are written to nbr_off / nbr_idx (capacity nbr_cap); returns 1 if the
  * capacity was too small (nbr_off[n] then holds the needed count). pred
  * ((n,3) or NULL) receives x* after the last prediction; rho_iter0 (nsteps or
- * NULL) the mean density after each step's first lambda pass.
+ * NULL) the mean density after each step's first lambda pass. orc_step2 also takes
+ * the first step's neighbour sets from in_off/in_idx (ascending lists) instead of
+ * searching, so an FP32 implementation can be compared on identical sets.
  */
-int orc_step(const pbf_params* prm, int64_t n, double* pos, double* vel, double* rho,
-             int nsteps, double dt, int64_t* nbr_off, int64_t* nbr_idx, int64_t nbr_cap,
-             double* pred, double* rho_iter0, int nthreads) {
+int orc_step2(const pbf_params* prm, int64_t n, double* pos, double* vel, double* rho,
+              int nsteps, double dt, int64_t* nbr_off, int64_t* nbr_idx, int64_t nbr_cap,
+              double* pred, double* rho_iter0, const int64_t* in_off, const int64_t* in_idx,
+              int nthreads) {
   set_threads(nthreads);
   ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
   if (!c) return -1;
@@ -507,7 +520,8 @@ int orc_step(const pbf_params* prm, int64_t n, double* pos, double* vel, double*
   for (int s = 0; s < nsteps && rc == 0; s++) {
     nbrs_t nb = {NULL, NULL};
     step_info_t info = {0};
-    rc = step_once(c, n, (v3*)pos, (v3*)vel, rho, dt, &nb,
+    nbrs_t given = {(int64_t*)in_off, (int64_t*)in_idx};
+    rc = step_once(c, n, (v3*)pos, (v3*)vel, rho, dt, &nb, (in_off && s == 0) ? &given : NULL,
                    (pred && s == nsteps - 1) ? (v3*)pred : NULL, &info);
     if (rc == 0 && rho_iter0) rho_iter0[s] = n ? info.density_iter0_sum / (double)n : 0.0;
     if (rc == 0 && s == nsteps - 1 && nbr_off) {
@@ -523,6 +537,13 @@ int orc_step(const pbf_params* prm, int64_t n, double* pos, double* vel, double*
   }
   free(c);
   return rc;
+}
+
+int orc_step(const pbf_params* prm, int64_t n, double* pos, double* vel, double* rho,
+             int nsteps, double dt, int64_t* nbr_off, int64_t* nbr_idx, int64_t nbr_cap,
+             double* pred, double* rho_iter0, int nthreads) {
+  return orc_step2(prm, n, pos, vel, rho, nsteps, dt, nbr_off, nbr_idx, nbr_cap, pred, rho_iter0,
+                   NULL, NULL, nthreads);
 }
 
 /* Particles::estimateDensities, particles.cpp:440-444: self included, sum in index order. */

