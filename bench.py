@@ -128,10 +128,23 @@ def run_reference_sample(scene, steps, procs, side=16):
     from concurrent.futures import ThreadPoolExecutor
 
     with ThreadPoolExecutor(max_workers=procs) as ex:
-        outs = list(ex.map(lambda s: ref_runner.run(s[0], s[1], scene.params, steps=steps, mode="literal"), samples))
+        outs = list(ex.map(lambda s: ref_runner.run(s[0], s[1], scene.params, steps=steps, mode="literal",
+                                                    restart=True), samples))
     secs = max(o["seconds"] for o in outs)
     n = samples[0][0].shape[0]
     return {"value": procs * n * steps / secs, "seconds": secs, "n": n, "steps": steps, "procs": procs}
+
+
+def port_steps(pos, vel, params, steps, threads):
+    """The FP64 restatement, `steps` single steps each from (pos, vel); returns seconds."""
+    from oracle import oracle
+
+    secs = 0.0
+    for _ in range(steps):
+        t = time.perf_counter()
+        oracle.step(pos, vel, params, steps=1, threads=threads)
+        secs += time.perf_counter() - t
+    return secs
 
 
 def cpu_baseline(scene, budget_s: float):
@@ -145,18 +158,13 @@ def cpu_baseline(scene, budget_s: float):
         r = run_reference_sample(scene, steps, 1)
         return {"value": r["value"], "unit": UNIT, "cores": 1, "kind": "reference",
                 "sample": f"reference particles.cpp step (FP64, O(N^2) all-pairs) on a {r['n']}-particle "
-                          f"16^3 sub-lattice of the workload, {steps} steps, 1 thread; the reference's cost "
+                          f"16^3 sub-lattice of the workload, {steps} steps each from the sample's configured "
+                          f"initial state, 1 thread; the reference's cost "
                           f"per particle grows with N, so this sample overstates its speed on the full scene"}
-    from oracle import oracle
-
     pos, vel = sample_block(scene, 32)
-    t = time.perf_counter()
-    oracle.step(pos, vel, scene.params, steps=2, threads=1)
-    dt = (time.perf_counter() - t) / 2
-    steps = max(1, int(budget_s / max(dt, 1e-4)))
-    t = time.perf_counter()
-    oracle.step(pos, vel, scene.params, steps=steps, threads=1)
-    secs = time.perf_counter() - t
+    dt = port_steps(pos, vel, scene.params, 2, 1) / 2
+    steps = max(1, min(200, int(budget_s / max(dt, 1e-4))))
+    secs = port_steps(pos, vel, scene.params, steps, 1)
     return {"value": pos.shape[0] * steps / secs, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"FP64 restatement (uniform grid) on a {pos.shape[0]}-particle sub-lattice, {steps} steps, "
                       f"1 thread (reference build unavailable)"}
@@ -167,13 +175,9 @@ def cpu_port_all_cores(scene, budget_s: float):
 
     pos, vel = sample_block(scene, 48)
     threads = oracle.max_threads()
-    t = time.perf_counter()
-    oracle.step(pos, vel, scene.params, steps=1, threads=threads)
-    dt = time.perf_counter() - t
-    steps = max(1, int(budget_s / max(dt, 1e-4)))
-    t = time.perf_counter()
-    oracle.step(pos, vel, scene.params, steps=steps, threads=threads)
-    secs = time.perf_counter() - t
+    dt = port_steps(pos, vel, scene.params, 1, threads)
+    steps = max(1, min(200, int(budget_s / max(dt, 1e-4))))
+    secs = port_steps(pos, vel, scene.params, steps, threads)
     return {"value": pos.shape[0] * steps / secs, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"FP64 restatement (uniform grid, OpenMP) on a {pos.shape[0]}-particle sub-lattice, "
                       f"{steps} steps"}
@@ -227,10 +231,8 @@ def bench_reference(args, scene, world, rank):
 
         pos, vel = sample_block(scene, 48)
         threads = oracle.max_threads()
-        oracle.step(pos, vel, scene.params, steps=max(args.warmup, 1), threads=threads)
-        t = time.perf_counter()
-        oracle.step(pos, vel, scene.params, steps=args.steps, threads=threads)
-        secs = time.perf_counter() - t
+        port_steps(pos, vel, scene.params, max(args.warmup, 1), threads)
+        secs = port_steps(pos, vel, scene.params, args.steps, threads)
         value = pos.shape[0] * args.steps / secs
         kind, cores = "port", threads
         sample = f"FP64 restatement (OpenMP) on a {pos.shape[0]}-particle sub-lattice, {args.steps} steps"

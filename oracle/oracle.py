@@ -19,6 +19,7 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
 SRC = HERE / "pbf_oracle.c"
 LIB = HERE / "_build" / "libpbf_oracle.so"
+LIB32 = HERE / "_build" / "libpbf_oracle_fp32.so"
 
 if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
@@ -27,24 +28,26 @@ from fluid_gb300.params import PbfParams  # noqa: E402
 
 
 def build(force: bool = False) -> Path:
+    """Build the FP64 restatement and its FP32 twin (same source, -DORC_FLOAT)."""
     LIB.parent.mkdir(parents=True, exist_ok=True)
-    if not force and LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
-        return LIB
-    cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
-           "-fPIC", "-shared", "-Wall", "-o", str(LIB), str(SRC), "-lm"]
-    subprocess.run(cmd, check=True)
+    for out, extra in ((LIB, []), (LIB32, ["-DORC_FLOAT"])):
+        if not force and out.exists() and out.stat().st_mtime >= SRC.stat().st_mtime:
+            continue
+        cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+               "-fPIC", "-shared", "-Wall", *extra, "-o", str(out), str(SRC), "-lm"]
+        subprocess.run(cmd, check=True)
     return LIB
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not LIB.exists():
+def lib(fp32: bool = False):
+    path = LIB32 if fp32 else LIB
+    if path not in _libs:
+        if not path.exists():
             build()
-        L = ctypes.CDLL(str(LIB))
+        L = ctypes.CDLL(str(path))
         P = ctypes.c_void_p
         L.orc_step.argtypes = [P, ctypes.c_int64, P, P, P, ctypes.c_int, ctypes.c_double,
                                P, P, ctypes.c_int64, P, P, ctypes.c_int]
@@ -57,8 +60,8 @@ def lib():
         L.orc_estimate_density_at.argtypes = [P, ctypes.c_int64, P, ctypes.c_int64, P, P, ctypes.c_int]
         L.orc_estimate_density_at.restype = ctypes.c_int
         L.orc_max_threads.restype = ctypes.c_int
-        _lib = L
-    return _lib
+        _libs[path] = L
+    return _libs[path]
 
 
 def _ptr(a):
@@ -67,12 +70,13 @@ def _ptr(a):
 
 def step(pos, vel, params: PbfParams, steps: int = 1, dt: float | None = None,
          neighbors: bool = False, predicted: bool = False, threads: int = 0,
-         given_neighbors=None) -> dict:
+         given_neighbors=None, fp32: bool = False) -> dict:
     """``steps`` FP64 steps from (pos, vel); returns pos, vel, density (+ neighbour CSR).
 
-    ``given_neighbors=(offsets, ids)`` replaces the first step's neighbour search.
+    ``given_neighbors=(offsets, ids)`` replaces the first step's neighbour search;
+    ``fp32`` runs the FP32 twin of the restatement (a statistical comparator only).
     """
-    L = lib()
+    L = lib(fp32)
     pos = np.array(pos, dtype=np.float64, order="C", copy=True)
     vel = np.array(vel, dtype=np.float64, order="C", copy=True)
     n = pos.shape[0]

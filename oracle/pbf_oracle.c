@@ -40,62 +40,70 @@
 
 #define EPS_D (0.00000000001) /* CGL/include/CGL/misc.h:11 */
 
-typedef struct { double x, y, z; } v3;
+/* Scalar type of the restatement: double (the reference's type) unless built with
+ * -DORC_FLOAT, which gives an FP32 comparator for statistics of long rollouts. */
+#ifdef ORC_FLOAT
+typedef float real;
+#else
+typedef double real;
+#endif
 
-static inline v3 V(double x, double y, double z) { v3 r = {x, y, z}; return r; }
+typedef struct { real x, y, z; } v3;
+
+static inline v3 V(real x, real y, real z) { v3 r = {x, y, z}; return r; }
 static inline v3 vadd(v3 a, v3 b) { return V(a.x + b.x, a.y + b.y, a.z + b.z); }
 static inline v3 vsub(v3 a, v3 b) { return V(a.x - b.x, a.y - b.y, a.z - b.z); }
-/* Vector3D * double and double * Vector3D: component products. */
-static inline v3 vscale(v3 a, double c) { return V(a.x * c, a.y * c, a.z * c); }
-static inline v3 svmul(double c, v3 a) { return V(c * a.x, c * a.y, c * a.z); }
-/* Vector3D / double: multiply by the reciprocal (vector3D.h operator/). */
-static inline v3 vdiv(v3 a, double c) { const double rc = 1.0 / c; return V(rc * a.x, rc * a.y, rc * a.z); }
-static inline double norm2(v3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
-static inline double vnorm(v3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
-static inline v3 unit(v3 a) { double r = 1. / sqrt(a.x * a.x + a.y * a.y + a.z * a.z); return V(r * a.x, r * a.y, r * a.z); }
-static inline double dot(v3 u, v3 v) { return u.x * v.x + u.y * v.y + u.z * v.z; }
+/* Vector3D * real and real * Vector3D: component products. */
+static inline v3 vscale(v3 a, real c) { return V(a.x * c, a.y * c, a.z * c); }
+static inline v3 svmul(real c, v3 a) { return V(c * a.x, c * a.y, c * a.z); }
+/* Vector3D / real: multiply by the reciprocal (vector3D.h operator/). */
+static inline v3 vdiv(v3 a, real c) { const real rc = 1.0 / c; return V(rc * a.x, rc * a.y, rc * a.z); }
+static inline real norm2(v3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+static inline real vnorm(v3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+static inline v3 unit(v3 a) { real r = 1. / sqrt(a.x * a.x + a.y * a.y + a.z * a.z); return V(r * a.x, r * a.y, r * a.z); }
+static inline real dot(v3 u, v3 v) { return u.x * v.x + u.y * v.y + u.z * v.z; }
 static inline v3 cross(v3 u, v3 v) {
   return V(u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x);
 }
-static inline double comp(v3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
-static inline void setcomp(v3* a, int k, double v) { if (k == 0) a->x = v; else if (k == 1) a->y = v; else a->z = v; }
+static inline real comp(v3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+static inline void setcomp(v3* a, int k, real v) { if (k == 0) a->x = v; else if (k == 1) a->y = v; else a->z = v; }
 /* std::max / std::min as <algorithm> defines them. */
-static inline double smax(double a, double b) { return (a < b) ? b : a; }
-static inline double smin(double a, double b) { return (b < a) ? b : a; }
+static inline real smax(real a, real b) { return (a < b) ? b : a; }
+static inline real smin(real a, real b) { return (b < a) ? b : a; }
 
 /* intpow<e>(b) = intpow<e-1>(b) * b, intpow<0> = 1 (src/bsdf.h:49-57). */
-static inline double intpow(double b, int e) {
-  double r = 1;
+static inline real intpow(real b, int e) {
+  real r = 1;
   for (int i = 0; i < e; i++) r = r * b;
   return r;
 }
 
 typedef struct {
-  double h, h2, h6, h9, tis;
-  double epsilon, k, vort_eps, xsph_c, rest_density;
+  real h, h2, h6, h9, tis;
+  real epsilon, k, vort_eps, xsph_c, rest_density;
   int iters, scorr_n;
   v3 gravity;
-  double clamp_lo[3], clamp_hi[3];
+  real clamp_lo[3], clamp_hi[3];
   int n_clip, clip_axis[2];
-  double clip_value[2];
+  real clip_value[2];
   int ntri;
   v3 tp[12][3];
   v3 tn[12];
 } ctx_t;
 
 /* poly6_kernel, particles.cpp:134-141 */
-static inline double poly6(const ctx_t* c, v3 r) {
-  double r_l_2 = norm2(r);
+static inline real poly6(const ctx_t* c, v3 r) {
+  real r_l_2 = norm2(r);
   if (r_l_2 >= c->h2) return 0.0;
-  double temp = c->h2 - r_l_2;
+  real temp = c->h2 - r_l_2;
   return 1.56668147106 * intpow(temp, 3) / c->h9;
 }
 
 /* grad_spiky_kernel, particles.cpp:143-149 */
 static inline v3 spiky(const ctx_t* c, v3 r) {
-  double r_l = vnorm(r);
+  real r_l = vnorm(r);
   if (r_l >= c->h || r_l < EPS_D) return V(0, 0, 0);
-  const double k0 = -3 * 4.774648292756860;
+  const real k0 = -3 * 4.774648292756860;
   return vdiv(svmul(k0 * intpow(c->h - r_l, 2), r), c->h6 * r_l);
 }
 
@@ -107,9 +115,9 @@ static void build_box(ctx_t* c, const double lo[3], const double hi[3], int open
     for (int side = 0; side < 2; side++) {
       if (open_mask & (1 << (2 * axis + side))) continue;
       int u = (axis + 1) % 3, w = (axis + 2) % 3;
-      double cc = side ? hi[axis] : lo[axis];
-      double us[4] = {lo[u], hi[u], hi[u], lo[u]};
-      double vs[4] = {lo[w], lo[w], hi[w], hi[w]};
+      real cc = side ? hi[axis] : lo[axis];
+      real us[4] = {lo[u], hi[u], hi[u], lo[u]};
+      real vs[4] = {lo[w], lo[w], hi[w], hi[w]};
       v3 corner[4];
       for (int k = 0; k < 4; k++) {
         corner[k] = V(0, 0, 0);
@@ -127,20 +135,20 @@ static void build_box(ctx_t* c, const double lo[3], const double hi[3], int open
   }
 }
 
-typedef struct { v3 o, d; double min_t, max_t; } ray_t;
+typedef struct { v3 o, d; real min_t, max_t; } ray_t;
 
 /* MarchingTriangle::intersect(const Ray&, Intersection*) arithmetic. */
 static int tri_hit(const ctx_t* c, int t, ray_t* r, v3* nrm) {
   v3 p1 = c->tp[t][0], p2 = c->tp[t][1], p3 = c->tp[t][2];
   v3 e1 = vsub(p2, p1), e2 = vsub(p3, p1), s = vsub(r->o, p1);
   v3 s1 = cross(r->d, e2), s2 = cross(s, e1);
-  double d = dot(s1, e1);
+  real d = dot(s1, e1);
   if (d == 0) return 0;
-  double tt = dot(s2, e2) / d;
+  real tt = dot(s2, e2) / d;
   if ((tt < r->min_t) || (tt > r->max_t)) return 0;
-  double u = dot(s1, s) / d;
-  double v = dot(s2, r->d) / d;
-  double w = 1 - u - v;
+  real u = dot(s1, s) / d;
+  real v = dot(s2, r->d) / d;
+  real w = 1 - u - v;
   if ((u < 0) || (u > 1) || (v < 0) || (v > 1) || (w < 0) || (w > 1)) return 0;
   r->max_t = tt;
   if (nrm) {
@@ -163,13 +171,13 @@ static inline void clamp_box(const ctx_t* c, v3* p) {
   p->z = smax(c->clamp_lo[2] + EPS_D, smin(c->clamp_hi[2] - EPS_D, p->z));
 }
 
-static inline int clip_planes(const ctx_t* c, v3 p, v3 d, double* l) {
+static inline int clip_planes(const ctx_t* c, v3 p, v3 d, real* l) {
   int intersect = 0;
   for (int i = 0; i < c->n_clip; i++) {
     int a = c->clip_axis[i];
-    double da = comp(d, a);
+    real da = comp(d, a);
     if (da != 0.0) {
-      double pt = (c->clip_value[i] - comp(p, a)) / da;
+      real pt = (c->clip_value[i] - comp(p, a)) / da;
       if (pt > 0.0 && pt < *l) {
         *l = pt;
         intersect = 1;
@@ -181,7 +189,7 @@ static inline int clip_planes(const ctx_t* c, v3 p, v3 d, double* l) {
 
 /* clamp, particles.cpp:51-84 */
 static void clamp_move(const ctx_t* c, v3* p, v3 delta_p) {
-  double l = vnorm(delta_p);
+  real l = vnorm(delta_p);
   if (l <= EPS_D) return;
   v3 d = vdiv(delta_p, l);
   int intersect = clip_planes(c, *p, d, &l);
@@ -195,9 +203,9 @@ static void clamp_move(const ctx_t* c, v3* p, v3 delta_p) {
 }
 
 /* clamp_response, particles.cpp:87-132 */
-static void clamp_response(const ctx_t* c, v3* p, v3 v, double dt) {
+static void clamp_response(const ctx_t* c, v3* p, v3 v, real dt) {
   v3 delta_p = vscale(v, dt);
-  double total_l = vnorm(delta_p), l = total_l;
+  real total_l = vnorm(delta_p), l = total_l;
   if (l <= EPS_D) return;
   v3 d = vdiv(delta_p, l);
   int intersect = clip_planes(c, *p, d, &l);
@@ -236,14 +244,14 @@ static int find_neighbors(const ctx_t* c, int64_t n, const v3* xs, nbrs_t* out) 
   out->idx = NULL;
   if (!out->off) return -1;
   if (n == 0) return 0;
-  double lo[3] = {xs[0].x, xs[0].y, xs[0].z}, hi[3] = {lo[0], lo[1], lo[2]};
+  real lo[3] = {xs[0].x, xs[0].y, xs[0].z}, hi[3] = {lo[0], lo[1], lo[2]};
   for (int64_t i = 1; i < n; i++)
     for (int k = 0; k < 3; k++) {
-      double v = comp(xs[i], k);
+      real v = comp(xs[i], k);
       if (v < lo[k]) lo[k] = v;
       if (v > hi[k]) hi[k] = v;
     }
-  const double cell = sqrt(c->h2) * (1.0 + 1e-6);
+  const real cell = sqrt(c->h2) * (1.0 + 1e-6);
   int64_t dim[3];
   for (int k = 0; k < 3; k++) {
     if (!(hi[k] - lo[k] < 1e6 * cell)) return -2; /* non-finite or absurd extent */
@@ -352,13 +360,13 @@ typedef struct {
 } step_info_t;
 
 /*
- * One step, "jacobi" form (see file comment). pos/vel/rho: n entries (v3 / double).
+ * One step, "jacobi" form (see file comment). pos/vel/rho: n entries (v3 / real).
  * nb receives the neighbour lists of this step (caller frees).
  */
-static int step_once(const ctx_t* c, int64_t n, v3* x, v3* v, double* rho, double dt,
+static int step_once(const ctx_t* c, int64_t n, v3* x, v3* v, real* rho, real dt,
                      nbrs_t* nb, const nbrs_t* given, v3* pred_out, step_info_t* info) {
   v3* xs = (v3*)malloc(sizeof(v3) * (size_t)(n ? n : 1));
-  double* lam = (double*)malloc(sizeof(double) * (size_t)(n ? n : 1));
+  real* lam = (real*)malloc(sizeof(real) * (size_t)(n ? n : 1));
   v3* vort = (v3*)malloc(sizeof(v3) * (size_t)(n ? n : 1));
   v3* vnew = (v3*)malloc(sizeof(v3) * (size_t)(n ? n : 1));
   if (!xs || !lam || !vort || !vnew) return -1;
@@ -389,7 +397,7 @@ static int step_once(const ctx_t* c, int64_t n, v3* x, v3* v, double* rho, doubl
   const int64_t* off = nb->off;
   const int64_t* idx = nb->idx;
   int64_t nnz = off[n];
-  double* scorr = (double*)malloc(sizeof(double) * (size_t)(nnz ? nnz : 1));
+  real* scorr = (real*)malloc(sizeof(real) * (size_t)(nnz ? nnz : 1));
   v3* gw = (v3*)malloc(sizeof(v3) * (size_t)(nnz ? nnz : 1));
   if (!scorr || !gw) return -1;
 
@@ -397,11 +405,11 @@ static int step_once(const ctx_t* c, int64_t n, v3* x, v3* v, double* rho, doubl
     /* newtonStepCalculateLambda, particles.cpp:185-204 */
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; i++) {
-      double density = 0.0, denom = 0.0;
+      real density = 0.0, denom = 0.0;
       v3 grad_i_c_i = V(0, 0, 0);
       for (int64_t e = off[i]; e < off[i + 1]; e++) {
         v3 r = vsub(xs[i], xs[idx[e]]);
-        double w = poly6(c, r);
+        real w = poly6(c, r);
         v3 g = spiky(c, r);
         density += w;
         scorr[e] = -c->k * intpow(w * c->tis, c->scorr_n);
@@ -410,7 +418,7 @@ static int step_once(const ctx_t* c, int64_t n, v3* x, v3* v, double* rho, doubl
         grad_i_c_i = vadd(grad_i_c_i, g);
         denom += norm2(g);
       }
-      double c_i = density / c->rest_density - 1.0;
+      real c_i = density / c->rest_density - 1.0;
       denom += norm2(grad_i_c_i);
       lam[i] = -c_i / (denom + c->epsilon);
       rho[i] = density;
@@ -440,14 +448,14 @@ static int step_once(const ctx_t* c, int64_t n, v3* x, v3* v, double* rho, doubl
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; i++) {
     v3 w_acc = V(0, 0, 0), visc = V(0, 0, 0);
-    double density = 0.0;
+    real density = 0.0;
     for (int64_t e = off[i]; e < off[i + 1]; e++) {
       int64_t j = idx[e];
       v3 v_i_n = vsub(v[j], v[i]);
       v3 r = vsub(xs[i], xs[j]);
       v3 g = spiky(c, r);
       w_acc = vadd(w_acc, cross(v_i_n, g));
-      double w = poly6(c, r);
+      real w = poly6(c, r);
       visc = vadd(visc, vscale(v_i_n, w));
       gw[e] = g;
       density += w;
@@ -478,6 +486,21 @@ static int step_once(const ctx_t* c, int64_t n, v3* x, v3* v, double* rho, doubl
   free(scorr);
   free(gw);
   return 0;
+}
+
+/* double (n,3) arrays <-> v3 of real (a copy also when real is double) */
+static v3* to_v3(const double* a, int64_t n) {
+  v3* r = (v3*)malloc(sizeof(v3) * (size_t)(n ? n : 1));
+  if (r && a)
+    for (int64_t i = 0; i < n; i++) r[i] = V((real)a[3 * i], (real)a[3 * i + 1], (real)a[3 * i + 2]);
+  return r;
+}
+static void from_v3(double* a, const v3* r, int64_t n) {
+  for (int64_t i = 0; i < n; i++) {
+    a[3 * i] = r[i].x;
+    a[3 * i + 1] = r[i].y;
+    a[3 * i + 2] = r[i].z;
+  }
 }
 
 /* ---- exported ---------------------------------------------------------------- */
@@ -514,15 +537,19 @@ int orc_step2(const pbf_params* prm, int64_t n, double* pos, double* vel, double
               int nthreads) {
   set_threads(nthreads);
   ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
-  if (!c) return -1;
+  v3* x = to_v3(pos, n);
+  v3* v = to_v3(vel, n);
+  v3* pr = pred ? to_v3(NULL, n) : NULL;
+  real* rr = (real*)malloc(sizeof(real) * (size_t)(n ? n : 1));
+  if (!c || !x || !v || !rr || (pred && !pr)) return -1;
   make_ctx(c, prm);
   int rc = 0;
   for (int s = 0; s < nsteps && rc == 0; s++) {
     nbrs_t nb = {NULL, NULL};
     step_info_t info = {0};
     nbrs_t given = {(int64_t*)in_off, (int64_t*)in_idx};
-    rc = step_once(c, n, (v3*)pos, (v3*)vel, rho, dt, &nb, (in_off && s == 0) ? &given : NULL,
-                   (pred && s == nsteps - 1) ? (v3*)pred : NULL, &info);
+    rc = step_once(c, n, x, v, rr, (real)dt, &nb, (in_off && s == 0) ? &given : NULL,
+                   (pred && s == nsteps - 1) ? pr : NULL, &info);
     if (rc == 0 && rho_iter0) rho_iter0[s] = n ? info.density_iter0_sum / (double)n : 0.0;
     if (rc == 0 && s == nsteps - 1 && nbr_off) {
       memcpy(nbr_off, nb.off, sizeof(int64_t) * (size_t)(n + 1));
@@ -535,6 +562,14 @@ int orc_step2(const pbf_params* prm, int64_t n, double* pos, double* vel, double
     free(nb.off);
     free(nb.idx);
   }
+  from_v3(pos, x, n);
+  from_v3(vel, v, n);
+  if (pred) from_v3(pred, pr, n);
+  for (int64_t i = 0; i < n; i++) rho[i] = rr[i];
+  free(x);
+  free(v);
+  free(pr);
+  free(rr);
   free(c);
   return rc;
 }
@@ -553,13 +588,14 @@ int orc_estimate_densities(const pbf_params* prm, int64_t n, const double* pos, 
   ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
   if (!c) return -1;
   make_ctx(c, prm);
-  const v3* x = (const v3*)pos;
+  v3* x = to_v3(pos, n);
+  if (!x) return -1;
   nbrs_t nb = {NULL, NULL};
   int rc = find_neighbors(c, n, x, &nb);
   if (rc == 0) {
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; i++) {
-      double d = 0.0;
+      real d = 0.0;
       int self_done = 0;
       for (int64_t e = nb.off[i]; e < nb.off[i + 1]; e++) {
         int64_t j = nb.idx[e];
@@ -575,6 +611,7 @@ int orc_estimate_densities(const pbf_params* prm, int64_t n, const double* pos, 
   }
   free(nb.off);
   free(nb.idx);
+  free(x);
   free(c);
   return rc;
 }
@@ -586,14 +623,17 @@ int orc_estimate_density_at(const pbf_params* prm, int64_t n, const double* pos,
   ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
   if (!c) return -1;
   make_ctx(c, prm);
-  const v3* x = (const v3*)pos;
-  const v3* q = (const v3*)pts;
+  v3* x = to_v3(pos, n);
+  v3* q = to_v3(pts, m);
+  if (!x || !q) return -1;
 #pragma omp parallel for schedule(static)
   for (int64_t k = 0; k < m; k++) {
-    double d = 0.0;
+    real d = 0.0;
     for (int64_t i = 0; i < n; i++) d += poly6(c, vsub(x[i], q[k]));
     out[k] = d;
   }
+  free(x);
+  free(q);
   free(c);
   return 0;
 }

@@ -22,7 +22,9 @@
 //        load_density[n], i64 nnz, i64 offsets[n+1], i64 idx[nnz],
 //        f64 seconds
 // flags: 2 = dump neighbour lists of the last step, 4 = run
-// Particles::estimateDensities() (src/particles.cpp:440-444) before stepping.
+// Particles::estimateDensities() (src/particles.cpp:440-444) before stepping,
+// 8 = restart: every step starts again from the input state (a fresh
+// Particles built untimed), so `seconds` times K steps of the same input.
 // open_mask: bit per box face to leave out (0 x-lo, 1 x-hi, 2 y-lo, 3 y-hi,
 // 4 z-lo, 5 z-hi).
 #include <chrono>
@@ -193,30 +195,41 @@ int main(int argc, char** argv) {
   std::vector<Primitive*> prims = box_triangles(lo, hi, static_cast<int>(open_mask));
   BVHAccel* bvh = new BVHAccel(prims);
 
-  Particles P(rest_density);
-  P.bvh = bvh;
-  for (int64_t i = 0; i < n; i++) {
-    P.addParticle(Vector3D(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]),
-                  Vector3D(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]));
-  }
+  auto make = [&]() {
+    Particles* P = new Particles(rest_density);
+    P->bvh = bvh;
+    for (int64_t i = 0; i < n; i++) {
+      P->addParticle(Vector3D(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]),
+                     Vector3D(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]));
+    }
+    return P;
+  };
+  Particles* Pp = make();
   std::vector<double> load_density(n, 0.0);
   if (flags & 4) {
-    P.estimateDensities();
+    Pp->estimateDensities();
     for (int64_t i = 0; i < n; i++)
-      load_density[i] = P.ps[i]->getLatestDensityEstimate();
+      load_density[i] = Pp->ps[i]->getLatestDensityEstimate();
   }
 
-  auto t0 = std::chrono::steady_clock::now();
+  double seconds = 0.0;
   for (int64_t s = 0; s < steps; s++) {
-    if (mode == 0) {
-      P.timeStep(pbf_ref_dt);
-    } else {
-      step_jacobi(P, pbf_ref_dt);
+    if ((flags & 8) && s > 0) {
+      for (Particle* q : Pp->ps) delete q;
+      delete Pp;
+      Pp = make();
     }
+    auto t0 = std::chrono::steady_clock::now();
+    if (mode == 0) {
+      Pp->timeStep(pbf_ref_dt);
+    } else {
+      step_jacobi(*Pp, pbf_ref_dt);
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    seconds += std::chrono::duration<double>(t1 - t0).count();
     sink.str("");
   }
-  auto t1 = std::chrono::steady_clock::now();
-  const double seconds = std::chrono::duration<double>(t1 - t0).count();
+  Particles& P = *Pp;
   std::cout.rdbuf(old_out);
   std::cerr.rdbuf(old_err);
 

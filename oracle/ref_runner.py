@@ -23,8 +23,11 @@ def available() -> bool:
 
 
 def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool = False,
-        load_density: bool = False, timeout: float | None = None) -> dict:
+        load_density: bool = False, restart: bool = False, timeout: float | None = None) -> dict:
     """Run ``steps`` reference steps. ``params`` is a fluid_gb300.params.PbfParams.
+
+    ``restart``: every step starts again from (pos, vel); ``seconds`` then times
+    ``steps`` steps of the same input.
 
     The reference hard-codes gravity on -y, the clip planes z=1 / y=1.49 and the
     clamp box (particles.cpp:57-83, 180); params that disagree are rejected.
@@ -45,7 +48,7 @@ def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool 
     pos = np.ascontiguousarray(pos, dtype=np.float64)
     vel = np.ascontiguousarray(vel, dtype=np.float64)
     n = pos.shape[0]
-    flags = (2 if neighbors else 0) | (4 if load_density else 0)
+    flags = (2 if neighbors else 0) | (4 if load_density else 0) | (8 if restart else 0)
     with tempfile.TemporaryDirectory() as td:
         fin = Path(td) / "in.bin"
         fout = Path(td) / "out.bin"
