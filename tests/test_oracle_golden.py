@@ -28,7 +28,7 @@ def golden(request):
 
 def test_golden_files_present():
     names = {_case_id(p) for p in GOLDEN}
-    assert {"block4096_mass_1step", "p_default_1step", "block512_mass_60step"} <= names
+    assert {"block4096_mass_1step", "p_default_1step", "block512_mass_20step"} <= names
 
 
 def test_oracle_matches_reference_bitwise(golden, oracle_lib):
