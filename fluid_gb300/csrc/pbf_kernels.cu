@@ -262,8 +262,10 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
 // ---------------------------------------------------------------------------
 // Jacobi density-constraint iterations
 // ---------------------------------------------------------------------------
+// lambda_i is stored in x*_i.w of the same buffer: within this pass every
+// thread reads only .xyz of its neighbours' x*, which no thread writes.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_lambda(const float4* __restrict__ xs,
+__global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs,
                                                   const float4* __restrict__ pos,
                                                   const uint4* __restrict__ hdr,
                                                   const uint32_t* __restrict__ words,
@@ -278,7 +280,7 @@ __global__ void __launch_bounds__(BLOCK) k_lambda(const float4* __restrict__ xs,
   float qsum = 0.f, g2 = 0.f;
   float3 gs = make_float3(0.f, 0.f, 0.f);
   for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) {
-    const float4 xj = __ldg(&xs[j]);
+    const float4 xj = xs[j];
     const float3 r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
     const float r2 = dot3(r, r);
     if (r2 < P.h2) {
@@ -294,7 +296,9 @@ __global__ void __launch_bounds__(BLOCK) k_lambda(const float4* __restrict__ xs,
   const float rho = P.poly6_c * qsum;
   const float kg = P.spiky_c * P.inv_rho0;
   const float denom = kg * kg * (g2 + dot3(gs, gs)) + P.epsilon;
-  lam[i] = -(rho * P.inv_rho0 - 1.0f) / denom;
+  const float l = -(rho * P.inv_rho0 - 1.0f) / denom;
+  lam[i] = l;
+  reinterpret_cast<float*>(xs)[4 * i + 3] = l;
   if (rho_iter0) rho_iter0[i] = rho;
 }
 
@@ -313,11 +317,11 @@ __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
   const float4 xi = xs[i];
   const float4 x4 = pos[i];
   const SceneDesc& sc = scenes[scene_of_slot(x4)];
-  const float li = lam[i];
+  const float li = xi.w;  // lambda_i (k_lambda stores it in x*.w)
   float3 dp = make_float3(0.f, 0.f, 0.f);
   for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) {
     const float4 xj = __ldg(&xs[j]);
-    const float lj = __ldg(&lam[j]);
+    const float lj = xj.w;
     const float3 r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
     const float r2 = dot3(r, r);
     float w = 0.f;
@@ -344,8 +348,9 @@ __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
 // ---------------------------------------------------------------------------
 // velocity, vorticity, XSPH, reported density; then vorticity confinement
 // ---------------------------------------------------------------------------
+// |omega_i| is stored in x*_i.w of the same buffer (neighbours read only .xyz here).
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_xsph(const float4* __restrict__ xs,
+__global__ void __launch_bounds__(BLOCK) k_xsph(float4* xs,
                                                 const float4* __restrict__ pos,
                                                 const float4* __restrict__ disp,
                                                 const uint4* __restrict__ hdr,
@@ -363,7 +368,7 @@ __global__ void __launch_bounds__(BLOCK) k_xsph(const float4* __restrict__ xs,
     float qsum = 0.f;
     float3 visc = make_float3(0.f, 0.f, 0.f), w = make_float3(0.f, 0.f, 0.f);
     for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) {
-      const float4 xj = __ldg(&xs[j]);
+      const float4 xj = xs[j];
       const float3 vij = f3(__ldg(&disp[j])) * inv_dt - vi;
       const float3 r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
       const float r2 = dot3(r, r);
@@ -380,7 +385,9 @@ __global__ void __launch_bounds__(BLOCK) k_xsph(const float4* __restrict__ xs,
     w = w * P.spiky_c;
     const float3 v = vi + visc * (P.xsph_c * P.poly6_c);
     vel_out[i] = make_float4(v.x, v.y, v.z, 0.f);
-    omega[i] = make_float4(w.x, w.y, w.z, sqrtf(dot3(w, w)));
+    const float wn = sqrtf(dot3(w, w));
+    omega[i] = make_float4(w.x, w.y, w.z, wn);
+    reinterpret_cast<float*>(xs)[4 * i + 3] = wn;
     rho_out[i] = rho;
   }
 }
@@ -403,7 +410,7 @@ __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
   float3 eta = make_float3(0.f, 0.f, 0.f);
   for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) {
     const float4 xj = __ldg(&xs[j]);
-    const float wj = __ldg(&omega[j].w);
+    const float wj = xj.w;  // |omega_j| (k_xsph stores it in x*.w)
     const float3 r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
     float s;
     if (spiky_s(dot3(r, r), P.h, &s)) eta = eta + r * (wj * s);
@@ -427,23 +434,22 @@ __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
 __global__ void __launch_bounds__(256) k_stats(const float* __restrict__ rho, const float* __restrict__ rho0,
                                                const uint4* __restrict__ hdr, DevStats* __restrict__ st,
                                                float inv_rho0, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = i < n;
   double r = 0.0, r0 = 0.0, es = 0.0;
   float em = 0.f;
   unsigned cmin = 0xffffffffu, cmax = 0u;
   unsigned long long csum = 0ull, low = 0ull;
-  if (live) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float x = rho[i];
-    r = x;
-    r0 = rho0[i];
+    r += x;
+    r0 += rho0[i];
     const float e = fabsf(x * inv_rho0 - 1.0f);
-    es = e;
-    em = e;
+    es += e;
+    em = fmaxf(em, e);
     const unsigned c = static_cast<unsigned>(nbr_total(hdr[i]));
-    cmin = cmax = c;
-    csum = c;
-    low = c < static_cast<unsigned>(kNeighborAlert) ? 1ull : 0ull;
+    cmin = min(cmin, c);
+    cmax = max(cmax, c);
+    csum += c;
+    low += c < static_cast<unsigned>(kNeighborAlert) ? 1ull : 0ull;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -456,7 +462,33 @@ __global__ void __launch_bounds__(256) k_stats(const float* __restrict__ rho, co
     csum += __shfl_down_sync(0xffffffffu, csum, o);
     low += __shfl_down_sync(0xffffffffu, low, o);
   }
-  if (lane_id() == 0 && live) {  // live threads form a prefix: lane 0 live iff any lane is
+  __shared__ double sd[3][8];
+  __shared__ float sem[8];
+  __shared__ unsigned smin[8], smax[8];
+  __shared__ unsigned long long ssum[8], slow[8];
+  const unsigned w = threadIdx.x >> 5;
+  if (lane_id() == 0) {
+    sd[0][w] = r;
+    sd[1][w] = r0;
+    sd[2][w] = es;
+    sem[w] = em;
+    smin[w] = cmin;
+    smax[w] = cmax;
+    ssum[w] = csum;
+    slow[w] = low;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (unsigned k = 1; k < (blockDim.x >> 5); ++k) {
+      r += sd[0][k];
+      r0 += sd[1][k];
+      es += sd[2][k];
+      em = fmaxf(em, sem[k]);
+      cmin = min(cmin, smin[k]);
+      cmax = max(cmax, smax[k]);
+      csum += ssum[k];
+      low += slow[k];
+    }
     atomicAdd(&st->rho_sum, r);
     atomicAdd(&st->rho_iter0_sum, r0);
     atomicAdd(&st->err_sum, es);
@@ -675,7 +707,7 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
                        b.xs[0], b.pos[B], b.cell_start, b.scenes, b.nbr_hdr, b.nbr_w, b.err, P, n));
   if (mk) mk->mark(kPhaseNeighbors, s);
   for (int it = 0; it < iters; ++it) {
-    const float4* xcur = b.xs[it & 1];
+    float4* xcur = b.xs[it & 1];
     float4* xnext = b.xs[(it + 1) & 1];
     PBF_BLOCK_SWITCH(t.block_solve,
                      k_lambda<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
@@ -688,7 +720,7 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
                          xnext, P, n));
     if (mk) mk->mark(kPhaseDeltaP, s);
   }
-  const float4* fin = b.xs[iters & 1];
+  float4* fin = b.xs[iters & 1];
   PBF_BLOCK_SWITCH(t.block_solve,
                    k_xsph<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
                        fin, b.pos[B], b.disp[1], b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.vel[B],
@@ -700,7 +732,7 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
                        b.err, P, dt, n));
   if (mk) mk->mark(kPhaseVorticity, s);
   if (P.stats)
-    k_stats<<<blocks_for(n, 256), 256, 0, s>>>(b.rho, b.rho_iter0, b.nbr_hdr, b.stats, P.inv_rho0, n);
+    k_stats<<<min(blocks_for(n, 256), 1216u), 256, 0, s>>>(b.rho, b.rho_iter0, b.nbr_hdr, b.stats, P.inv_rho0, n);
   if (mk) mk->mark(kPhaseStats, s);
   return cudaGetLastError();
 }
