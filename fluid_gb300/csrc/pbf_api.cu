@@ -78,8 +78,8 @@ bool make_dev_params(const pbf_params& p, DevParams* d, double* cell_out, std::s
       return false;
     }
   const int max_nbr = p.max_neighbors == 0 ? 128 : p.max_neighbors;
-  if (max_nbr < 4 || max_nbr > 255) {
-    *why = "max_neighbors must be in [4, 255]";
+  if (max_nbr < 4 || max_nbr > 1024) {
+    *why = "max_neighbors must be in [4, 1024]";
     return false;
   }
   std::memset(d, 0, sizeof(*d));
@@ -110,7 +110,7 @@ bool make_dev_params(const pbf_params& p, DevParams* d, double* cell_out, std::s
   }
   d->scorr_n = p.scorr_n;
   d->open_mask = p.box_open_mask;
-  d->max_words = (max_nbr + 3) / 4;
+  d->max_words = (max_nbr + 1) / 2;
   d->stats = (p.flags & PBF_FLAG_STATS) ? 1 : 0;
   *cell_out = cell;
   return true;

@@ -143,46 +143,57 @@ __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 
 }
 
 // ---- neighbour lists -----------------------------------------------------------
-// A particle's neighbours lie in the 9 rows (dz, dy) of 3 consecutive cells
-// (cx-1..cx+1) around its cell; each row is a contiguous slot range of the
-// cell-sorted arrays. A neighbour is stored as a u8 offset from its row's first
-// slot; hdr holds the 9 row counts (bytes), the total (hdr.z bits 8-15) and the
-// packed cell coordinates (hdr.w).
-__device__ __forceinline__ int row_count(const uint4& h, int r) {
-  const uint32_t w = r < 4 ? h.x : (r < 8 ? h.y : h.z);
-  return static_cast<int>((w >> (8 * (r & 3))) & 0xffu);
+// A particle's neighbours lie in 3 z-slabs (dz = -1, 0, 1) of its cell; inside a slab
+// they lie in the rows dy = -1..1 of cells cx-1..cx+1, all within 2*nx+3 cells after the
+// slab's first candidate cell, i.e. a short slot range of the cell-sorted arrays. A
+// neighbour is stored as a u16 entry (slab << 14 | slot offset from the slab's first
+// candidate slot), two entries per u32 word, word-major ([word][N]) so a warp's loads of
+// one word index coalesce. hdr = {slab base -1, slab base 0, slab base +1, count}.
+constexpr int kOffsetBits = 14;
+constexpr uint32_t kOffsetMask = (1u << kOffsetBits) - 1u;
+
+__device__ __forceinline__ int nbr_total(const uint4& h) { return static_cast<int>(h.w); }
+
+__device__ __forceinline__ uint32_t nbr_decode(const uint4& h, uint32_t e) {
+  const uint32_t g = e >> kOffsetBits;
+  const uint32_t base = g == 0u ? h.x : (g == 1u ? h.y : h.z);
+  return base + (e & kOffsetMask);
 }
-__device__ __forceinline__ int nbr_total(const uint4& h) { return static_cast<int>((h.z >> 8) & 0xffu); }
 
 // Calls f(j) for every neighbour slot j of slot i, ascending.
 template <typename F>
 __device__ __forceinline__ void for_each_neighbor(int i, int n, const uint4 h,
-                                                  const uint32_t* __restrict__ words,
-                                                  const uint32_t* __restrict__ cell_start,
-                                                  const SceneDesc& sc, F&& f) {
-  const int cx = static_cast<int>(h.w & 1023u);
-  const int cy = static_cast<int>((h.w >> 10) & 2047u);
-  const int cz = static_cast<int>(h.w >> 21);
-  const int x0 = cx > 0 ? cx - 1 : 0;
-  uint32_t base[9];
-#pragma unroll
-  for (int r = 0; r < 9; ++r) {
-    const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
-    base[r] = row_count(h, r)
-                  ? __ldg(&cell_start[sc.cell_off + static_cast<uint32_t>((z * sc.dim[1] + y) * sc.dim[0] + x0)])
-                  : 0u;
-  }
+                                                  const uint32_t* __restrict__ words, F&& f) {
+  const int total = nbr_total(h);
   int k = 0;
-  uint32_t word = 0;
-#pragma unroll
-  for (int r = 0; r < 9; ++r) {
-    const int c = row_count(h, r);
-    for (int t = 0; t < c; ++t, ++k) {
-      if ((k & 3) == 0) word = __ldg(&words[static_cast<size_t>(k >> 2) * n + i]);
-      const uint32_t j = base[r] + ((word >> ((k & 3) * 8)) & 0xffu);
-      f(j);
-    }
+  for (; k + 1 < total; k += 2) {
+    const uint32_t w = __ldg(&words[static_cast<size_t>(k >> 1) * n + i]);
+    f(nbr_decode(h, w & 0xffffu));
+    f(nbr_decode(h, w >> 16));
   }
+  if (k < total) {
+    const uint32_t w = __ldg(&words[static_cast<size_t>(k >> 1) * n + i]);
+    f(nbr_decode(h, w & 0xffffu));
+  }
+}
+
+// Pair geometry shared by every neighbour pass, branch-free:
+//   r = x_i - x_j, r2 = |r|^2,
+//   q = max(h2 - r2, 0)       so W = poly6_c * q^3     (particles.cpp:134-141)
+//   s = (h - |r|)^2 / |r| on [EPS_D, h), else 0, so grad W = spiky_c * s * r (:143-149)
+struct Pair {
+  float3 r;
+  float r2, q, s;
+};
+__device__ __forceinline__ Pair pair_of(const float4& xi, const float4& xj, float h, float h2) {
+  Pair p;
+  p.r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+  p.r2 = dot3(p.r, p.r);
+  p.q = fmaxf(h2 - p.r2, 0.0f);
+  const float rinv = rsqrtf(p.r2);
+  const float hr = fmaxf(h - p.r2 * rinv, 0.0f);
+  p.s = p.r2 >= kEps * kEps ? hr * hr * rinv : 0.0f;
+  return p;
 }
 
 // Spiky gradient factor s with grad W(r) = spiky_c * s * r (particles.cpp:143-149);

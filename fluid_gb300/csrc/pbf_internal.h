@@ -10,8 +10,8 @@
 //   lam    float   lambda                                    4 B
 //   rho    float   reported density                          4 B
 //   id     u32     original particle index                   4 B
-//   nbr_hdr uint4  9 row counts (u8), total (u8), packed cell coords
-//   nbr_w   u32    [words][N] neighbour offsets, 4 x u8 per word, word-major
+//   nbr_hdr uint4  first candidate slot of the 3 z-slabs, neighbour count
+//   nbr_w   u32    [words][N] neighbour entries, 2 x u16 per word, word-major
 //   cell_count / cell_start u32 [C] / [C+1]
 #pragma once
 

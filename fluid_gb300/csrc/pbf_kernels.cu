@@ -216,46 +216,56 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
   const float4 xi = xs[i];
   const SceneDesc& sc = scenes[scene_of_slot(pos[i])];
   const CellCoord cc = cell_of(f3(xi), sc, P.inv_cell);
-  const int cap = min(P.max_words * 4, 255);
-  uint32_t cnt[3] = {0u, 0u, 0u};
+  const int cap = P.max_words * 2;
+  uint32_t gbase[3] = {0u, 0u, 0u};
   int total = 0;
   uint32_t word = 0;
   unsigned flags = 0;
   const int x0 = cc.x > 0 ? cc.x - 1 : 0;
   const int x1 = cc.x + 1 < sc.dim[0] ? cc.x + 1 : sc.dim[0] - 1;
+  const int y0 = cc.y > 0 ? cc.y - 1 : 0;
+  const int y1 = cc.y + 1 < sc.dim[1] ? cc.y + 1 : sc.dim[1] - 1;
+#pragma unroll
+  for (int g = 0; g < 3; ++g) {
+    const int z = cc.z + g - 1;
+    if (z < 0 || z >= sc.dim[2]) continue;
+    const uint32_t slab = sc.cell_off + static_cast<uint32_t>(z * sc.dim[1] * sc.dim[0]);
+    const uint32_t gstart = __ldg(&cell_start[slab + static_cast<uint32_t>(y0 * sc.dim[0] + x0)]);
+    gbase[g] = gstart;
 #pragma unroll 1
-  for (int r = 0; r < 9; ++r) {
-    const int z = cc.z + r / 3 - 1, y = cc.y + r % 3 - 1;
-    if (z < 0 || z >= sc.dim[2] || y < 0 || y >= sc.dim[1]) continue;
-    const uint32_t row = sc.cell_off + static_cast<uint32_t>((z * sc.dim[1] + y) * sc.dim[0]);
-    const uint32_t start = __ldg(&cell_start[row + x0]);
-    uint32_t end = __ldg(&cell_start[row + x1 + 1]);
-    if (end - start > static_cast<uint32_t>(kMaxRowCandidates)) {
-      flags |= PBF_ERRBIT_ROW_CAPACITY;
-      end = start + kMaxRowCandidates;
-    }
-    uint32_t c = 0;
-    for (uint32_t j = start; j < end; ++j) {
-      if (j == static_cast<uint32_t>(i)) continue;
-      const float4 xj = __ldg(&xs[j]);
-      if (dist2_rn(xi, xj) <= P.h2) {
-        if (total < cap) {
-          word |= (j - start) << (8 * (total & 3));
-          ++total;
-          ++c;
-          if ((total & 3) == 0) {
-            words[static_cast<size_t>((total >> 2) - 1) * n + i] = word;
-            word = 0;
+    for (int y = y0; y <= y1; ++y) {
+      const uint32_t row = slab + static_cast<uint32_t>(y * sc.dim[0]);
+      const uint32_t start = __ldg(&cell_start[row + x0]);
+      uint32_t end = __ldg(&cell_start[row + x1 + 1]);
+      if (end - start > static_cast<uint32_t>(kMaxRowCandidates)) {
+        flags |= PBF_ERRBIT_ROW_CAPACITY;
+        end = start + kMaxRowCandidates;
+      }
+      for (uint32_t j = start; j < end; ++j) {
+        if (j == static_cast<uint32_t>(i)) continue;
+        const float4 xj = __ldg(&xs[j]);
+        if (dist2_rn(xi, xj) <= P.h2) {
+          const uint32_t off = j - gstart;
+          if (off > kOffsetMask) {
+            flags |= PBF_ERRBIT_ROW_CAPACITY;
+          } else if (total < cap) {
+            const uint32_t e = (static_cast<uint32_t>(g) << kOffsetBits) | off;
+            if ((total & 1) == 0) {
+              word = e;
+            } else {
+              word |= e << 16;
+              words[static_cast<size_t>(total >> 1) * n + i] = word;
+            }
+            ++total;
+          } else {
+            flags |= PBF_ERRBIT_NEIGHBOR_CAPACITY;
           }
-        } else {
-          flags |= PBF_ERRBIT_NEIGHBOR_CAPACITY;
         }
       }
     }
-    cnt[r >> 2] |= c << (8 * (r & 3));
   }
-  if (total & 3) words[static_cast<size_t>(total >> 2) * n + i] = word;
-  hdr[i] = make_uint4(cnt[0], cnt[1], cnt[2] | (static_cast<uint32_t>(total) << 8), pack_coord(cc));
+  if (total & 1) words[static_cast<size_t>(total >> 1) * n + i] = word;
+  hdr[i] = make_uint4(gbase[0], gbase[1], gbase[2], static_cast<uint32_t>(total));
   if (flags) atomicOr(err, flags);
 }
 
@@ -265,33 +275,20 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
 // lambda_i is stored in x*_i.w of the same buffer: within this pass every
 // thread reads only .xyz of its neighbours' x*, which no thread writes.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs,
-                                                  const float4* __restrict__ pos,
-                                                  const uint4* __restrict__ hdr,
+__global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs, const uint4* __restrict__ hdr,
                                                   const uint32_t* __restrict__ words,
-                                                  const uint32_t* __restrict__ cell_start,
-                                                  const SceneDesc* __restrict__ scenes,
                                                   float* __restrict__ lam, float* __restrict__ rho_iter0,
                                                   DevParams P, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 xi = xs[i];
-  const SceneDesc& sc = scenes[scene_of_slot(pos[i])];
   float qsum = 0.f, g2 = 0.f;
   float3 gs = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) {
-    const float4 xj = xs[j];
-    const float3 r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
-    const float r2 = dot3(r, r);
-    if (r2 < P.h2) {
-      const float q = P.h2 - r2;
-      qsum += q * q * q;
-    }
-    float s;
-    if (spiky_s(r2, P.h, &s)) {
-      gs = gs + r * s;
-      g2 += s * s * r2;
-    }
+  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
+    const Pair p = pair_of(xi, xs[j], P.h, P.h2);
+    qsum += p.q * p.q * p.q;
+    gs = gs + p.r * p.s;
+    g2 += p.s * p.s * p.r2;
   });
   const float rho = P.poly6_c * qsum;
   const float kg = P.spiky_c * P.inv_rho0;
@@ -302,41 +299,40 @@ __global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs,
   if (rho_iter0) rho_iter0[i] = rho;
 }
 
-template <int BLOCK>
+// (lambda_i + lambda_j + s_corr) grad W summed over neighbours; N4 specialises the
+// tensile exponent N = 4 of particles.cpp:40.
+template <int BLOCK, bool N4>
 __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
                                                   const float4* __restrict__ pos,
                                                   const uint4* __restrict__ hdr,
                                                   const uint32_t* __restrict__ words,
-                                                  const uint32_t* __restrict__ cell_start,
                                                   const SceneDesc* __restrict__ scenes,
-                                                  const float* __restrict__ lam,
                                                   float4* __restrict__ disp, float4* __restrict__ xs_next,
                                                   DevParams P, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 xi = xs[i];
-  const float4 x4 = pos[i];
-  const SceneDesc& sc = scenes[scene_of_slot(x4)];
   const float li = xi.w;  // lambda_i (k_lambda stores it in x*.w)
+  const float wt = P.poly6_c * P.tis;
   float3 dp = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) {
+  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
     const float4 xj = __ldg(&xs[j]);
-    const float lj = xj.w;
-    const float3 r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
-    const float r2 = dot3(r, r);
-    float w = 0.f;
-    if (r2 < P.h2) {
-      const float q = P.h2 - r2;
-      w = P.poly6_c * (q * q * q);
+    const Pair p = pair_of(xi, xj, P.h, P.h2);
+    const float a = wt * (p.q * p.q * p.q);  // W / W(dq)
+    float an;
+    if (N4) {
+      const float a2 = a * a;
+      an = a2 * a2;
+    } else {
+      an = a;
+      for (int e = 1; e < P.scorr_n; ++e) an *= a;
     }
-    const float a = w * P.tis;
-    float an = a;
-    for (int e = 1; e < P.scorr_n; ++e) an *= a;
-    const float scorr = -P.scorr_k * an;
-    float s;
-    if (spiky_s(r2, P.h, &s)) dp = dp + r * ((li + lj + scorr) * s);
+    const float coef = (li + xj.w) - P.scorr_k * an;  // lambda_i + lambda_j + s_corr
+    dp = dp + p.r * (coef * p.s);
   });
   dp = dp * (P.spiky_c * P.inv_rho0);
+  const float4 x4 = pos[i];
+  const SceneDesc& sc = scenes[scene_of_slot(x4)];
   const float4 d4 = disp[i];
   float3 d = f3(d4);
   const float3 x = f3(x4);
@@ -350,46 +346,34 @@ __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
 // ---------------------------------------------------------------------------
 // |omega_i| is stored in x*_i.w of the same buffer (neighbours read only .xyz here).
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_xsph(float4* xs,
-                                                const float4* __restrict__ pos,
-                                                const float4* __restrict__ disp,
+__global__ void __launch_bounds__(BLOCK) k_xsph(float4* xs, const float4* __restrict__ disp,
                                                 const uint4* __restrict__ hdr,
                                                 const uint32_t* __restrict__ words,
-                                                const uint32_t* __restrict__ cell_start,
-                                                const SceneDesc* __restrict__ scenes,
                                                 float4* __restrict__ vel_out, float4* __restrict__ omega,
                                                 float* __restrict__ rho_out, DevParams P, float inv_dt,
                                                 int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    const float4 xi = xs[i];
-    const SceneDesc& sc = scenes[scene_of_slot(pos[i])];
-    const float3 vi = f3(disp[i]) * inv_dt;  // updateVelocity, particles.cpp:215-217
-    float qsum = 0.f;
-    float3 visc = make_float3(0.f, 0.f, 0.f), w = make_float3(0.f, 0.f, 0.f);
-    for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) {
-      const float4 xj = xs[j];
-      const float3 vij = f3(__ldg(&disp[j])) * inv_dt - vi;
-      const float3 r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
-      const float r2 = dot3(r, r);
-      if (r2 < P.h2) {
-        const float q = P.h2 - r2;
-        const float q3 = q * q * q;
-        visc = visc + vij * q3;
-        qsum += q3;
-      }
-      float s;
-      if (spiky_s(r2, P.h, &s)) w = w + cross3(vij, r * s);
-    });
-    const float rho = P.poly6_c * qsum;
-    w = w * P.spiky_c;
-    const float3 v = vi + visc * (P.xsph_c * P.poly6_c);
-    vel_out[i] = make_float4(v.x, v.y, v.z, 0.f);
-    const float wn = sqrtf(dot3(w, w));
-    omega[i] = make_float4(w.x, w.y, w.z, wn);
-    reinterpret_cast<float*>(xs)[4 * i + 3] = wn;
-    rho_out[i] = rho;
-  }
+  if (i >= n) return;
+  const float4 xi = xs[i];
+  const float3 vi = f3(disp[i]) * inv_dt;  // updateVelocity, particles.cpp:215-217
+  float qsum = 0.f;
+  float3 visc = make_float3(0.f, 0.f, 0.f), w = make_float3(0.f, 0.f, 0.f);
+  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
+    const Pair p = pair_of(xi, xs[j], P.h, P.h2);
+    const float3 vij = f3(__ldg(&disp[j])) * inv_dt - vi;
+    const float q3 = p.q * p.q * p.q;
+    visc = visc + vij * q3;
+    qsum += q3;
+    w = w + cross3(vij, p.r * p.s);
+  });
+  const float rho = P.poly6_c * qsum;
+  w = w * P.spiky_c;
+  const float3 v = vi + visc * (P.xsph_c * P.poly6_c);
+  vel_out[i] = make_float4(v.x, v.y, v.z, 0.f);
+  const float wn = sqrtf(dot3(w, w));
+  omega[i] = make_float4(w.x, w.y, w.z, wn);
+  reinterpret_cast<float*>(xs)[4 * i + 3] = wn;
+  rho_out[i] = rho;
 }
 
 template <int BLOCK>
@@ -398,22 +382,16 @@ __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
                                                 const float4* __restrict__ omega,
                                                 const uint4* __restrict__ hdr,
                                                 const uint32_t* __restrict__ words,
-                                                const uint32_t* __restrict__ cell_start,
-                                                const SceneDesc* __restrict__ scenes,
                                                 float4* __restrict__ vel, unsigned* __restrict__ err,
                                                 DevParams P, float dt, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 xi = xs[i];
-  const float4 p4 = pos[i];
-  const SceneDesc& sc = scenes[scene_of_slot(p4)];
   float3 eta = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) {
+  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
     const float4 xj = __ldg(&xs[j]);
-    const float wj = xj.w;  // |omega_j| (k_xsph stores it in x*.w)
-    const float3 r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
-    float s;
-    if (spiky_s(dot3(r, r), P.h, &s)) eta = eta + r * (wj * s);
+    const Pair p = pair_of(xi, xj, P.h, P.h2);
+    eta = eta + p.r * (xj.w * p.s);  // |omega_j| (k_xsph stores it in x*.w)
   });
   eta = eta * P.spiky_c;
   float3 v = f3(vel[i]);
@@ -422,6 +400,7 @@ __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
     const float4 wi = omega[i];
     v = v + cross3(eta * (1.0f / en), f3(wi)) * (dt * P.vort_eps);
   }
+  const float4 p4 = pos[i];
   vel[i] = make_float4(v.x, v.y, v.z, 0.f);
   pos[i] = make_float4(xi.x, xi.y, xi.z, p4.w);  // updatePosition, particles.cpp:246-248
   if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(xi.x) && isfinite(xi.y) &&
@@ -583,15 +562,13 @@ __global__ void k_nbr_counts(const uint4* __restrict__ hdr, const uint32_t* __re
 }
 
 // ids[offsets[id[i]] ...] = original ids of i's neighbours (cell order).
-__global__ void k_nbr_ids(const float4* __restrict__ pos, const uint4* __restrict__ hdr,
-                          const uint32_t* __restrict__ words, const uint32_t* __restrict__ cell_start,
-                          const SceneDesc* __restrict__ scenes, const uint32_t* __restrict__ id,
-                          const uint32_t* __restrict__ offsets, uint32_t* __restrict__ ids, int n) {
+__global__ void k_nbr_ids(const uint4* __restrict__ hdr, const uint32_t* __restrict__ words,
+                          const uint32_t* __restrict__ id, const uint32_t* __restrict__ offsets,
+                          uint32_t* __restrict__ ids, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const SceneDesc& sc = scenes[scene_of_slot(pos[i])];
   uint32_t o = offsets[id[i]];
-  for_each_neighbor(i, n, hdr[i], words, cell_start, sc, [&](uint32_t j) { ids[o++] = id[j]; });
+  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) { ids[o++] = id[j]; });
 }
 
 // Particles::estimateDensities (particles.cpp:440-444) on cell-sorted x: self included.
@@ -711,25 +688,27 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
     float4* xnext = b.xs[(it + 1) & 1];
     PBF_BLOCK_SWITCH(t.block_solve,
                      k_lambda<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                         xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.lam,
-                         (it == 0 && P.stats) ? b.rho_iter0 : nullptr, P, n));
+                         xcur, b.nbr_hdr, b.nbr_w, b.lam, (it == 0 && P.stats) ? b.rho_iter0 : nullptr, P, n));
     if (mk) mk->mark(kPhaseLambda, s);
-    PBF_BLOCK_SWITCH(t.block_solve,
-                     k_deltap<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                         xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.lam, b.disp[1],
-                         xnext, P, n));
+    if (P.scorr_n == 4) {
+      PBF_BLOCK_SWITCH(t.block_solve,
+                       (k_deltap<BLOCK, true><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                           xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, P, n)));
+    } else {
+      PBF_BLOCK_SWITCH(t.block_solve,
+                       (k_deltap<BLOCK, false><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                           xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, P, n)));
+    }
     if (mk) mk->mark(kPhaseDeltaP, s);
   }
   float4* fin = b.xs[iters & 1];
   PBF_BLOCK_SWITCH(t.block_solve,
                    k_xsph<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                       fin, b.pos[B], b.disp[1], b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.vel[B],
-                       b.omega, b.rho, P, 1.0f / dt, n));
+                       fin, b.disp[1], b.nbr_hdr, b.nbr_w, b.vel[B], b.omega, b.rho, P, 1.0f / dt, n));
   if (mk) mk->mark(kPhaseXsph, s);
   PBF_BLOCK_SWITCH(t.block_solve,
                    k_vort<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                       fin, b.pos[B], b.omega, b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes, b.vel[B],
-                       b.err, P, dt, n));
+                       fin, b.pos[B], b.omega, b.nbr_hdr, b.nbr_w, b.vel[B], b.err, P, dt, n));
   if (mk) mk->mark(kPhaseVorticity, s);
   if (P.stats)
     k_stats<<<min(blocks_for(n, 256), 1216u), 256, 0, s>>>(b.rho, b.rho_iter0, b.nbr_hdr, b.stats, P.inv_rho0, n);
@@ -798,8 +777,7 @@ cudaError_t launch_neighbor_ids(const Buffers& b, int cur, const uint32_t* offse
                                 cudaStream_t s) {
   const int n = static_cast<int>(b.n);
   if (n == 0) return cudaSuccess;
-  k_nbr_ids<<<blocks_for(n, 256), 256, 0, s>>>(b.pos[cur], b.nbr_hdr, b.nbr_w, b.cell_start, b.scenes,
-                                               b.id[cur], offsets, ids, n);
+  k_nbr_ids<<<blocks_for(n, 256), 256, 0, s>>>(b.nbr_hdr, b.nbr_w, b.id[cur], offsets, ids, n);
   return cudaGetLastError();
 }
 
