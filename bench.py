@@ -271,6 +271,7 @@ def bench_ours(args, scene, world, rank, local):
 
     sim.sort()
     sim.snapshot()
+    tuning = sim.autotune(dt, reps=3) if not args.no_autotune else sim.tuning()
     for _ in range(args.warmup):
         sim.restore()
         sim.step_async(dt, 1)
@@ -366,6 +367,7 @@ def bench_ours(args, scene, world, rank, local):
                      "algo_bytes_per_launch": algo, "avg_launch_ms": per_launch_s * 1e3,
                      "step_frac": step_bytes / (total_ms / args.steps / 1e3) / 1e9 / peak},
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items()},
+        "tuning": tuning,
         "gpu_launches": launches,
         "clocks": clk,
         "stats": {"mean_density_over_rho0": stats["mean_density"] / prm.rest_density,
@@ -391,6 +393,7 @@ def main(argv=None):
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

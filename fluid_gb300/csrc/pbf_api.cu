@@ -787,6 +787,129 @@ pbf_status pbf_restore(pbf_handle* hh) {
   return st;
 }
 
+pbf_status pbf_get_tuning(pbf_handle* hh, pbf_tuning* out) {
+  if (!hh || !out) return PBF_ERR_INVALID;
+  const pbf::Tuning& t = reinterpret_cast<Handle*>(hh)->tune;
+  out->block_predict = t.block_predict;
+  out->block_nbr = t.block_nbr;
+  out->block_solve = t.block_solve;
+  out->block_misc = t.block_misc;
+  return PBF_OK;
+}
+
+static bool valid_block(int b) { return b == 64 || b == 128 || b == 256 || b == 512; }
+
+pbf_status pbf_set_tuning(pbf_handle* hh, const pbf_tuning* t) {
+  if (!hh || !t) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!valid_block(t->block_predict) || !valid_block(t->block_nbr) || !valid_block(t->block_solve) ||
+      !valid_block(t->block_misc))
+    return h->fail(PBF_ERR_INVALID, "block sizes must be 64, 128, 256 or 512");
+  h->tune.block_predict = t->block_predict;
+  h->tune.block_nbr = t->block_nbr;
+  h->tune.block_solve = t->block_solve;
+  h->tune.block_misc = t->block_misc;
+  h->drop_graphs();
+  return PBF_OK;
+}
+
+namespace {
+// Device ms per phase of `reps` steps from the snapshot (restored before each step).
+pbf_status time_phases(Handle* h, float dt, int reps, double* ms) {
+  pbf_status st = pbf_reset_phase_times(reinterpret_cast<pbf_handle*>(h));
+  for (int r = 0; r < reps && st == PBF_OK; ++r) {
+    st = pbf_restore(reinterpret_cast<pbf_handle*>(h));
+    if (st == PBF_OK) st = h->enqueue_steps(dt, 1);
+  }
+  if (st == PBF_OK) st = pbf_get_phase_times(reinterpret_cast<pbf_handle*>(h), ms, nullptr, pbf::kNumPhases);
+  return st;
+}
+}  // namespace
+
+pbf_status pbf_autotune(pbf_handle* hh, double dt, int reps, pbf_tuning* out) {
+  if (!hh || reps < 1) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  const double d = dt > 0 ? dt : h->params.dt;
+  pbf::DeviceGuard g(h->device);
+  if (h->b.n == 0) return out ? pbf_get_tuning(hh, out) : PBF_OK;
+  // keep the caller's checkpoint, if any, and the state
+  const bool had_prof = h->profiling;
+  const uint64_t steps0 = h->steps;
+  const double time0 = h->simulate_time;
+  std::vector<float4> keep_pos, keep_vel;
+  std::vector<uint32_t> keep_id;
+  const bool had_snap = h->snap_valid;
+  const size_t n = h->b.n;
+  if (had_snap) {  // save the caller's snapshot to host
+    keep_pos.resize(n);
+    keep_vel.resize(n);
+    keep_id.resize(n);
+    pbf_status st = h->cuda(cudaMemcpy(keep_pos.data(), h->snap_pos, sizeof(float4) * n, cudaMemcpyDeviceToHost), "D2H");
+    if (st == PBF_OK) st = h->cuda(cudaMemcpy(keep_vel.data(), h->snap_vel, sizeof(float4) * n, cudaMemcpyDeviceToHost), "D2H");
+    if (st == PBF_OK) st = h->cuda(cudaMemcpy(keep_id.data(), h->snap_id, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost), "D2H");
+    if (st != PBF_OK) return st;
+  }
+  const uint64_t snap_steps0 = h->snap_steps;
+  const double snap_time0 = h->snap_time;
+  pbf_status st = pbf_snapshot(hh);
+  if (st != PBF_OK) return st;
+  h->profiling = true;
+  static const int kCand[4] = {64, 128, 256, 512};
+  pbf::Tuning best = h->tune;
+  struct Family {
+    int* field;
+    int phases[4];
+  } fams[] = {
+      {&best.block_nbr, {pbf::kPhaseNeighbors, -1, -1, -1}},
+      {&best.block_solve, {pbf::kPhaseLambda, pbf::kPhaseDeltaP, pbf::kPhaseXsph, pbf::kPhaseVorticity}},
+      {&best.block_predict, {pbf::kPhasePredict, -1, -1, -1}},
+      {&best.block_misc, {pbf::kPhaseSort, pbf::kPhaseGather, -1, -1}},
+  };
+  for (auto& f : fams) {
+    double best_ms = 1e300;
+    int best_b = *f.field;
+    for (int c : kCand) {
+      pbf::Tuning trial = best;
+      *reinterpret_cast<int*>(reinterpret_cast<char*>(&trial) +
+                              (reinterpret_cast<char*>(f.field) - reinterpret_cast<char*>(&best))) = c;
+      h->tune = trial;
+      double ms[pbf::kNumPhases] = {};
+      st = time_phases(h, static_cast<float>(d), 1, ms);  // warm the shape
+      if (st == PBF_OK) st = time_phases(h, static_cast<float>(d), reps, ms);
+      if (st != PBF_OK) break;
+      double tot = 0;
+      for (int q : f.phases)
+        if (q >= 0) tot += ms[q];
+      if (tot < best_ms) {
+        best_ms = tot;
+        best_b = c;
+      }
+    }
+    if (st != PBF_OK) break;
+    *f.field = best_b;
+  }
+  h->tune = best;
+  h->profiling = had_prof;
+  pbf_status st2 = pbf_restore(hh);
+  if (st == PBF_OK) st = st2;
+  if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "sync");
+  pbf_reset_phase_times(hh);
+  h->steps = steps0;
+  h->simulate_time = time0;
+  if (had_snap && st == PBF_OK) {
+    st = h->cuda(cudaMemcpy(h->snap_pos, keep_pos.data(), sizeof(float4) * n, cudaMemcpyHostToDevice), "H2D");
+    if (st == PBF_OK) st = h->cuda(cudaMemcpy(h->snap_vel, keep_vel.data(), sizeof(float4) * n, cudaMemcpyHostToDevice), "H2D");
+    if (st == PBF_OK) st = h->cuda(cudaMemcpy(h->snap_id, keep_id.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice), "H2D");
+    h->snap_steps = snap_steps0;
+    h->snap_time = snap_time0;
+  } else {
+    h->snap_valid = had_snap;
+  }
+  h->drop_graphs();
+  if (st == PBF_OK && out) st = pbf_get_tuning(hh, out);
+  return st;
+}
+
 static const char* kPhaseNames[pbf::kNumPhases] = {"predict", "scan", "sort", "gather", "neighbors",
                                                     "lambda", "deltap", "xsph", "vorticity", "stats"};
 

@@ -28,6 +28,11 @@ class PbfError(RuntimeError):
         self.status = status
 
 
+class CTuning(ctypes.Structure):
+    _fields_ = [("block_predict", ctypes.c_int32), ("block_nbr", ctypes.c_int32),
+                ("block_solve", ctypes.c_int32), ("block_misc", ctypes.c_int32)]
+
+
 class CStats(ctypes.Structure):
     _fields_ = [
         ("steps", ctypes.c_uint64),
@@ -72,6 +77,9 @@ def _declare(L):
         "pbf_get_neighbors": (st, [P, P, P, sz, P]),
         "pbf_get_cells": (st, [P, P]),
         "pbf_get_predicted": (st, [P, P]),
+        "pbf_get_tuning": (st, [P, P]),
+        "pbf_set_tuning": (st, [P, P]),
+        "pbf_autotune": (st, [P, ctypes.c_double, ctypes.c_int, P]),
         "pbf_sort": (st, [P]),
         "pbf_snapshot": (st, [P]),
         "pbf_restore": (st, [P]),
@@ -249,6 +257,23 @@ class Simulator:
         out = np.zeros(self.n, dtype=np.uint32)
         self._check(lib().pbf_get_cells(self._h, _ptr(out)))
         return out
+
+    def tuning(self) -> dict:
+        t = CTuning()
+        self._check(lib().pbf_get_tuning(self._h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in CTuning._fields_}
+
+    def set_tuning(self, **kw):
+        cur = self.tuning()
+        cur.update(kw)
+        t = CTuning(**cur)
+        self._check(lib().pbf_set_tuning(self._h, ctypes.byref(t)))
+
+    def autotune(self, dt: float = 0.0, reps: int = 3) -> dict:
+        """Pick the fastest launch shape per kernel family on the current state."""
+        t = CTuning()
+        self._check(lib().pbf_autotune(self._h, float(dt), int(reps), ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in CTuning._fields_}
 
     def sort(self):
         self._check(lib().pbf_sort(self._h))

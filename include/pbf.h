@@ -197,6 +197,25 @@ PBF_API pbf_status pbf_reset_phase_times(pbf_handle* h);
 PBF_API int pbf_num_phases(void);
 PBF_API const char* pbf_phase_name(int phase);
 
+/* Launch shapes (threads per block) of the kernel families of a step. */
+typedef struct pbf_tuning {
+  int32_t block_predict;  /* prediction, cell count */
+  int32_t block_nbr;      /* neighbour-set build */
+  int32_t block_solve;    /* lambda, delta-p, XSPH/vorticity passes */
+  int32_t block_misc;     /* scatter, cell sort, gather */
+} pbf_tuning;
+
+PBF_API pbf_status pbf_get_tuning(pbf_handle* h, pbf_tuning* out);
+/* Each block size must be 64, 128, 256 or 512. Drops captured graphs. */
+PBF_API pbf_status pbf_set_tuning(pbf_handle* h, const pbf_tuning* t);
+/*
+ * Autotuner: times every candidate block size of each kernel family with
+ * CUDA events over `reps` steps of dt from the current state (checkpointed
+ * and restored around every trial, so the state is unchanged on return),
+ * keeps the fastest shape per family and reports it in *out (may be NULL).
+ */
+PBF_API pbf_status pbf_autotune(pbf_handle* h, double dt, int reps, pbf_tuning* out);
+
 PBF_API size_t pbf_size(const pbf_handle* h);
 PBF_API int pbf_num_scenes(const pbf_handle* h);
 

@@ -252,3 +252,20 @@ def test_neighbor_capacity_is_reported(pbf):
         with pytest.raises(pbf.PbfError) as e:
             sim.time_step(prm.dt, 1)
         assert e.value.status == 5
+
+
+def test_autotune_keeps_state_and_results(pbf):
+    """The autotuner restores the state it timed on; launch shapes never change results."""
+    sc = scenes.block4096(3)
+    with pbf.Simulator(_f32(sc.pos), _f32(sc.vel), sc.params) as sim:
+        sim.time_step(sc.params.dt, 2)
+        x0 = sim.positions()
+        best = sim.autotune(sc.params.dt, reps=2)
+        assert all(v in (64, 128, 256, 512) for v in best.values())
+        assert np.array_equal(sim.positions(), x0)
+        sim.time_step(sc.params.dt, 3)
+        xa = sim.positions()
+    with pbf.Simulator(_f32(sc.pos), _f32(sc.vel), sc.params) as sim:
+        sim.set_tuning(block_nbr=512, block_solve=64, block_predict=128, block_misc=64)
+        sim.time_step(sc.params.dt, 5)
+        assert np.array_equal(sim.positions(), xa)
