@@ -151,7 +151,7 @@ void Handle::free_all() {
   }
   void* ptrs[] = {b.pos[0], b.pos[1], b.disp[0], b.disp[1], b.xs[0], b.xs[1], b.vel[0], b.vel[1],
                   b.omega, b.pred, b.lam, b.rho, b.rho_iter0, b.id[0], b.id[1], b.key, b.rank,
-                  b.perm, b.nbr_cnt, b.skey, b.nbr_w, b.cell_count, b.cell_start, b.scan_tmp, b.scenes,
+                  b.perm, b.nbr_hdr, b.nbr_w, b.cell_count, b.cell_start, b.scan_tmp, b.scenes,
                   b.stats, b.err, b.io, b.io2, scratch, snap_pos, snap_vel, snap_id};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -177,7 +177,7 @@ pbf_status Handle::alloc_all() {
       {(void**)&b.xs[0], f4}, {(void**)&b.xs[1], f4}, {(void**)&b.vel[0], f4}, {(void**)&b.vel[1], f4},
       {(void**)&b.omega, f4}, {(void**)&b.lam, u4}, {(void**)&b.rho, u4}, {(void**)&b.rho_iter0, u4},
       {(void**)&b.id[0], u4}, {(void**)&b.id[1], u4}, {(void**)&b.key, u4}, {(void**)&b.rank, u4},
-      {(void**)&b.perm, u4}, {(void**)&b.nbr_cnt, u4}, {(void**)&b.skey, u4},
+      {(void**)&b.perm, u4}, {(void**)&b.nbr_hdr, sizeof(uint4) * n},
       {(void**)&b.nbr_w, u4 * static_cast<size_t>(b.max_words)},
       {(void**)&b.cell_count, sizeof(uint32_t) * b.n_cells},
       {(void**)&b.cell_start, sizeof(uint32_t) * (b.n_cells + 1)},
@@ -433,7 +433,6 @@ pbf_status pbf_batch_create(const pbf_params* params, int n_scenes, const size_t
   pbf::DeviceGuard g(device);
   pbf_status st = h->cuda(cudaSetDevice(device), "cudaSetDevice");
   if (st == PBF_OK) st = h->cuda(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
-  if (st == PBF_OK) st = h->cuda(pbf::configure_kernels(), "kernel attributes");
   if (st == PBF_OK) st = h->alloc_all();
   if (st == PBF_OK)
     st = h->cuda(cudaMemcpyAsync(h->b.scenes, scenes.data(), sizeof(pbf::SceneDesc) * n_scenes,

@@ -1,6 +1,6 @@
 // Device-side building blocks of the PBF step: vector helpers, the SPH
-// kernels of the reference and the box collider. Included by every PBF
-// translation unit.
+// kernels of the reference, the box collider and the compressed neighbour
+// iteration. Included by every PBF translation unit.
 #pragma once
 
 #include <cstdint>
@@ -47,6 +47,10 @@ __device__ __forceinline__ CellCoord cell_of(const float3 p, const SceneDesc& sc
 }
 __device__ __forceinline__ uint32_t cell_key(const CellCoord& c, const SceneDesc& sc) {
   return sc.cell_off + static_cast<uint32_t>((c.z * sc.dim[1] + c.y) * sc.dim[0] + c.x);
+}
+__device__ __forceinline__ uint32_t pack_coord(const CellCoord& c) {
+  return static_cast<uint32_t>(c.x) | (static_cast<uint32_t>(c.y) << 10) |
+         (static_cast<uint32_t>(c.z) << 21);
 }
 
 // ---- collider ------------------------------------------------------------------
@@ -135,6 +139,41 @@ __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 
     const float qa = cmp3(q, a);
     if (qa < P.clamp_lo[a]) set3(d, a, P.clamp_lo[a] - cmp3(x, a));
     else if (qa > P.clamp_hi[a]) set3(d, a, P.clamp_hi[a] - cmp3(x, a));
+  }
+}
+
+// ---- neighbour lists -----------------------------------------------------------
+// A particle's neighbours lie in 3 z-slabs (dz = -1, 0, 1) of its cell; inside a slab
+// they lie in the rows dy = -1..1 of cells cx-1..cx+1, all within 2*nx+3 cells after the
+// slab's first candidate cell, i.e. a short slot range of the cell-sorted arrays. A
+// neighbour is stored as a u16 entry (slab << 14 | slot offset from the slab's first
+// candidate slot), two entries per u32 word, word-major ([word][N]) so a warp's loads of
+// one word index coalesce. hdr = {slab base -1, slab base 0, slab base +1, count}.
+constexpr int kOffsetBits = 14;
+constexpr uint32_t kOffsetMask = (1u << kOffsetBits) - 1u;
+
+__device__ __forceinline__ int nbr_total(const uint4& h) { return static_cast<int>(h.w); }
+
+__device__ __forceinline__ uint32_t nbr_decode(const uint4& h, uint32_t e) {
+  const uint32_t g = e >> kOffsetBits;
+  const uint32_t base = g == 0u ? h.x : (g == 1u ? h.y : h.z);
+  return base + (e & kOffsetMask);
+}
+
+// Calls f(j) for every neighbour slot j of slot i, ascending.
+template <typename F>
+__device__ __forceinline__ void for_each_neighbor(int i, int n, const uint4 h,
+                                                  const uint32_t* __restrict__ words, F&& f) {
+  const int total = nbr_total(h);
+  int k = 0;
+  for (; k + 1 < total; k += 2) {
+    const uint32_t w = __ldg(&words[static_cast<size_t>(k >> 1) * n + i]);
+    f(nbr_decode(h, w & 0xffffu));
+    f(nbr_decode(h, w >> 16));
+  }
+  if (k < total) {
+    const uint32_t w = __ldg(&words[static_cast<size_t>(k >> 1) * n + i]);
+    f(nbr_decode(h, w & 0xffffu));
   }
 }
 

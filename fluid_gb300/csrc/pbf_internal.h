@@ -10,10 +10,8 @@
 //   lam    float   lambda                                    4 B
 //   rho    float   reported density                          4 B
 //   id     u32     original particle index                   4 B
-//   skey    u32    cell key of each slot
-//   nbr_cnt u32    neighbour count
-//   nbr_w   u32    [words][N] neighbour entries (u16 index into the cell's candidate
-//                  enumeration), 2 per word, word-major
+//   nbr_hdr uint4  first candidate slot of the 3 z-slabs, neighbour count
+//   nbr_w   u32    [words][N] neighbour entries, 2 x u16 per word, word-major
 //   cell_count / cell_start u32 [C] / [C+1]
 #pragma once
 
@@ -86,8 +84,7 @@ struct Buffers {
   uint32_t* key = nullptr;
   uint32_t* rank = nullptr;
   uint32_t* perm = nullptr;
-  uint32_t* nbr_cnt = nullptr;  // neighbours per slot
-  uint32_t* skey = nullptr;     // cell key per slot (cell order)
+  uint4* nbr_hdr = nullptr;
   uint32_t* nbr_w = nullptr;
   uint32_t* cell_count = nullptr;
   uint32_t* cell_start = nullptr;  // n_cells + 1
@@ -138,8 +135,6 @@ struct PhaseMarks {
 };
 
 // ---- launchers (pbf_kernels.cu) ----
-// Per-process kernel attributes (shared-memory opt-ins); call once per device.
-cudaError_t configure_kernels();
 // cur: index of the buffers holding the current (sorted) state; the step
 // writes the next state into 1 - cur.
 cudaError_t launch_step(const Buffers& b, const DevParams& p, const Tuning& t, int cur,

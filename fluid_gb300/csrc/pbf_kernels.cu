@@ -8,20 +8,19 @@
 //   k_scan_*      exclusive prefix sum of the cell counts
 //   k_scatter     slot = cell start + rank
 //   k_cellsort    order each cell's slots by original index (determinism)
-//   k_gather      reorder x, delta, id, cell key into cell order; x* = x + delta
-//   k_cells_build neighbour sets |x*_i - x*_j|^2 <= H2 over the 27 cells
-//                 (particles.cpp:258-265) + lambda of iteration 0
-//   k_cells_lambda  density + lambda      (particles.cpp:185-204)   x (iters - 1)
-//   k_cells_deltap  delta p + collision   (particles.cpp:206-213)   x iters
-//   k_cells_xsph    velocity, vorticity, XSPH, reported density
-//                   (particles.cpp:215-234, order-independent form)
-//   k_cells_vort    vorticity confinement, x <- x* (particles.cpp:236-248)
-// The k_cells_* kernels are cell-cooperative (pbf_cells.cuh).
+//   k_gather      reorder x, delta, id into cell order; x* = x + delta
+//   k_nbr_build   neighbour sets |x*_i - x*_j|^2 <= H2 over the 27 cells,
+//                 stored row-compressed (particles.cpp:258-265)
+//   k_lambda      density + lambda            (particles.cpp:185-204)   x iters
+//   k_deltap      delta p + collision         (particles.cpp:206-213)   x iters
+//   k_xsph        velocity, vorticity, XSPH, reported density
+//                 (particles.cpp:215-234, order-independent form)
+//   k_vort        vorticity confinement, x <- x* (particles.cpp:236-248)
 #include <cfloat>
 #include <climits>
 #include <cstdint>
 
-#include "pbf_cells.cuh"
+#include "pbf_device.cuh"
 
 namespace pbf {
 namespace {
@@ -185,14 +184,12 @@ __global__ void k_cellsort(const uint32_t* __restrict__ cell_start, uint32_t* __
 
 __global__ void k_gather(const uint32_t* __restrict__ perm, const float4* __restrict__ pos_a,
                          const float4* __restrict__ disp_a, const float4* __restrict__ vel_a,
-                         const uint32_t* __restrict__ id_a, const uint32_t* __restrict__ key_a,
-                         float4* __restrict__ pos_b, float4* __restrict__ disp_b, float4* __restrict__ xs_b,
-                         float4* __restrict__ vel_b, uint32_t* __restrict__ id_b, uint32_t* __restrict__ key_b,
-                         int n) {
+                         const uint32_t* __restrict__ id_a, float4* __restrict__ pos_b,
+                         float4* __restrict__ disp_b, float4* __restrict__ xs_b,
+                         float4* __restrict__ vel_b, uint32_t* __restrict__ id_b, int n) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const uint32_t i = perm[s];
-  key_b[s] = key_a[i];
   const float4 x = pos_a[i];
   pos_b[s] = x;
   id_b[s] = id_a[i];
@@ -205,438 +202,216 @@ __global__ void k_gather(const uint32_t* __restrict__ perm, const float4* __rest
 }
 
 // ---------------------------------------------------------------------------
-// neighbour sets + first-iteration lambda; lambda / delta-p / XSPH / vorticity
-// passes (cell-cooperative, see pbf_cells.cuh)
+// neighbour sets
 // ---------------------------------------------------------------------------
-struct LambdaAcc {
-  float qsum, g2;
-  float3 gs;
-};
-__device__ __forceinline__ void lambda_add(LambdaAcc& a, const Pair& p) {
-  a.qsum += p.q * p.q * p.q;
-  a.gs = a.gs + p.r * p.s;
-  a.g2 += p.s * p.s * p.r2;
-}
-__device__ __forceinline__ void lambda_reduce(LambdaAcc& a, int L) {
-  a.qsum = group_sum(a.qsum, L);
-  a.g2 = group_sum(a.g2, L);
-  a.gs.x = group_sum(a.gs.x, L);
-  a.gs.y = group_sum(a.gs.y, L);
-  a.gs.z = group_sum(a.gs.z, L);
-}
-// newtonStepCalculateLambda, particles.cpp:185-204
-__device__ __forceinline__ float lambda_of(const LambdaAcc& a, const DevParams& P, float* rho) {
-  *rho = P.poly6_c * a.qsum;
-  const float kg = P.spiky_c * P.inv_rho0;
-  const float denom = kg * kg * (a.g2 + dot3(a.gs, a.gs)) + P.epsilon;
-  return -(*rho * P.inv_rho0 - 1.0f) / denom;
-}
-
-__device__ __forceinline__ uint32_t entry_of(uint32_t w, int half) { return half ? (w >> 16) : (w & 0xffffu); }
-
-// The build: neighbour sets N(i) = {j != i : fl(|x*_i - x*_j|^2) <= H2}
-// (particles.cpp:258-265) as candidate indices, and lambda of iteration 0.
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_cells_build(float4* xs, const float4* __restrict__ pos,
-                                                            const uint32_t* __restrict__ skey,
-                                                            const uint32_t* __restrict__ cell_start,
-                                                            const SceneDesc* __restrict__ scenes,
-                                                            uint32_t* __restrict__ nbr_cnt,
-                                                            uint32_t* __restrict__ words, float* __restrict__ lam,
-                                                            float* __restrict__ rho_iter0,
-                                                            unsigned* __restrict__ err, DevParams P, int n) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int warp = static_cast<int>(threadIdx.x >> 5);
-  unsigned char* my = smem + warp * kBuildWarpBytes;
-  float4* cand = reinterpret_cast<float4*>(my);
-  uint16_t* list = reinterpret_cast<uint16_t*>(my + kCandMax * 16);
-  int* cnt_s = reinterpret_cast<int*>(my + kCandMax * 16 + kBuildM * kBuildCap * 2);
-  CellRows* rows = reinterpret_cast<CellRows*>(my + kCandMax * 16 + kBuildM * kBuildCap * 2 + 128);
-  const unsigned lane = lane_id();
-  const unsigned lt = lanemask_lt_();
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ xs,
+                                                     const float4* __restrict__ pos,
+                                                     const uint32_t* __restrict__ cell_start,
+                                                     const SceneDesc* __restrict__ scenes,
+                                                     uint4* __restrict__ hdr, uint32_t* __restrict__ words,
+                                                     unsigned* __restrict__ err, DevParams P, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = xs[i];
+  const SceneDesc& sc = scenes[scene_of_slot(pos[i])];
+  const CellCoord cc = cell_of(f3(xi), sc, P.inv_cell);
   const int cap = P.max_words * 2;
-  const int fast_cap = cap < kBuildCap ? cap : kBuildCap;
+  uint32_t gbase[3] = {0u, 0u, 0u};
+  int total = 0;
+  uint32_t word = 0;
   unsigned flags = 0;
-  for_each_owned_cell(skey, cell_start, pos, n, static_cast<int>(blockIdx.x) * WARPS + warp,
-                      [&](const CellInfo& c, uint32_t key) {
-    const SceneDesc& sc = scenes[c.sid];
-    cell_rows(key, sc, cell_start, rows, &flags);
-    const uint32_t total = rows->pref[9];
-    const uint32_t self0 = rows->pref[4] + (c.cs - rows->start[4]);
-    // fast: the cell fits the buffers and lies inside its own (uncapped) staged row
-    bool fast = c.m <= static_cast<uint32_t>(kBuildM) && total <= static_cast<uint32_t>(kCandMax) &&
-                (c.cs - rows->start[4]) + c.m <= rows->pref[5] - rows->pref[4];
-    if (fast) {
-      stage_rows(rows, xs, cand);
-      __syncwarp();
-      int cnt = 0;
-      for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-        const uint32_t t = t0 + lane;
-        const bool has = t < total;
-        const float4 xj = has ? cand[t] : make_float4(0.f, 0.f, 0.f, 0.f);
-        for (uint32_t q = 0; q < c.m; ++q) {
-          const float4 xq = cand[self0 + q];
-          const bool hit = has && t != self0 + q && dist2_rn(xq, xj) <= P.h2;
-          const unsigned b = __ballot_sync(0xffffffffu, hit);
-          if (b) {
-            const int cq = __shfl_sync(0xffffffffu, cnt, static_cast<int>(q));
-            if (hit) {
-              const int rank = cq + __popc(b & lt);
-              if (rank < fast_cap) list[q * kBuildCap + rank] = static_cast<uint16_t>(t);
-            }
-            if (lane == q) cnt += __popc(b);
-          }
-        }
+  const int x0 = cc.x > 0 ? cc.x - 1 : 0;
+  const int x1 = cc.x + 1 < sc.dim[0] ? cc.x + 1 : sc.dim[0] - 1;
+  const int y0 = cc.y > 0 ? cc.y - 1 : 0;
+  const int y1 = cc.y + 1 < sc.dim[1] ? cc.y + 1 : sc.dim[1] - 1;
+#pragma unroll
+  for (int g = 0; g < 3; ++g) {
+    const int z = cc.z + g - 1;
+    if (z < 0 || z >= sc.dim[2]) continue;
+    const uint32_t slab = sc.cell_off + static_cast<uint32_t>(z * sc.dim[1] * sc.dim[0]);
+    const uint32_t gstart = __ldg(&cell_start[slab + static_cast<uint32_t>(y0 * sc.dim[0] + x0)]);
+    gbase[g] = gstart;
+#pragma unroll 1
+    for (int y = y0; y <= y1; ++y) {
+      const uint32_t row = slab + static_cast<uint32_t>(y * sc.dim[0]);
+      const uint32_t start = __ldg(&cell_start[row + x0]);
+      uint32_t end = __ldg(&cell_start[row + x1 + 1]);
+      if (end - start > static_cast<uint32_t>(kMaxRowCandidates)) {
+        flags |= PBF_ERRBIT_ROW_CAPACITY;
+        end = start + kMaxRowCandidates;
       }
-      if (__any_sync(0xffffffffu, lane < c.m && cnt > fast_cap)) {
-        fast = false;  // a list overflows the buffer: redo the cell per particle
-      } else {
-        if (lane < c.m) {
-          cnt_s[lane] = cnt;
-          nbr_cnt[c.cs + lane] = static_cast<uint32_t>(cnt);
-        }
-        __syncwarp();
-        const unsigned mw = __reduce_max_sync(0xffffffffu, lane < c.m ? static_cast<unsigned>((cnt + 1) >> 1) : 0u);
-        for (uint32_t idx = lane; idx < c.m * mw; idx += 32) {
-          const uint32_t q = idx % c.m, w = idx / c.m;
-          const int cq = cnt_s[q];
-          if (static_cast<int>(2 * w) < cq) {
-            const uint32_t e0 = list[q * kBuildCap + 2 * w];
-            const uint32_t e1 = static_cast<int>(2 * w + 1) < cq ? list[q * kBuildCap + 2 * w + 1] : 0u;
-            words[static_cast<size_t>(w) * n + c.cs + q] = e0 | (e1 << 16);
-          }
-        }
-        const int L = lanes_per_particle(c.m), per = 32 / L;
-        for (uint32_t q0 = 0; q0 < c.m; q0 += per) {
-          const uint32_t q = q0 + lane / L;
-          const int sub = static_cast<int>(lane) % L;
-          const bool act = q < c.m;
-          LambdaAcc a{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
-          if (act) {
-            const float4 xi = cand[self0 + q];
-            const int cq = cnt_s[q];
-            for (int k = sub; k < cq; k += L) lambda_add(a, pair_of(xi, cand[list[q * kBuildCap + k]], P.h, P.h2));
-          }
-          lambda_reduce(a, L);
-          if (act && sub == 0) {
-            float rho;
-            const float l = lambda_of(a, P, &rho);
-            const uint32_t i = c.cs + q;
-            lam[i] = l;
-            reinterpret_cast<float*>(xs)[4 * i + 3] = l;
-            if (rho_iter0) rho_iter0[i] = rho;
+      for (uint32_t j = start; j < end; ++j) {
+        if (j == static_cast<uint32_t>(i)) continue;
+        const float4 xj = __ldg(&xs[j]);
+        if (dist2_rn(xi, xj) <= P.h2) {
+          const uint32_t off = j - gstart;
+          if (off > kOffsetMask) {
+            flags |= PBF_ERRBIT_ROW_CAPACITY;
+          } else if (total < cap) {
+            const uint32_t e = (static_cast<uint32_t>(g) << kOffsetBits) | off;
+            if ((total & 1) == 0) {
+              word = e;
+            } else {
+              word |= e << 16;
+              words[static_cast<size_t>(total >> 1) * n + i] = word;
+            }
+            ++total;
+          } else {
+            flags |= PBF_ERRBIT_NEIGHBOR_CAPACITY;
           }
         }
       }
     }
-    if (!fast) {
-      for (uint32_t q = lane; q < c.m; q += 32) {
-        const uint32_t i = c.cs + q;
-        const float4 xi = xs[i];
-        int cnt = 0;
-        uint32_t word = 0;
-        for (int r = 0; r < 9; ++r) {
-          const uint32_t p0 = rows->pref[r], len = rows->pref[r + 1] - p0, s0 = rows->start[r];
-          for (uint32_t u = 0; u < len; ++u) {
-            const uint32_t j = s0 + u;
-            if (j == i) continue;
-            if (dist2_rn(xi, __ldg(&xs[j])) <= P.h2) {
-              if (cnt < cap) {
-                const uint32_t e = p0 + u;
-                if ((cnt & 1) == 0) {
-                  word = e;
-                } else {
-                  word |= e << 16;
-                  words[static_cast<size_t>(cnt >> 1) * n + i] = word;
-                }
-                ++cnt;
-              } else {
-                flags |= PBF_ERRBIT_NEIGHBOR_CAPACITY;
-              }
-            }
-          }
-        }
-        if (cnt & 1) words[static_cast<size_t>(cnt >> 1) * n + i] = word;
-        nbr_cnt[i] = static_cast<uint32_t>(cnt);
-        LambdaAcc a{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
-        for (int k = 0; k < cnt; ++k) {
-          const uint32_t e = entry_of(words[static_cast<size_t>(k >> 1) * n + i], k & 1);
-          lambda_add(a, pair_of(xi, __ldg(&xs[cand_slot(rows, e)]), P.h, P.h2));
-        }
-        float rho;
-        const float l = lambda_of(a, P, &rho);
-        lam[i] = l;
-        reinterpret_cast<float*>(xs)[4 * i + 3] = l;
-        if (rho_iter0) rho_iter0[i] = rho;
-      }
-    }
-    __syncwarp();
-  });
-  if (flags) atomicOr(err, flags);
-}
-
-// Passes. Per owned cell: rows, staging (when the candidates fit), then L lanes
-// per particle walk the particle's list words (lane sub takes words sub, sub+L,
-// ...), each word holding two candidate indices; partial sums are reduced over
-// the L lanes and lane sub = 0 finishes the particle.
-#define PBF_PASS_PROLOGUE(STAGE)                                                   \
-  cell_rows(key, sc, cell_start, rows, &flags);                                    \
-  const uint32_t total = rows->pref[9];                                            \
-  const uint32_t self0 = rows->pref[4] + (c.cs - rows->start[4]);                  \
-  const bool fast = total <= static_cast<uint32_t>(kCandMax) &&                   \
-                    (c.cs - rows->start[4]) + c.m <= rows->pref[5] - rows->pref[4];  \
-  if (fast) {                                                                      \
-    STAGE;                                                                         \
-    __syncwarp();                                                                  \
-  }                                                                                \
-  const int L = lanes_per_particle(c.m), per = 32 / L;
-
-#define PBF_FOR_NEIGHBORS(BODY)                                                    \
-  for (int wk_ = sub; 2 * wk_ < cq; wk_ += L) {                                    \
-    const uint32_t wd = __ldg(&words[static_cast<size_t>(wk_) * n + i]);           \
-    _Pragma("unroll") for (int hh = 0; hh < 2; ++hh) {                             \
-      if (2 * wk_ + hh < cq) {                                                     \
-        const uint32_t t = entry_of(wd, hh);                                       \
-        const uint32_t jj = fast ? t : cand_slot(rows, t);                         \
-        BODY;                                                                      \
-      }                                                                            \
-    }                                                                              \
   }
-
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_cells_lambda(float4* xs, const float4* __restrict__ pos,
-                                                             const uint32_t* __restrict__ skey,
-                                                             const uint32_t* __restrict__ cell_start,
-                                                             const SceneDesc* __restrict__ scenes,
-                                                             const uint32_t* __restrict__ nbr_cnt,
-                                                             const uint32_t* __restrict__ words,
-                                                             float* __restrict__ lam, unsigned* __restrict__ err,
-                                                             DevParams P, int n) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int warp = static_cast<int>(threadIdx.x >> 5);
-  unsigned char* my = smem + warp * kPassWarpBytes;
-  float4* cand = reinterpret_cast<float4*>(my);
-  CellRows* rows = reinterpret_cast<CellRows*>(my + kCandMax * 16);
-  const unsigned lane = lane_id();
-  unsigned flags = 0;
-  for_each_owned_cell(skey, cell_start, pos, n, static_cast<int>(blockIdx.x) * WARPS + warp,
-                      [&](const CellInfo& c, uint32_t key) {
-    const SceneDesc& sc = scenes[c.sid];
-    PBF_PASS_PROLOGUE(stage_rows(rows, xs, cand))
-    for (uint32_t q0 = 0; q0 < c.m; q0 += per) {
-      const uint32_t q = q0 + lane / L;
-      const int sub = static_cast<int>(lane) % L;
-      const bool act = q < c.m;
-      const uint32_t i = c.cs + q;
-      const int cq = act ? static_cast<int>(__ldg(&nbr_cnt[i])) : 0;
-      const float4 xi = act ? (fast ? cand[self0 + q] : xs[i]) : make_float4(0.f, 0.f, 0.f, 0.f);
-      LambdaAcc a{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
-      PBF_FOR_NEIGHBORS(lambda_add(a, pair_of(xi, fast ? cand[jj] : __ldg(&xs[jj]), P.h, P.h2)))
-      lambda_reduce(a, L);
-      if (act && sub == 0) {
-        float rho;
-        const float l = lambda_of(a, P, &rho);
-        lam[i] = l;
-        reinterpret_cast<float*>(xs)[4 * i + 3] = l;
-      }
-    }
-    __syncwarp();
-  });
+  if (total & 1) words[static_cast<size_t>(total >> 1) * n + i] = word;
+  hdr[i] = make_uint4(gbase[0], gbase[1], gbase[2], static_cast<uint32_t>(total));
   if (flags) atomicOr(err, flags);
 }
 
-// newtonStepUpdatePosition (particles.cpp:206-213) + clamp (:51-84). lambda_j
-// arrives in x*_j.w; N4 specialises the tensile exponent N = 4 (particles.cpp:40).
-template <int WARPS, bool N4>
-__global__ void __launch_bounds__(WARPS * 32) k_cells_deltap(const float4* __restrict__ xs,
-                                                             const float4* __restrict__ pos,
-                                                             const uint32_t* __restrict__ skey,
-                                                             const uint32_t* __restrict__ cell_start,
-                                                             const SceneDesc* __restrict__ scenes,
-                                                             const uint32_t* __restrict__ nbr_cnt,
-                                                             const uint32_t* __restrict__ words,
-                                                             float4* __restrict__ disp, float4* __restrict__ xs_next,
-                                                             unsigned* __restrict__ err, DevParams P, int n) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int warp = static_cast<int>(threadIdx.x >> 5);
-  unsigned char* my = smem + warp * kPassWarpBytes;
-  float4* cand = reinterpret_cast<float4*>(my);
-  CellRows* rows = reinterpret_cast<CellRows*>(my + kCandMax * 16);
-  const unsigned lane = lane_id();
+// ---------------------------------------------------------------------------
+// Jacobi density-constraint iterations
+// ---------------------------------------------------------------------------
+// lambda_i is stored in x*_i.w of the same buffer: within this pass every
+// thread reads only .xyz of its neighbours' x*, which no thread writes.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs, const uint4* __restrict__ hdr,
+                                                  const uint32_t* __restrict__ words,
+                                                  float* __restrict__ lam, float* __restrict__ rho_iter0,
+                                                  DevParams P, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = xs[i];
+  float qsum = 0.f, g2 = 0.f;
+  float3 gs = make_float3(0.f, 0.f, 0.f);
+  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
+    const Pair p = pair_of(xi, xs[j], P.h, P.h2);
+    qsum += p.q * p.q * p.q;
+    gs = gs + p.r * p.s;
+    g2 += p.s * p.s * p.r2;
+  });
+  const float rho = P.poly6_c * qsum;
+  const float kg = P.spiky_c * P.inv_rho0;
+  const float denom = kg * kg * (g2 + dot3(gs, gs)) + P.epsilon;
+  const float l = -(rho * P.inv_rho0 - 1.0f) / denom;
+  lam[i] = l;
+  reinterpret_cast<float*>(xs)[4 * i + 3] = l;
+  if (rho_iter0) rho_iter0[i] = rho;
+}
+
+// (lambda_i + lambda_j + s_corr) grad W summed over neighbours; N4 specialises the
+// tensile exponent N = 4 of particles.cpp:40.
+template <int BLOCK, bool N4>
+__global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
+                                                  const float4* __restrict__ pos,
+                                                  const uint4* __restrict__ hdr,
+                                                  const uint32_t* __restrict__ words,
+                                                  const SceneDesc* __restrict__ scenes,
+                                                  float4* __restrict__ disp, float4* __restrict__ xs_next,
+                                                  DevParams P, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = xs[i];
+  const float li = xi.w;  // lambda_i (k_lambda stores it in x*.w)
   const float wt = P.poly6_c * P.tis;
-  unsigned flags = 0;
-  for_each_owned_cell(skey, cell_start, pos, n, static_cast<int>(blockIdx.x) * WARPS + warp,
-                      [&](const CellInfo& c, uint32_t key) {
-    const SceneDesc& sc = scenes[c.sid];
-    PBF_PASS_PROLOGUE(stage_rows(rows, xs, cand))
-    for (uint32_t q0 = 0; q0 < c.m; q0 += per) {
-      const uint32_t q = q0 + lane / L;
-      const int sub = static_cast<int>(lane) % L;
-      const bool act = q < c.m;
-      const uint32_t i = c.cs + q;
-      const int cq = act ? static_cast<int>(__ldg(&nbr_cnt[i])) : 0;
-      const float4 xi = act ? (fast ? cand[self0 + q] : __ldg(&xs[i])) : make_float4(0.f, 0.f, 0.f, 0.f);
-      float3 dp = make_float3(0.f, 0.f, 0.f);
-      PBF_FOR_NEIGHBORS({
-        const float4 xj = fast ? cand[jj] : __ldg(&xs[jj]);
-        const Pair p = pair_of(xi, xj, P.h, P.h2);
-        const float a = wt * (p.q * p.q * p.q);  // W / W(dq)
-        float an;
-        if (N4) {
-          const float a2 = a * a;
-          an = a2 * a2;
-        } else {
-          an = a;
-          for (int e = 1; e < P.scorr_n; ++e) an *= a;
-        }
-        const float coef = (xi.w + xj.w) - P.scorr_k * an;  // lambda_i + lambda_j + s_corr
-        dp = dp + p.r * (coef * p.s);
-      })
-      dp.x = group_sum(dp.x, L);
-      dp.y = group_sum(dp.y, L);
-      dp.z = group_sum(dp.z, L);
-      if (act && sub == 0) {
-        dp = dp * (P.spiky_c * P.inv_rho0);
-        const float4 x4 = __ldg(&pos[i]);
-        float3 d = f3(disp[i]);
-        const float3 x = f3(x4);
-        collide(x, d, dp, false, sc, P);
-        disp[i] = make_float4(d.x, d.y, d.z, 0.f);
-        xs_next[i] = make_float4(x.x + d.x, x.y + d.y, x.z + d.z, 0.f);
-      }
+  float3 dp = make_float3(0.f, 0.f, 0.f);
+  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
+    const float4 xj = __ldg(&xs[j]);
+    const Pair p = pair_of(xi, xj, P.h, P.h2);
+    const float a = wt * (p.q * p.q * p.q);  // W / W(dq)
+    float an;
+    if (N4) {
+      const float a2 = a * a;
+      an = a2 * a2;
+    } else {
+      an = a;
+      for (int e = 1; e < P.scorr_n; ++e) an *= a;
     }
-    __syncwarp();
+    const float coef = (li + xj.w) - P.scorr_k * an;  // lambda_i + lambda_j + s_corr
+    dp = dp + p.r * (coef * p.s);
   });
-  if (flags) atomicOr(err, flags);
+  dp = dp * (P.spiky_c * P.inv_rho0);
+  const float4 x4 = pos[i];
+  const SceneDesc& sc = scenes[scene_of_slot(x4)];
+  const float4 d4 = disp[i];
+  float3 d = f3(d4);
+  const float3 x = f3(x4);
+  collide(x, d, dp, false, sc, P);
+  disp[i] = make_float4(d.x, d.y, d.z, 0.f);
+  xs_next[i] = make_float4(x.x + d.x, x.y + d.y, x.z + d.z, 0.f);
 }
 
-// updateVelocity + calculateVorticityApplyXSPHViscosity (particles.cpp:215-234) in
-// the order-independent form; |omega_i| goes to x*_i.w for the vorticity pass.
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_cells_xsph(float4* xs, const float4* __restrict__ pos,
-                                                           const uint32_t* __restrict__ skey,
-                                                           const uint32_t* __restrict__ cell_start,
-                                                           const SceneDesc* __restrict__ scenes,
-                                                           const uint32_t* __restrict__ nbr_cnt,
-                                                           const uint32_t* __restrict__ words,
-                                                           const float4* __restrict__ disp,
-                                                           float4* __restrict__ vel_out, float4* __restrict__ omega,
-                                                           float* __restrict__ rho_out, unsigned* __restrict__ err,
-                                                           DevParams P, float inv_dt, int n) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int warp = static_cast<int>(threadIdx.x >> 5);
-  unsigned char* my = smem + warp * kPass2WarpBytes;
-  float4* cand = reinterpret_cast<float4*>(my);
-  float4* cand_d = cand + kCandMax;
-  CellRows* rows = reinterpret_cast<CellRows*>(my + 2 * kCandMax * 16);
-  const unsigned lane = lane_id();
-  unsigned flags = 0;
-  for_each_owned_cell(skey, cell_start, pos, n, static_cast<int>(blockIdx.x) * WARPS + warp,
-                      [&](const CellInfo& c, uint32_t key) {
-    const SceneDesc& sc = scenes[c.sid];
-    PBF_PASS_PROLOGUE({
-      stage_rows(rows, xs, cand);
-      stage_rows(rows, disp, cand_d);
-    })
-    for (uint32_t q0 = 0; q0 < c.m; q0 += per) {
-      const uint32_t q = q0 + lane / L;
-      const int sub = static_cast<int>(lane) % L;
-      const bool act = q < c.m;
-      const uint32_t i = c.cs + q;
-      const int cq = act ? static_cast<int>(__ldg(&nbr_cnt[i])) : 0;
-      const float4 xi = act ? (fast ? cand[self0 + q] : xs[i]) : make_float4(0.f, 0.f, 0.f, 0.f);
-      const float3 vi = act ? f3(fast ? cand_d[self0 + q] : __ldg(&disp[i])) * inv_dt : make_float3(0.f, 0.f, 0.f);
-      float qsum = 0.f;
-      float3 visc = make_float3(0.f, 0.f, 0.f), w = make_float3(0.f, 0.f, 0.f);
-      PBF_FOR_NEIGHBORS({
-        const Pair p = pair_of(xi, fast ? cand[jj] : xs[jj], P.h, P.h2);
-        const float3 vij = f3(fast ? cand_d[jj] : __ldg(&disp[jj])) * inv_dt - vi;
-        const float q3 = p.q * p.q * p.q;
-        visc = visc + vij * q3;
-        qsum += q3;
-        w = w + cross3(vij, p.r * p.s);
-      })
-      qsum = group_sum(qsum, L);
-      visc.x = group_sum(visc.x, L);
-      visc.y = group_sum(visc.y, L);
-      visc.z = group_sum(visc.z, L);
-      w.x = group_sum(w.x, L);
-      w.y = group_sum(w.y, L);
-      w.z = group_sum(w.z, L);
-      if (act && sub == 0) {
-        const float rho = P.poly6_c * qsum;
-        w = w * P.spiky_c;
-        const float3 v = vi + visc * (P.xsph_c * P.poly6_c);
-        vel_out[i] = make_float4(v.x, v.y, v.z, 0.f);
-        const float wn = sqrtf(dot3(w, w));
-        omega[i] = make_float4(w.x, w.y, w.z, wn);
-        reinterpret_cast<float*>(xs)[4 * i + 3] = wn;
-        rho_out[i] = rho;
-      }
-    }
-    __syncwarp();
+// ---------------------------------------------------------------------------
+// velocity, vorticity, XSPH, reported density; then vorticity confinement
+// ---------------------------------------------------------------------------
+// |omega_i| is stored in x*_i.w of the same buffer (neighbours read only .xyz here).
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_xsph(float4* xs, const float4* __restrict__ disp,
+                                                const uint4* __restrict__ hdr,
+                                                const uint32_t* __restrict__ words,
+                                                float4* __restrict__ vel_out, float4* __restrict__ omega,
+                                                float* __restrict__ rho_out, DevParams P, float inv_dt,
+                                                int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = xs[i];
+  const float3 vi = f3(disp[i]) * inv_dt;  // updateVelocity, particles.cpp:215-217
+  float qsum = 0.f;
+  float3 visc = make_float3(0.f, 0.f, 0.f), w = make_float3(0.f, 0.f, 0.f);
+  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
+    const Pair p = pair_of(xi, xs[j], P.h, P.h2);
+    const float3 vij = f3(__ldg(&disp[j])) * inv_dt - vi;
+    const float q3 = p.q * p.q * p.q;
+    visc = visc + vij * q3;
+    qsum += q3;
+    w = w + cross3(vij, p.r * p.s);
   });
-  if (flags) atomicOr(err, flags);
+  const float rho = P.poly6_c * qsum;
+  w = w * P.spiky_c;
+  const float3 v = vi + visc * (P.xsph_c * P.poly6_c);
+  vel_out[i] = make_float4(v.x, v.y, v.z, 0.f);
+  const float wn = sqrtf(dot3(w, w));
+  omega[i] = make_float4(w.x, w.y, w.z, wn);
+  reinterpret_cast<float*>(xs)[4 * i + 3] = wn;
+  rho_out[i] = rho;
 }
 
-// applyVorticity + updatePosition (particles.cpp:236-248); |omega_j| in x*_j.w.
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_cells_vort(const float4* __restrict__ xs, float4* __restrict__ pos,
-                                                           const uint32_t* __restrict__ skey,
-                                                           const uint32_t* __restrict__ cell_start,
-                                                           const SceneDesc* __restrict__ scenes,
-                                                           const uint32_t* __restrict__ nbr_cnt,
-                                                           const uint32_t* __restrict__ words,
-                                                           const float4* __restrict__ omega, float4* __restrict__ vel,
-                                                           unsigned* __restrict__ err, DevParams P, float dt, int n) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int warp = static_cast<int>(threadIdx.x >> 5);
-  unsigned char* my = smem + warp * kPassWarpBytes;
-  float4* cand = reinterpret_cast<float4*>(my);
-  CellRows* rows = reinterpret_cast<CellRows*>(my + kCandMax * 16);
-  const unsigned lane = lane_id();
-  unsigned flags = 0;
-  for_each_owned_cell(skey, cell_start, pos, n, static_cast<int>(blockIdx.x) * WARPS + warp,
-                      [&](const CellInfo& c, uint32_t key) {
-    const SceneDesc& sc = scenes[c.sid];
-    PBF_PASS_PROLOGUE(stage_rows(rows, xs, cand))
-    for (uint32_t q0 = 0; q0 < c.m; q0 += per) {
-      const uint32_t q = q0 + lane / L;
-      const int sub = static_cast<int>(lane) % L;
-      const bool act = q < c.m;
-      const uint32_t i = c.cs + q;
-      const int cq = act ? static_cast<int>(__ldg(&nbr_cnt[i])) : 0;
-      const float4 xi = act ? (fast ? cand[self0 + q] : __ldg(&xs[i])) : make_float4(0.f, 0.f, 0.f, 0.f);
-      float3 eta = make_float3(0.f, 0.f, 0.f);
-      PBF_FOR_NEIGHBORS({
-        const float4 xj = fast ? cand[jj] : __ldg(&xs[jj]);
-        const Pair p = pair_of(xi, xj, P.h, P.h2);
-        eta = eta + p.r * (xj.w * p.s);
-      })
-      eta.x = group_sum(eta.x, L);
-      eta.y = group_sum(eta.y, L);
-      eta.z = group_sum(eta.z, L);
-      if (act && sub == 0) {
-        eta = eta * P.spiky_c;
-        float3 v = f3(vel[i]);
-        const float en = sqrtf(dot3(eta, eta));
-        if (en > kEps) v = v + cross3(eta * (1.0f / en), f3(__ldg(&omega[i]))) * (dt * P.vort_eps);
-        vel[i] = make_float4(v.x, v.y, v.z, 0.f);
-        pos[i] = make_float4(xi.x, xi.y, xi.z, pos[i].w);  // updatePosition, particles.cpp:246-248
-        if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(xi.x) && isfinite(xi.y) &&
-              isfinite(xi.z)))
-          flags |= PBF_ERRBIT_NONFINITE;
-      }
-    }
-    __syncwarp();
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
+                                                float4* __restrict__ pos,
+                                                const float4* __restrict__ omega,
+                                                const uint4* __restrict__ hdr,
+                                                const uint32_t* __restrict__ words,
+                                                float4* __restrict__ vel, unsigned* __restrict__ err,
+                                                DevParams P, float dt, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = xs[i];
+  float3 eta = make_float3(0.f, 0.f, 0.f);
+  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
+    const float4 xj = __ldg(&xs[j]);
+    const Pair p = pair_of(xi, xj, P.h, P.h2);
+    eta = eta + p.r * (xj.w * p.s);  // |omega_j| (k_xsph stores it in x*.w)
   });
-  if (flags) atomicOr(err, flags);
+  eta = eta * P.spiky_c;
+  float3 v = f3(vel[i]);
+  const float en = sqrtf(dot3(eta, eta));
+  if (en > kEps) {
+    const float4 wi = omega[i];
+    v = v + cross3(eta * (1.0f / en), f3(wi)) * (dt * P.vort_eps);
+  }
+  const float4 p4 = pos[i];
+  vel[i] = make_float4(v.x, v.y, v.z, 0.f);
+  pos[i] = make_float4(xi.x, xi.y, xi.z, p4.w);  // updatePosition, particles.cpp:246-248
+  if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(xi.x) && isfinite(xi.y) &&
+        isfinite(xi.z)))
+    atomicOr(err, PBF_ERRBIT_NONFINITE);
 }
 
 // Step statistics (the prints of particles.cpp:267-295 and the neighbour
 // alert of :168-172, as numbers): one pass over densities and list headers.
 __global__ void __launch_bounds__(256) k_stats(const float* __restrict__ rho, const float* __restrict__ rho0,
-                                               const uint32_t* __restrict__ nbr_cnt, DevStats* __restrict__ st,
+                                               const uint4* __restrict__ hdr, DevStats* __restrict__ st,
                                                float inv_rho0, int n) {
   double r = 0.0, r0 = 0.0, es = 0.0;
   float em = 0.f;
@@ -649,7 +424,7 @@ __global__ void __launch_bounds__(256) k_stats(const float* __restrict__ rho, co
     const float e = fabsf(x * inv_rho0 - 1.0f);
     es += e;
     em = fmaxf(em, e);
-    const unsigned c = nbr_cnt[i];
+    const unsigned c = static_cast<unsigned>(nbr_total(hdr[i]));
     cmin = min(cmin, c);
     cmax = max(cmax, c);
     csum += c;
@@ -780,53 +555,20 @@ __global__ void k_cells_of(const float4* __restrict__ xs, const float4* __restri
   cells[id[s]] = cell_key(cell_of(f3(xs[s]), sc, P.inv_cell), sc);
 }
 
-__global__ void k_nbr_counts(const uint32_t* __restrict__ nbr_cnt, const uint32_t* __restrict__ id,
+__global__ void k_nbr_counts(const uint4* __restrict__ hdr, const uint32_t* __restrict__ id,
                              uint32_t* __restrict__ counts, int n) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < n) counts[id[s]] = nbr_cnt[s];
-}
-
-// Candidate rows of a cell computed by one thread (introspection paths).
-__device__ void cell_rows_thread(uint32_t key, const SceneDesc& sc, const uint32_t* __restrict__ cell_start,
-                                 CellRows* rows) {
-  const uint32_t local = key - sc.cell_off;
-  const int nx = sc.dim[0], ny = sc.dim[1], nz = sc.dim[2];
-  const int cx = static_cast<int>(local % nx), cy = static_cast<int>((local / nx) % ny);
-  const int cz = static_cast<int>(local / (nx * ny));
-  uint32_t acc = 0;
-  for (int r = 0; r < 9; ++r) {
-    const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
-    uint32_t start = 0, len = 0;
-    if (z >= 0 && z < nz && y >= 0 && y < ny) {
-      const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < nx ? cx + 1 : nx - 1;
-      const uint32_t row = sc.cell_off + static_cast<uint32_t>((z * ny + y) * nx);
-      start = cell_start[row + x0];
-      len = cell_start[row + x1 + 1] - start;
-      if (len > static_cast<uint32_t>(kMaxRowCandidates)) len = kMaxRowCandidates;
-    }
-    rows->start[r] = start;
-    rows->pref[r] = acc;
-    acc += len;
-  }
-  rows->pref[9] = acc;
+  if (s < n) counts[id[s]] = static_cast<uint32_t>(nbr_total(hdr[s]));
 }
 
 // ids[offsets[id[i]] ...] = original ids of i's neighbours (cell order).
-__global__ void k_nbr_ids(const float4* __restrict__ pos, const uint32_t* __restrict__ skey,
-                          const uint32_t* __restrict__ cell_start, const SceneDesc* __restrict__ scenes,
-                          const uint32_t* __restrict__ nbr_cnt, const uint32_t* __restrict__ words,
+__global__ void k_nbr_ids(const uint4* __restrict__ hdr, const uint32_t* __restrict__ words,
                           const uint32_t* __restrict__ id, const uint32_t* __restrict__ offsets,
                           uint32_t* __restrict__ ids, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  CellRows rows;
-  cell_rows_thread(skey[i], scenes[__float_as_int(pos[i].w)], cell_start, &rows);
   uint32_t o = offsets[id[i]];
-  const int cnt = static_cast<int>(nbr_cnt[i]);
-  for (int k = 0; k < cnt; ++k) {
-    const uint32_t t = entry_of(words[static_cast<size_t>(k >> 1) * n + i], k & 1);
-    ids[o++] = id[cand_slot(&rows, t)];
-  }
+  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) { ids[o++] = id[j]; });
 }
 
 // Particles::estimateDensities (particles.cpp:440-444) on cell-sorted x: self included.
@@ -912,36 +654,6 @@ cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& 
 
 }  // namespace
 
-// Threads per block -> warps per block for the cell-cooperative kernels.
-#define PBF_WARPS_SWITCH(block, ...)                                    \
-  switch (block) {                                                      \
-    case 64: { constexpr int WARPS = 2; __VA_ARGS__; } break;           \
-    case 256: { constexpr int WARPS = 8; __VA_ARGS__; } break;          \
-    case 512: { constexpr int WARPS = 16; __VA_ARGS__; } break;         \
-    default: { constexpr int WARPS = 4; __VA_ARGS__; } break;           \
-  }
-
-// One warp per 32 slots.
-inline unsigned cell_grid(int n, int warps) { return static_cast<unsigned>((n + 32 * warps - 1) / (32 * warps)); }
-
-// Dynamic shared memory above 48 KB needs an opt-in per kernel; granted once
-// per process for every instantiation at its largest launch shape.
-template <typename K>
-cudaError_t optin(K* k, int bytes) {
-  return cudaFuncSetAttribute(reinterpret_cast<const void*>(k), cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-}
-
-template <int W>
-cudaError_t optin_all() {
-  cudaError_t e = optin(k_cells_build<W>, W * kBuildWarpBytes);
-  if (e == cudaSuccess) e = optin(k_cells_lambda<W>, W * kPassWarpBytes);
-  if (e == cudaSuccess) e = optin(k_cells_deltap<W, true>, W * kPassWarpBytes);
-  if (e == cudaSuccess) e = optin(k_cells_deltap<W, false>, W * kPassWarpBytes);
-  if (e == cudaSuccess) e = optin(k_cells_xsph<W>, W * kPass2WarpBytes);
-  if (e == cudaSuccess) e = optin(k_cells_vort<W>, W * kPassWarpBytes);
-  return e;
-}
-
 #define PBF_BLOCK_SWITCH(block, ...)                          \
   switch (block) {                                            \
     case 64: { constexpr int BLOCK = 64; __VA_ARGS__; } break;   \
@@ -949,14 +661,6 @@ cudaError_t optin_all() {
     case 512: { constexpr int BLOCK = 512; __VA_ARGS__; } break; \
     default: { constexpr int BLOCK = 256; __VA_ARGS__; } break;  \
   }
-
-cudaError_t configure_kernels() {
-  cudaError_t e = optin_all<2>();
-  if (e == cudaSuccess) e = optin_all<4>();
-  if (e == cudaSuccess) e = optin_all<8>();
-  if (e == cudaSuccess) e = optin_all<16>();
-  return e;
-}
 
 cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, int cur, float dt,
                         int iters, bool keep_pred, cudaStream_t s, PhaseMarks* mk) {
@@ -969,64 +673,45 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
   cudaError_t e = sort_into_cells(b, P, t, A, dt, true, s, mk);
   if (e != cudaSuccess) return e;
   k_gather<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(
-      b.perm, b.pos[A], b.disp[0], nullptr, b.id[A], b.key, b.pos[B], b.disp[1], b.xs[0], nullptr, b.id[B],
-      b.skey, n);
+      b.perm, b.pos[A], b.disp[0], nullptr, b.id[A], b.pos[B], b.disp[1], b.xs[0], nullptr, b.id[B], n);
   if (keep_pred && b.pred) {
     e = cudaMemcpyAsync(b.pred, b.xs[0], sizeof(float4) * b.n, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return e;
   }
   if (mk) mk->mark(kPhaseGather, s);
-  {
-    PBF_WARPS_SWITCH(t.block_nbr, {
-      const int bytes = WARPS * kBuildWarpBytes;
-      k_cells_build<WARPS><<<cell_grid(n, WARPS), WARPS * 32, bytes, s>>>(
-          b.xs[0], b.pos[B], b.skey, b.cell_start, b.scenes, b.nbr_cnt, b.nbr_w, b.lam,
-          P.stats ? b.rho_iter0 : nullptr, b.err, P, n);
-    });
-  }
+  PBF_BLOCK_SWITCH(t.block_nbr,
+                   k_nbr_build<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                       b.xs[0], b.pos[B], b.cell_start, b.scenes, b.nbr_hdr, b.nbr_w, b.err, P, n));
   if (mk) mk->mark(kPhaseNeighbors, s);
   for (int it = 0; it < iters; ++it) {
     float4* xcur = b.xs[it & 1];
     float4* xnext = b.xs[(it + 1) & 1];
-    if (it > 0) {  // iteration 0's lambda comes with the neighbour build
-      PBF_WARPS_SWITCH(t.block_solve, {
-        const int bytes = WARPS * kPassWarpBytes;
-        k_cells_lambda<WARPS><<<cell_grid(n, WARPS), WARPS * 32, bytes, s>>>(
-            xcur, b.pos[B], b.skey, b.cell_start, b.scenes, b.nbr_cnt, b.nbr_w, b.lam, b.err, P, n);
-      });
-    }
+    PBF_BLOCK_SWITCH(t.block_solve,
+                     k_lambda<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                         xcur, b.nbr_hdr, b.nbr_w, b.lam, (it == 0 && P.stats) ? b.rho_iter0 : nullptr, P, n));
     if (mk) mk->mark(kPhaseLambda, s);
     if (P.scorr_n == 4) {
-      PBF_WARPS_SWITCH(t.block_solve, {
-        const int bytes = WARPS * kPassWarpBytes;
-        k_cells_deltap<WARPS, true><<<cell_grid(n, WARPS), WARPS * 32, bytes, s>>>(
-            xcur, b.pos[B], b.skey, b.cell_start, b.scenes, b.nbr_cnt, b.nbr_w, b.disp[1], xnext, b.err, P, n);
-      });
+      PBF_BLOCK_SWITCH(t.block_solve,
+                       (k_deltap<BLOCK, true><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                           xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, P, n)));
     } else {
-      PBF_WARPS_SWITCH(t.block_solve, {
-        const int bytes = WARPS * kPassWarpBytes;
-        k_cells_deltap<WARPS, false><<<cell_grid(n, WARPS), WARPS * 32, bytes, s>>>(
-            xcur, b.pos[B], b.skey, b.cell_start, b.scenes, b.nbr_cnt, b.nbr_w, b.disp[1], xnext, b.err, P, n);
-      });
+      PBF_BLOCK_SWITCH(t.block_solve,
+                       (k_deltap<BLOCK, false><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                           xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, P, n)));
     }
     if (mk) mk->mark(kPhaseDeltaP, s);
   }
   float4* fin = b.xs[iters & 1];
-  PBF_WARPS_SWITCH(t.block_solve, {
-    const int bytes = WARPS * kPass2WarpBytes;
-    k_cells_xsph<WARPS><<<cell_grid(n, WARPS), WARPS * 32, bytes, s>>>(
-        fin, b.pos[B], b.skey, b.cell_start, b.scenes, b.nbr_cnt, b.nbr_w, b.disp[1], b.vel[B], b.omega, b.rho,
-        b.err, P, 1.0f / dt, n);
-  });
+  PBF_BLOCK_SWITCH(t.block_solve,
+                   k_xsph<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                       fin, b.disp[1], b.nbr_hdr, b.nbr_w, b.vel[B], b.omega, b.rho, P, 1.0f / dt, n));
   if (mk) mk->mark(kPhaseXsph, s);
-  PBF_WARPS_SWITCH(t.block_solve, {
-    const int bytes = WARPS * kPassWarpBytes;
-    k_cells_vort<WARPS><<<cell_grid(n, WARPS), WARPS * 32, bytes, s>>>(
-        fin, b.pos[B], b.skey, b.cell_start, b.scenes, b.nbr_cnt, b.nbr_w, b.omega, b.vel[B], b.err, P, dt, n);
-  });
+  PBF_BLOCK_SWITCH(t.block_solve,
+                   k_vort<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                       fin, b.pos[B], b.omega, b.nbr_hdr, b.nbr_w, b.vel[B], b.err, P, dt, n));
   if (mk) mk->mark(kPhaseVorticity, s);
   if (P.stats)
-    k_stats<<<min(blocks_for(n, 256), 1216u), 256, 0, s>>>(b.rho, b.rho_iter0, b.nbr_cnt, b.stats, P.inv_rho0, n);
+    k_stats<<<min(blocks_for(n, 256), 1216u), 256, 0, s>>>(b.rho, b.rho_iter0, b.nbr_hdr, b.stats, P.inv_rho0, n);
   if (mk) mk->mark(kPhaseStats, s);
   return cudaGetLastError();
 }
@@ -1039,8 +724,8 @@ cudaError_t launch_resort(const Buffers& b, const DevParams& P, const Tuning& t,
   cudaError_t e = sort_into_cells(b, P, t, cur, 0.f, false, s);
   if (e != cudaSuccess) return e;
   k_gather<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(
-      b.perm, b.pos[cur], nullptr, b.vel[cur], b.id[cur], b.key, b.pos[1 - cur], nullptr, nullptr,
-      b.vel[1 - cur], b.id[1 - cur], b.skey, n);
+      b.perm, b.pos[cur], nullptr, b.vel[cur], b.id[cur], b.pos[1 - cur], nullptr, nullptr, b.vel[1 - cur],
+      b.id[1 - cur], n);
   return cudaGetLastError();
 }
 
@@ -1084,7 +769,7 @@ cudaError_t launch_cells_of(const Buffers& b, const DevParams& P, int cur, uint3
 cudaError_t launch_neighbor_counts(const Buffers& b, int cur, uint32_t* counts, cudaStream_t s) {
   const int n = static_cast<int>(b.n);
   if (n == 0) return cudaSuccess;
-  k_nbr_counts<<<blocks_for(n, 256), 256, 0, s>>>(b.nbr_cnt, b.id[cur], counts, n);
+  k_nbr_counts<<<blocks_for(n, 256), 256, 0, s>>>(b.nbr_hdr, b.id[cur], counts, n);
   return cudaGetLastError();
 }
 
@@ -1092,8 +777,7 @@ cudaError_t launch_neighbor_ids(const Buffers& b, int cur, const uint32_t* offse
                                 cudaStream_t s) {
   const int n = static_cast<int>(b.n);
   if (n == 0) return cudaSuccess;
-  k_nbr_ids<<<blocks_for(n, 256), 256, 0, s>>>(b.pos[cur], b.skey, b.cell_start, b.scenes, b.nbr_cnt, b.nbr_w,
-                                               b.id[cur], offsets, ids, n);
+  k_nbr_ids<<<blocks_for(n, 256), 256, 0, s>>>(b.nbr_hdr, b.nbr_w, b.id[cur], offsets, ids, n);
   return cudaGetLastError();
 }
 
