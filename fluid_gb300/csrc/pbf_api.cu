@@ -31,6 +31,8 @@ double poly6_ref(double r2, double h, double h2) {
 
 namespace pbf {
 
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+
 pbf_status Handle::fail(pbf_status st, const std::string& msg) {
   err = msg;
   return st;

@@ -14,6 +14,9 @@ struct DeviceGuard {
   ~DeviceGuard();
 };
 
+// Message returned by pbf_last_error(NULL) on this thread.
+void set_global_error(const std::string& msg);
+
 bool make_dev_params(const pbf_params& p, DevParams* d, double* cell_out, std::string* why);
 bool make_scene(const pbf_params& p, double cell, const float* lo, const float* hi, SceneDesc* sc,
                 std::string* why);

@@ -157,6 +157,11 @@ cudaError_t launch_neighbor_ids(const Buffers& b, int cur, const uint32_t* offse
 cudaError_t launch_neighbor_counts(const Buffers& b, int cur, uint32_t* counts, cudaStream_t s);
 cudaError_t launch_density_self(const Buffers& b, const DevParams& p, const Tuning& t, int cur,
                                 float* rho_sorted, cudaStream_t s);
+// Exclusive prefix sum of count[0, m) into start[0, m] (start[m] = total);
+// tile_sums holds exclusive_scan_tiles(m) entries of scratch.
+cudaError_t launch_exclusive_scan(const uint32_t* count, uint32_t* start, uint32_t* tile_sums, uint32_t m,
+                                  cudaStream_t s);
+uint32_t exclusive_scan_tiles(uint32_t m);
 cudaError_t launch_density_at(const Buffers& b, const DevParams& p, int cur, size_t m,
                               const float* pts, float* out, cudaStream_t s);
 

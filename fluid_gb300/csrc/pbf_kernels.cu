@@ -781,6 +781,17 @@ cudaError_t launch_neighbor_ids(const Buffers& b, int cur, const uint32_t* offse
   return cudaGetLastError();
 }
 
+cudaError_t launch_exclusive_scan(const uint32_t* count, uint32_t* start, uint32_t* tile_sums, uint32_t m,
+                                  cudaStream_t s) {
+  const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
+  k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(count, start, tile_sums, m);
+  k_scan_sums<<<1, 1024, 0, s>>>(tile_sums, tiles, start, m);
+  k_scan_add<<<tiles, kScanThreads, 0, s>>>(start, tile_sums, m);
+  return cudaGetLastError();
+}
+
+uint32_t exclusive_scan_tiles(uint32_t m) { return (m + kScanTile - 1) / kScanTile; }
+
 cudaError_t launch_density_self(const Buffers& b, const DevParams& P, const Tuning& t, int cur,
                                 float* rho_sorted, cudaStream_t s) {
   const int n = static_cast<int>(b.n);

@@ -88,6 +88,7 @@ def _declare(L):
         "pbf_reset_phase_times": (st, [P]),
         "pbf_num_phases": (ctypes.c_int, []),
         "pbf_phase_name": (ctypes.c_char_p, [ctypes.c_int]),
+        "pbf_density_noalloc": (st, [P, sz, P, P, P]),
         "pbf_size": (sz, [P]),
         "pbf_num_scenes": (ctypes.c_int, [P]),
         "pbf_last_error": (ctypes.c_char_p, [P]),
