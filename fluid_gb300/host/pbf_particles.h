@@ -1,0 +1,204 @@
+// C++ host facade with the reference's particle interface (src/particles.h:19-140),
+// backed by the GB300 step through the C ABI of include/pbf.h.
+//
+// Particles / Particle keep the reference's member names and meanings so the
+// reference's callers -- Application::load_particles (application.cpp:302-344),
+// PathTracer's m/c/g/h keys and the -d mode (pathtracer.cpp:414-479) -- drive the
+// GPU path unchanged. The classes are templates over the caller's 3-vector type V
+// (anything with x, y, z members and a V(x, y, z) constructor, e.g. the
+// reference's CGL::Vector3D) and colour type C (constructible from r, g, b, a).
+//
+//   Particles<V, C> p(rho0);              // Particles(double rest_density)
+//   p.addParticle(pos, v);                // addParticle(Vector3D, Vector3D)
+//   p.estimateDensities();                // estimateDensities()
+//   p.timeStep(dt); p.timeStep();         // timeStep(double), timeStep()
+//   p.ps[i]->getPosition() / getNewPosition() / getLatestDensityEstimate()
+//   p.ps[i]->velocity, getDensityBasedColor(), p.estimateDensityAt(pos)
+//
+// Differences, by design: the collider is the axis-aligned box of the pbf_params
+// (the reference casts rays against a BVH of scene triangles; `bvh` is kept as an
+// opaque, unused pointer); the XSPH pass is order-independent; positions,
+// velocities and densities are FP32 on the device and mirrored into V after
+// every step; Particle::neighbors stays empty (neighbour sets live on the device,
+// see pbf_get_neighbors). Errors throw std::runtime_error with pbf_last_error().
+#pragma once
+
+#include <cstdio>
+#include <iostream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "pbf.h"
+
+namespace pbf_host {
+
+struct Rgba {
+  double r, g, b, a;
+  Rgba(double r_, double g_, double b_, double a_) : r(r_), g(g_), b(b_), a(a_) {}
+};
+
+template <class V, class C>
+class Particles;
+
+template <class V, class C = Rgba>
+class Particle {
+ public:
+  V velocity;
+  std::vector<Particle*> neighbors;  // kept for source compatibility; not filled
+
+  Particle(const V& p, const V& v, double rest_density)
+      : velocity(v), position_(p), new_position_(p), density_(0.0), rest_density_(rest_density) {}
+
+  double getLatestDensityEstimate() const { return density_; }
+  const V getPosition() const { return position_; }
+  const V getNewPosition() const { return new_position_; }
+
+  // particles.h:48-52: red for dense, white at 0.8 rho0 and below.
+  C getDensityBasedColor() const {
+    const double ratio = (density_ - 0.8 * rest_density_) / (0.4 * rest_density_);
+    const double c = ratio < 0.0 ? 0.0 : (ratio > 1.0 ? 1.0 : ratio);
+    return C(1.0, 1.0 - c, 1.0 - c, 1.0);
+  }
+
+ private:
+  friend class Particles<V, C>;
+  V position_;
+  V new_position_;
+  double density_;
+  double rest_density_;
+};
+
+template <class V, class C = Rgba>
+class Particles {
+ public:
+  using ParticleT = Particle<V, C>;
+
+  std::vector<ParticleT*> ps;
+  void* bvh = nullptr;  // the reference's BVHAccel*; the GPU collider is params().box_*
+  double simulate_time = 0.0;
+  const double rest_density;
+  bool surfaceUpToTimestep = false;
+
+  explicit Particles(double rest_density_ = 1000.0, const pbf_params* params = nullptr, int device = 0)
+      : rest_density(rest_density_), device_(device) {
+    if (params) {
+      prm_ = *params;
+    } else {
+      pbf_params_default(&prm_);
+    }
+    prm_.rest_density = rest_density_;
+  }
+  Particles(const Particles&) = delete;
+  Particles& operator=(const Particles&) = delete;
+  ~Particles() {
+    if (h_) pbf_destroy(h_);
+    for (ParticleT* p : ps) delete p;
+  }
+
+  void addParticle(V pos, V v) {
+    ps.push_back(new ParticleT(pos, v, rest_density));
+    dirty_ = true;
+  }
+
+  // Particles::timeStep(double), particles.cpp:250-297.
+  void timeStep(double delta_t) {
+    if (verbose_) std::cerr << "Time: " << simulate_time;
+    simulate_time += delta_t;
+    if (verbose_) std::cerr << " => " << simulate_time << std::endl;
+    ensure_handle();
+    check(pbf_step(h_, delta_t, 1));
+    pull(true);
+    if (verbose_) {
+      pbf_stats s;
+      check(pbf_get_stats(h_, &s));
+      std::cout << "avg rho: " << s.mean_density_iter0 << " => " << s.mean_density << std::endl;
+    }
+    surfaceUpToTimestep = false;
+  }
+  // particles.cpp:299-301
+  void timeStep() { timeStep(prm_.dt); }
+
+  // particles.cpp:440-444: every particle's density at its position, self included.
+  void estimateDensities() {
+    if (ps.empty()) return;
+    ensure_handle();
+    std::vector<float> rho(ps.size());
+    check(pbf_estimate_densities(h_, rho.data()));
+    for (size_t i = 0; i < ps.size(); ++i) ps[i]->density_ = rho[i];
+  }
+
+  // particles.cpp:446-453
+  double estimateDensityAt(V pos) {
+    if (ps.empty()) return 0.0;
+    ensure_handle();
+    const float q[3] = {static_cast<float>(pos.x), static_cast<float>(pos.y), static_cast<float>(pos.z)};
+    float out = 0.f;
+    check(pbf_estimate_density_at(h_, 1, q, &out));
+    return out;
+  }
+
+  const pbf_params& params() const { return prm_; }
+  pbf_stats stats() {
+    pbf_stats s{};
+    if (h_) check(pbf_get_stats(h_, &s));
+    return s;
+  }
+  // print the reference's per-step progress lines (particles.cpp:251-253, 267, 279, 295)
+  void set_verbose(bool v) { verbose_ = v; }
+  pbf_handle* handle() { return h_; }
+
+ private:
+  pbf_params prm_{};
+  pbf_handle* h_ = nullptr;
+  bool dirty_ = true;
+  bool verbose_ = false;
+  int device_ = 0;
+
+  void check(pbf_status st) const {
+    if (st != PBF_OK) throw std::runtime_error(std::string("pbf: ") + pbf_last_error(h_));
+  }
+
+  // (Re)create the device simulator from the mirrors when particles were added.
+  void ensure_handle() {
+    if (h_ && !dirty_) return;
+    if (h_) {
+      pbf_destroy(h_);
+      h_ = nullptr;
+    }
+    std::vector<float> x(3 * ps.size()), v(3 * ps.size());
+    for (size_t i = 0; i < ps.size(); ++i) {
+      const V& p = ps[i]->position_;
+      const V& u = ps[i]->velocity;
+      x[3 * i] = static_cast<float>(p.x);
+      x[3 * i + 1] = static_cast<float>(p.y);
+      x[3 * i + 2] = static_cast<float>(p.z);
+      v[3 * i] = static_cast<float>(u.x);
+      v[3 * i + 1] = static_cast<float>(u.y);
+      v[3 * i + 2] = static_cast<float>(u.z);
+    }
+    pbf_handle* h = nullptr;
+    const pbf_status st = pbf_create(&prm_, ps.size(), x.data(), v.data(), device_, &h);
+    if (st != PBF_OK) throw std::runtime_error(std::string("pbf_create: ") + pbf_last_error(nullptr));
+    h_ = h;
+    dirty_ = false;
+  }
+
+  // Mirror device state into the Particle objects (original order).
+  void pull(bool with_density) {
+    const size_t n = ps.size();
+    std::vector<float> x(3 * n), v(3 * n), rho(with_density ? n : 0);
+    check(pbf_get_positions(h_, x.data()));
+    check(pbf_get_velocities(h_, v.data()));
+    if (with_density) check(pbf_get_densities(h_, rho.data()));
+    for (size_t i = 0; i < n; ++i) {
+      ParticleT* p = ps[i];
+      p->position_ = V(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+      p->new_position_ = p->position_;
+      p->velocity = V(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+      if (with_density) p->density_ = rho[i];
+    }
+  }
+};
+
+}  // namespace pbf_host

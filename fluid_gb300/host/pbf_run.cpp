@@ -1,0 +1,176 @@
+// pbf_run: headless driver for the GPU PBF step with the reference's key semantics.
+//
+// The reference drives its simulator from GLFW key presses (PathTracer::key_press,
+// src/pathtracer.cpp:414-433) and from the windowless -d mode (src/main.cpp:159-170,
+// Application::fluid_simulate_render_to_file). There is no window here, so the keys
+// become command-line actions on the same Particles interface:
+//
+//   m  one step                                  (fluid_simulate_time_step, :464-469)
+//   c  steps until one second has passed          (fluid_simulate_time(1), :444-462)
+//   g  as c, dumping every frame                  (the reference saves a screenshot)
+//   h  as c, dumping every frame                  (the reference path-traces a PNG;
+//                                                  rendering is not part of this build)
+//   -d T  simulate T seconds, dumping every frame (the -d windowless mode)
+//
+// A frame dump is <dir>/frame_NNNNNN.bin: "PBFFRAME", int64 n, float64 time,
+// float32 positions (n, 3), float32 densities (n).
+#include <cerrno>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <iostream>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+#include "pbf.h"
+#include "pbf_particles.h"
+#include "pbf_xml.h"
+
+namespace {
+
+struct Vec3 {
+  double x = 0, y = 0, z = 0;
+  Vec3() = default;
+  Vec3(double a, double b, double c) : x(a), y(b), z(c) {}
+};
+
+using Sim = pbf_host::Particles<Vec3>;
+
+struct Options {
+  std::string file;
+  std::string keys;
+  double seconds = -1.0;
+  std::string out = "pbf_out";
+  bool parse_only = false;
+  bool quiet = false;
+  bool graph = false;
+};
+
+void usage() {
+  std::fprintf(stderr,
+               "usage: pbf_run -p particles.xml [-k keys] [-d seconds] [-o dir] [--graph] [--quiet]\n"
+               "       pbf_run -p particles.xml --parse-only\n"
+               "  keys: m = one step, c = one second, g / h = one second with a frame dump per step\n");
+}
+
+int frame_no = 0;
+
+bool dump(Sim& sim, const std::string& dir) {
+  char name[64];
+  std::snprintf(name, sizeof(name), "/frame_%06d.bin", frame_no++);
+  std::FILE* f = std::fopen((dir + name).c_str(), "wb");
+  if (!f) return false;
+  const int64_t n = static_cast<int64_t>(sim.ps.size());
+  std::fwrite("PBFFRAME", 1, 8, f);
+  std::fwrite(&n, sizeof(n), 1, f);
+  std::fwrite(&sim.simulate_time, sizeof(double), 1, f);
+  std::vector<float> x(3 * n), rho(n);
+  for (int64_t i = 0; i < n; ++i) {
+    const Vec3 p = sim.ps[i]->getPosition();
+    x[3 * i] = static_cast<float>(p.x);
+    x[3 * i + 1] = static_cast<float>(p.y);
+    x[3 * i + 2] = static_cast<float>(p.z);
+    rho[i] = static_cast<float>(sim.ps[i]->getLatestDensityEstimate());
+  }
+  std::fwrite(x.data(), sizeof(float), x.size(), f);
+  std::fwrite(rho.data(), sizeof(float), rho.size(), f);
+  return std::fclose(f) == 0;
+}
+
+// PathTracer::fluid_simulate_time: step until `delta` seconds have passed.
+bool simulate_time(Sim& sim, double delta, bool dump_frames, const std::string& dir) {
+  const double start = sim.simulate_time;
+  if (dump_frames && !dump(sim, dir)) return false;
+  while (sim.simulate_time < start + delta) {
+    sim.timeStep();
+    if (dump_frames && !dump(sim, dir)) return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  Options o;
+  for (int i = 1; i < argc; ++i) {
+    const std::string a = argv[i];
+    auto next = [&]() -> std::string {
+      if (i + 1 >= argc) {
+        usage();
+        std::exit(2);
+      }
+      return argv[++i];
+    };
+    if (a == "-p") o.file = next();
+    else if (a == "-k") o.keys += next();
+    else if (a == "-d") o.seconds = std::atof(next().c_str());
+    else if (a == "-o") o.out = next();
+    else if (a == "--parse-only") o.parse_only = true;
+    else if (a == "--quiet") o.quiet = true;
+    else if (a == "--graph") o.graph = true;
+    else {
+      usage();
+      return 2;
+    }
+  }
+  pbf_host::ParticleFile pf;
+  std::string msg;
+  const pbf_host::LoadStatus st = pbf_host::load_particle_file(o.file, &pf, &msg);
+  if (st == pbf_host::LoadStatus::missing) {
+    // application.cpp:303-308 warns and continues with an empty Particles()
+    std::cout << "[Warning] Particle file not passed in or not found\n";
+  } else if (st != pbf_host::LoadStatus::ok) {
+    std::cout << "[ERROR] " << msg << std::endl;  // application.cpp:311-317 exits on XML errors
+    return EXIT_FAILURE;
+  }
+  if (o.parse_only) {
+    std::printf("particles %zu rest_density %.9g h %.9g iters %d dt %.9g params %s\n", pf.size(), pf.rest_density,
+                pf.params.h, pf.params.iters, pf.params.dt, pf.has_params ? "file" : "default");
+    return 0;
+  }
+  pbf_params prm = pf.params;
+  if (o.graph) prm.flags |= PBF_FLAG_GRAPH;
+  try {
+    Sim sim(pf.rest_density, &prm);
+    sim.set_verbose(!o.quiet);
+    for (size_t i = 0; i < pf.size(); ++i) {
+      sim.addParticle(Vec3(pf.pos[3 * i], pf.pos[3 * i + 1], pf.pos[3 * i + 2]),
+                      Vec3(pf.vel[3 * i], pf.vel[3 * i + 1], pf.vel[3 * i + 2]));
+    }
+    sim.estimateDensities();  // application.cpp:342
+    const bool needs_dir = o.seconds >= 0 || o.keys.find_first_of("gGhH") != std::string::npos;
+    if (needs_dir && mkdir(o.out.c_str(), 0755) != 0 && errno != EEXIST) {
+      std::cerr << "cannot create " << o.out << "\n";
+      return EXIT_FAILURE;
+    }
+    for (char k : o.keys) {
+      switch (k) {
+        case 'm': case 'M':
+          sim.timeStep();
+          std::cout << "[Fluid Simulation] Fluid particles updated.\n";
+          break;
+        case 'c': case 'C':
+          simulate_time(sim, 1.0, false, o.out);
+          std::cout << "[Fluid Simulation] Fluid particles updated.\n";
+          break;
+        case 'g': case 'G': case 'h': case 'H':
+          if (!simulate_time(sim, 1.0, true, o.out)) return EXIT_FAILURE;
+          std::cout << "[Fluid Simulation] Fluid particles updated, frames saved.\n";
+          break;
+        default:
+          std::cerr << "unknown key '" << k << "'\n";
+          return 2;
+      }
+    }
+    if (o.seconds >= 0 && !simulate_time(sim, o.seconds, true, o.out)) return EXIT_FAILURE;
+    if (o.keys.empty() && o.seconds < 0 && !dump(sim, o.out.empty() ? "." : o.out)) {
+      // nothing requested: write the loaded state for inspection
+    }
+  } catch (const std::exception& e) {
+    std::cerr << e.what() << "\n";
+    return EXIT_FAILURE;
+  }
+  return 0;
+}

@@ -235,12 +235,13 @@ def write_xml(path, pos: np.ndarray, vel: np.ndarray, rest_density: float, param
         pe = ET.SubElement(root, "params")
         for key in ("h", "h2", "iters", "scorr_n", "epsilon", "scorr_k", "scorr_dq",
                     "vort_eps", "xsph_c", "dt"):
-            ET.SubElement(pe, key).text = repr(getattr(params, key))
+            ET.SubElement(pe, key).text = repr(float(getattr(params, key))) if key != "iters" and key != "scorr_n" \
+                else str(int(getattr(params, key)))
         ET.SubElement(pe, "gravity").text = " ".join(repr(float(x)) for x in params.gravity)
         ET.SubElement(pe, "box_lo").text = " ".join(repr(float(x)) for x in params.box_lo)
         ET.SubElement(pe, "box_hi").text = " ".join(repr(float(x)) for x in params.box_hi)
     ps = ET.SubElement(root, "ps")
-    for p, v in zip(pos, vel):
+    for p, v in zip(np.asarray(pos, dtype=np.float64).tolist(), np.asarray(vel, dtype=np.float64).tolist()):
         pe = ET.SubElement(ps, "particle")
         ET.SubElement(pe, "pos").text = f"{p[0]!r} {p[1]!r} {p[2]!r}"
         ET.SubElement(pe, "v").text = f"{v[0]!r} {v[1]!r} {v[2]!r}"
