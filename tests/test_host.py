@@ -39,7 +39,7 @@ def test_reference_format_round_trip(pbf_run, tmp_path):
     assert rc == 0, out
     fields = out.split()
     assert fields[1] == "4096"
-    assert float(fields[3]) == float(np.float32(sc.params.rest_density))  # stof, application.cpp:331
+    assert float(fields[3]) == pytest.approx(float(np.float32(sc.params.rest_density)), rel=1e-8)  # stof
     assert float(fields[5]) == pytest.approx(sc.params.h) and fields[7] == "4"
     assert fields[-1] == "file"
 
