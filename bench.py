@@ -49,7 +49,8 @@ ALGO_BYTES = {"predict": 64 + 24, "sort": 104, "gather": 0, "lambda": 20, "delta
               "xsph": 84, "vorticity": 64, "neighbors": 16, "scan": 0, "stats": 0}
 # DRAM bytes per particle per launch measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum) on the 1M colliding-blocks scene; see profiles/.
-NCU_TRAFFIC_PER_PARTICLE: dict[str, float] = {}
+# Source: profiles/k_deltap_k_lambda_k_nbr_build_colliding_blocks_1m.md.
+NCU_TRAFFIC_PER_PARTICLE: dict[str, float] = {"deltap": 142.2, "lambda": 100.1, "neighbors": 62.6}
 
 
 def peaks():
