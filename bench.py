@@ -220,6 +220,76 @@ def barrier(world):
         dist.barrier()
 
 
+def bench_batched(args, local, steps: int = 10, warmup: int = 3) -> dict:
+    """256 independent scenes of 2k-32k particles: one batched handle (one launch per
+    phase over every scene, the step replayed as a CUDA graph, launch shapes from the
+    autotuner) against the same scenes stepped one at a time, each with its own graph.
+    Both time device work with CUDA events per step; every step starts from the scenes'
+    configured state (snapshot restored between steps, untimed)."""
+    import torch
+
+    from fluid_gb300 import pbf, scenes
+    from fluid_gb300.params import PBF_FLAG_GRAPH
+
+    b = scenes.batched_256()
+    prm = b.params.with_(flags=PBF_FLAG_GRAPH)
+    dt = prm.dt
+    sim = pbf.Simulator(b.pos, b.vel, prm, device=local, counts=b.counts, boxes=b.boxes)
+    sim.sort()
+    sim.snapshot()
+    tuning = sim.autotune(dt, reps=2)
+    stream = torch.cuda.ExternalStream(sim.stream)
+    for _ in range(warmup):
+        sim.restore()
+        sim.step_async(dt, 1)
+    sim.sync()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        sim.restore()
+        ev[k][0].record(stream)
+        sim.step_async(dt, 1)
+        ev[k][1].record(stream)
+    sim.sync()
+    batched_s = sum(a.elapsed_time(z) for a, z in ev) / 1e3
+    n_total = sim.n
+    sim.close()
+
+    singles = []
+    off = 0
+    for c in b.counts:
+        s1 = pbf.Simulator(b.pos[off:off + c], b.vel[off:off + c], prm, device=local)
+        s1.set_tuning(**tuning)
+        s1.sort()
+        s1.snapshot()
+        singles.append(s1)
+        off += c
+    for s1 in singles:  # warm each graph
+        for _ in range(2):
+            s1.restore()
+            s1.step_async(dt, 1)
+        s1.sync()
+    single_s = 0.0
+    for _ in range(steps):
+        for s1 in singles:
+            st = torch.cuda.ExternalStream(s1.stream)
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s1.restore()
+            a.record(st)
+            s1.step_async(dt, 1)
+            z.record(st)
+            s1.sync()
+            single_s += a.elapsed_time(z) / 1e3
+    for s1 in singles:
+        s1.close()
+    v_b = n_total * steps / batched_s
+    v_1 = n_total * steps / single_s
+    return {"workload": "batched_256", "scenes": len(b.counts), "particles": int(n_total),
+            "counts_min_max": [min(b.counts), max(b.counts)], "steps": steps,
+            "value": v_b, "one_at_a_time": v_1, "speedup": v_b / v_1, "unit": UNIT,
+            "ms_per_step": batched_s / steps * 1e3, "one_at_a_time_ms_per_step": single_s / steps * 1e3,
+            "graph": True, "tuning": tuning}
+
+
 def bench_reference(args, scene, world, rank):
     if rank != 0:
         return 0
@@ -376,6 +446,8 @@ def bench_ours(args, scene, world, rank, local):
     }
     if e2e:
         line["e2e"] = e2e
+    if not args.no_batched:
+        line["batched"] = bench_batched(args, local)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
         line["cpu_port_all_cores"] = cpu_port_all_cores(scene, min(args.cpu_seconds, 10.0))
@@ -395,6 +467,7 @@ def main(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
