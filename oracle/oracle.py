@@ -20,6 +20,8 @@ ROOT = HERE.parent
 SRC = HERE / "pbf_oracle.c"
 LIB = HERE / "_build" / "libpbf_oracle.so"
 LIB32 = HERE / "_build" / "libpbf_oracle_fp32.so"
+SRC_ADJ = HERE / "pbf_oracle_adj.c"
+LIB_ADJ = HERE / "_build" / "libpbf_oracle_adj.so"
 
 if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
@@ -28,13 +30,15 @@ from fluid_gb300.params import PbfParams  # noqa: E402
 
 
 def build(force: bool = False) -> Path:
-    """Build the FP64 restatement and its FP32 twin (same source, -DORC_FLOAT)."""
+    """Build the FP64 restatement, its FP32 twin (same source, -DORC_FLOAT) and the
+    FP64 reference gradient (pbf_oracle_adj.c, which includes the restatement)."""
     LIB.parent.mkdir(parents=True, exist_ok=True)
-    for out, extra in ((LIB, []), (LIB32, ["-DORC_FLOAT"])):
-        if not force and out.exists() and out.stat().st_mtime >= SRC.stat().st_mtime:
+    for out, src, extra in ((LIB, SRC, []), (LIB32, SRC, ["-DORC_FLOAT"]), (LIB_ADJ, SRC_ADJ, [])):
+        newest = max(SRC.stat().st_mtime, src.stat().st_mtime)
+        if not force and out.exists() and out.stat().st_mtime >= newest:
             continue
         cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
-               "-fPIC", "-shared", "-Wall", *extra, "-o", str(out), str(SRC), "-lm"]
+               "-fPIC", "-shared", "-Wall", *extra, "-o", str(out), str(src), "-lm"]
         subprocess.run(cmd, check=True)
     return LIB
 
@@ -42,13 +46,17 @@ def build(force: bool = False) -> Path:
 _libs = {}
 
 
-def lib(fp32: bool = False):
-    path = LIB32 if fp32 else LIB
+def lib(fp32: bool = False, adjoint: bool = False):
+    path = LIB_ADJ if adjoint else (LIB32 if fp32 else LIB)
     if path not in _libs:
         if not path.exists():
             build()
         L = ctypes.CDLL(str(path))
         P = ctypes.c_void_p
+        if adjoint:
+            L.orc_step_adjoint.argtypes = [P, ctypes.c_int64, P, P, ctypes.c_double, P, P, P, P, P, P, P,
+                                           P, P, P, ctypes.c_int]
+            L.orc_step_adjoint.restype = ctypes.c_int
         L.orc_step.argtypes = [P, ctypes.c_int64, P, P, P, ctypes.c_int, ctypes.c_double,
                                P, P, ctypes.c_int64, P, P, ctypes.c_int]
         L.orc_step.restype = ctypes.c_int
@@ -138,6 +146,59 @@ def estimate_density_at(pos, pts, params: PbfParams, threads: int = 0) -> np.nda
     if rc:
         raise RuntimeError(f"orc_estimate_density_at failed: {rc}")
     return out
+
+
+def step_adjoint(pos, vel, params: PbfParams, gx, gv, dt: float | None = None,
+                 given_neighbors=None, threads: int = 0) -> dict:
+    """One FP64 step and its reverse mode (oracle/pbf_oracle_adj.c).
+
+    ``gx``/``gv``: adjoints of the step's output positions / velocities. Returns the
+    adjoints of the inputs (``gx``, ``gv``, ``grho0``) and the step's outputs
+    (``pos``, ``vel``) and ``kinds``, the census of collision kinds (not moved, free,
+    stop, stop + slide, stop + slide + stop) of the prediction (0-4) and of the Jacobi
+    iterations (5-9). ``given_neighbors=(offsets, ids)`` fixes the neighbour sets.
+    """
+    L = lib(adjoint=True)
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+    pos, vel, gx, gv = f64(pos), f64(vel), f64(gx), f64(gv)
+    n = pos.shape[0]
+    out = {k: np.zeros((n, 3), dtype=np.float64) for k in ("gx", "gv", "pos", "vel")}
+    g0 = ctypes.c_double(0.0)
+    kinds = np.zeros(10, dtype=np.int64)
+    g_off = g_idx = None
+    if given_neighbors is not None:
+        g_off = np.ascontiguousarray(given_neighbors[0], dtype=np.int64)
+        g_idx = np.ascontiguousarray(given_neighbors[1], dtype=np.int64)
+        if g_idx.size == 0:
+            g_idx = np.zeros(1, dtype=np.int64)
+    cp = params.to_c()
+    rc = L.orc_step_adjoint(ctypes.byref(cp), n, _ptr(pos), _ptr(vel), params.dt if dt is None else dt,
+                            _ptr(g_off), _ptr(g_idx), _ptr(gx), _ptr(gv), _ptr(out["gx"]), _ptr(out["gv"]),
+                            ctypes.byref(g0), _ptr(out["pos"]), _ptr(out["vel"]), _ptr(kinds), threads)
+    if rc:
+        raise RuntimeError(f"orc_step_adjoint failed: {rc}")
+    out["grho0"] = g0.value
+    out["kinds"] = kinds
+    return out
+
+
+def rollout_adjoint(pos, vel, params: PbfParams, steps: int, gx, gv, dt: float | None = None,
+                    threads: int = 0) -> dict:
+    """Reverse mode of ``steps`` FP64 steps: checkpoints (x, v) per step on the way
+    forward, recomputes each step's forward inside its reverse call (neighbour sets
+    searched again from the checkpoint, as in the forward)."""
+    xs, vs = [np.array(pos, dtype=np.float64)], [np.array(vel, dtype=np.float64)]
+    for _ in range(steps):
+        o = step(xs[-1], vs[-1], params, 1, dt=dt, threads=threads)
+        xs.append(o["pos"])
+        vs.append(o["vel"])
+    gx = np.array(gx, dtype=np.float64)
+    gv = np.array(gv, dtype=np.float64)
+    g0 = 0.0
+    for s in range(steps - 1, -1, -1):
+        a = step_adjoint(xs[s], vs[s], params, gx, gv, dt=dt, threads=threads)
+        gx, gv, g0 = a["gx"], a["gv"], g0 + a["grho0"]
+    return {"gx": gx, "gv": gv, "grho0": g0, "pos": xs[-1], "vel": vs[-1]}
 
 
 def max_threads() -> int:

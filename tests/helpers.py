@@ -85,3 +85,46 @@ def neighbor_sets_fp32(xs32, h2):
 
 def csr_sets(off, idx):
     return [set(idx[off[i]:off[i + 1]].tolist()) for i in range(len(off) - 1)]
+
+
+# ---------------------------------------------------------------------------
+# small scenes for the adjoint checks (h = 0.05, s = 0.025, [0,1]^3 box)
+# ---------------------------------------------------------------------------
+
+def adjoint_fall_scene(m: int = 6, seed: int = 7):
+    """m^3 jittered lattice on the floor with random velocities and a downward push:
+    floor stops in the prediction and in the Jacobi iterations."""
+    from fluid_gb300.scenes import lattice, physical_params, uniform
+
+    s = 0.025
+    p = lattice(m, m, m, s, corner=(0.4, 0.0, 0.4))
+    p += uniform(seed, p.size, -0.2 * s, 0.2 * s).reshape(p.shape)
+    v = uniform(seed, p.size, -0.3, 0.3, stream=1).reshape(p.shape)
+    v[:, 1] -= 0.5
+    return p, v, physical_params(0.05, s)
+
+
+def adjoint_corner_scene(seed: int = 3):
+    """5^3 lattice in the x = 0, y = 0 corner moving into it with a z component:
+    wall stops, slides along a wall and second stops on the other wall."""
+    from fluid_gb300.scenes import lattice, physical_params, uniform
+
+    s = 0.025
+    p = lattice(5, 5, 5, s, corner=(0.0, 0.0, 0.3))
+    p += uniform(seed, p.size, -0.2 * s, 0.2 * s).reshape(p.shape)
+    p = np.clip(p, 0.002, None)
+    v = np.tile([-1.5, -1.5, 0.8], (p.shape[0], 1)) + uniform(seed + 1, p.size, -0.2, 0.2).reshape(p.shape)
+    return p, v, physical_params(0.05, s)
+
+
+def adjoint_free_scene(m: int = 8, seed: int = 5):
+    """m^3 jittered lattice at rest, far from every wall (a [0,3]^3 box without clip
+    planes): no collision for several steps, so the rollout is a smooth map."""
+    from fluid_gb300.scenes import lattice, physical_params, uniform
+
+    s = 0.025
+    p = lattice(m, m, m, s, corner=(1.0, 2.0, 1.0))
+    p += uniform(seed, p.size, -0.008 * s, 0.008 * s).reshape(p.shape)
+    prm = physical_params(0.05, s, box_lo=(0.0, 0.0, 0.0), box_hi=(3.0, 3.0, 3.0), clip_planes=(),
+                          clamp_lo=(0.0, 0.0, 0.0), clamp_hi=(3.0, 3.0, 3.0))
+    return p, np.zeros_like(p), prm

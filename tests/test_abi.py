@@ -45,7 +45,7 @@ def test_every_declared_symbol_is_exported(libpbf):
 
 
 def test_abi_version(libpbf):
-    assert libpbf.pbf_abi_version() == 1
+    assert libpbf.pbf_abi_version() == 2
 
 
 def test_default_params_are_the_reference_constants(libpbf):
