@@ -158,6 +158,7 @@ void Handle::free_all() {
   for (void* q : ptrs)
     if (q) cudaFree(q);
   b = Buffers();
+  free_tape();
   snap_pos = snap_vel = nullptr;
   snap_id = nullptr;
   snap_valid = false;
@@ -197,6 +198,42 @@ pbf_status Handle::alloc_all() {
     if (st != PBF_OK) return st;
   }
   return cuda(cudaMemsetAsync(b.err, 0, sizeof(unsigned), stream), "cudaMemsetAsync");
+}
+
+void Handle::free_tape() {
+  void* ptrs[] = {tape.x, tape.v, tape.xs, tape.dp, tape.gxs, tape.pl[0], tape.pl[1], tape.gr,
+                  tape.gvo, tape.gx, tape.wb, tape.eb, tape.r0, tape.r0_part};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  tape = Tape();
+}
+
+pbf_status Handle::ensure_tape() {
+  if (tape.x && tape.n == b.n && tape.iters == params.iters) return PBF_OK;
+  free_tape();
+  const size_t n = b.n ? b.n : 1;
+  const size_t f4 = sizeof(float4) * n;
+  const size_t it = static_cast<size_t>(params.iters);
+  struct A {
+    void** p;
+    size_t bytes;
+  } list[] = {
+      {(void**)&tape.x, f4}, {(void**)&tape.v, f4}, {(void**)&tape.xs, f4 * (it + 1)},
+      {(void**)&tape.dp, f4 * (it ? it : 1)}, {(void**)&tape.gxs, f4}, {(void**)&tape.pl[0], f4},
+      {(void**)&tape.pl[1], f4}, {(void**)&tape.gr, f4}, {(void**)&tape.gvo, f4}, {(void**)&tape.gx, f4},
+      {(void**)&tape.wb, f4}, {(void**)&tape.eb, f4}, {(void**)&tape.r0, sizeof(float) * n},
+      {(void**)&tape.r0_part, sizeof(double) * kAdjReduceBlocks},
+  };
+  for (auto& a : list) {
+    pbf_status st = cuda(cudaMalloc(a.p, a.bytes), "cudaMalloc(adjoint)");
+    if (st != PBF_OK) {
+      free_tape();
+      return st;
+    }
+  }
+  tape.n = b.n;
+  tape.iters = params.iters;
+  return PBF_OK;
 }
 
 pbf_status Handle::ensure_scratch(size_t bytes) {
@@ -510,6 +547,42 @@ pbf_status pbf_sync(pbf_handle* hh) {
 
 void* pbf_stream(pbf_handle* hh) {
   return hh ? reinterpret_cast<void*>(reinterpret_cast<Handle*>(hh)->stream) : nullptr;
+}
+
+pbf_status pbf_adjoint_step_device(pbf_handle* hh, double dt, const float* xyz, const float* vel,
+                                   const float* gx_out, const float* gv_out, float* gx_in, float* gv_in,
+                                   double* g_rho0, float* xyz_out, float* vel_out, void* stream) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  const double d = dt > 0 ? dt : h->params.dt;
+  if (!(d > 0) || !std::isfinite(d)) return h->fail(PBF_ERR_INVALID, "dt must be positive");
+  if (!g_rho0) return h->fail(PBF_ERR_INVALID, "g_rho0 is NULL");
+  if (h->b.n && (!gx_in || !gv_in)) return h->fail(PBF_ERR_INVALID, "gx_in / gv_in is NULL");
+  pbf::DeviceGuard g(h->device);
+  pbf_status st = h->ensure_tape();
+  if (st != PBF_OK) return st;
+  st = h->join_from(static_cast<cudaStream_t>(stream));
+  if (st != PBF_OK) return st;
+  if (xyz) {
+    st = h->cuda(pbf::launch_upload(h->b, h->cur, xyz, vel, nullptr, h->stream), "upload");
+    if (st != PBF_OK) return st;
+  }
+  const float df = static_cast<float>(d);
+  st = h->cuda(pbf::launch_step(h->b, h->dp, h->tune, h->cur, df, h->params.iters, false, h->stream, nullptr,
+                                &h->tape),
+               "recording step");
+  if (st != PBF_OK) return st;
+  st = h->cuda(pbf::launch_adjoint(h->b, h->dp, h->tune, h->cur, df, h->tape, gx_out, gv_out, gx_in, gv_in,
+                                   g_rho0, h->stream),
+               "adjoint");
+  if (st != PBF_OK) return st;
+  h->cur ^= 1;
+  h->nbr_valid = true;
+  if (xyz_out || vel_out) {
+    st = h->cuda(pbf::launch_download(h->b, h->cur, xyz_out, vel_out, nullptr, h->stream), "download");
+    if (st != PBF_OK) return st;
+  }
+  return h->join_to(static_cast<cudaStream_t>(stream));
 }
 
 static pbf_status download(Handle* h, float* xyz, float* vel, float* rho) {

@@ -85,32 +85,72 @@ __device__ __forceinline__ float wall_value(const SceneDesc& sc, int wall) {
   return (wall & 1) ? sc.hi[wall >> 1] : sc.lo[wall >> 1];
 }
 
+// applyForceVelocity (particles.cpp:180, v += g dt) and the predicted move v dt.
+__device__ __forceinline__ float3 predict_delta(const float4& v4, const DevParams& P, float dt) {
+  const float3 v = make_float3(v4.x + P.g[0] * dt, v4.y + P.g[1] * dt, v4.z + P.g[2] * dt);
+  return v * dt;
+}
+
+// Collision record (written by the recording forward of the adjoint): the branch
+// collide() took, enough to apply its reverse with the active set fixed.
+//   bits 0-2  kind: 0 no move (|delta| <= EPS_D), 1 free, 2 stop, 3 stop + slide,
+//             4 stop + slide + second stop
+//   bit 3     the stop is a clip plane (else a wall)
+//   bits 4-6  wall index (2 axis + side) or clip plane index of the stop
+//   bit 7     the stop distance was clamped to 0 (the point was already past the wall)
+//   bits 8-10 wall index of the second stop
+//   bit 11    the second stop distance was clamped to 0
+//   bits 12-14 coordinates pinned by the clamp box
+constexpr uint32_t kCollNone = 0u, kCollFree = 1u, kCollStop = 2u, kCollSlide = 3u, kCollSlideStop = 4u;
+constexpr uint32_t kCollClipBit = 1u << 3, kCollTau0Bit = 1u << 7, kCollTau2Bit = 1u << 11;
+__device__ __forceinline__ uint32_t coll_kind(uint32_t c) { return c & 7u; }
+__device__ __forceinline__ uint32_t coll_index(uint32_t c) { return (c >> 4) & 7u; }
+__device__ __forceinline__ uint32_t coll_wall2(uint32_t c) { return (c >> 8) & 7u; }
+__device__ __forceinline__ uint32_t coll_clamped(uint32_t c) { return (c >> 12) & 7u; }
+
 // Move x* = x + d by `delta` against the collider, in displacement form: d is
 // updated, x is fixed. Follows clamp (slide = false, particles.cpp:51-84) and
 // clamp_response (slide = true, particles.cpp:87-132): clip planes first, the
 // nearest wall stops the move (the stopped coordinate is placed exactly on
 // the wall), the predict move slides once along the wall for half the
 // remaining length unless a clip plane was crossed, then the clamp box.
+// REC additionally writes the collision record to *code (same arithmetic).
+template <bool REC = false>
 __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 delta, bool slide,
-                                        const SceneDesc& sc, const DevParams& P) {
+                                        const SceneDesc& sc, const DevParams& P, uint32_t* code = nullptr) {
   const float3 p = x + d;
   float l = sqrtf(delta.x * delta.x + delta.y * delta.y + delta.z * delta.z);
-  if (!(l > kEps)) return;  // particles.cpp:53-55 / 90-92: no move, no clamp
+  if (!(l > kEps)) {  // particles.cpp:53-55 / 90-92: no move, no clamp
+    if (REC) *code = kCollNone;
+    return;
+  }
   const float3 dir = delta * (1.0f / l);
   const float total = l;
   bool intersect = false;
+  int clip = 0;
   for (int c = 0; c < P.n_clip; ++c) {
     const int a = P.clip_axis[c];
     const float da = cmp3(dir, a);
     if (da != 0.0f) {
       const float pt = (P.clip_value[c] - cmp3(p, a)) / da;
-      if (pt > 0.0f && pt < l) { l = pt; intersect = true; }
+      if (pt > 0.0f && pt < l) { l = pt; intersect = true; clip = c; }
     }
   }
+  uint32_t rc = kCollFree;
   int wall;
   const float t = wall_hit(p, dir, l, sc, P.open_mask, &wall);
   if (wall >= 0 || intersect) {
     float3 nd = d + dir * t;
+    if (REC) {
+      rc = kCollStop;
+      if (wall >= 0) {
+        const int a = wall >> 1;
+        rc |= static_cast<uint32_t>(wall) << 4;
+        if ((wall_value(sc, wall) - cmp3(p, a)) / cmp3(dir, a) < 0.0f) rc |= kCollTau0Bit;
+      } else {
+        rc |= kCollClipBit | (static_cast<uint32_t>(clip) << 4);
+      }
+    }
     if (wall >= 0) set3(nd, wall >> 1, wall_value(sc, wall) - cmp3(x, wall >> 1));
     if (slide && wall >= 0 && !intersect) {
       const int a = wall >> 1;
@@ -123,8 +163,17 @@ __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 
           const float3 dir2 = tan * (1.0f / tl);
           const float l2 = (total - t) * 0.5f;
           int wall2;
-          const float t2 = wall_hit(x + nd, dir2, l2, sc, P.open_mask, &wall2);
+          const float3 p1 = x + nd;
+          const float t2 = wall_hit(p1, dir2, l2, sc, P.open_mask, &wall2);
           nd = nd + dir2 * t2;
+          if (REC) {
+            rc = (rc & ~7u) | kCollSlide;
+            if (wall2 >= 0) {
+              const int a2 = wall2 >> 1;
+              rc = (rc & ~7u) | kCollSlideStop | (static_cast<uint32_t>(wall2) << 8);
+              if ((wall_value(sc, wall2) - cmp3(p1, a2)) / cmp3(dir2, a2) < 0.0f) rc |= kCollTau2Bit;
+            }
+          }
           if (wall2 >= 0) set3(nd, wall2 >> 1, wall_value(sc, wall2) - cmp3(x, wall2 >> 1));
         }
       }
@@ -137,9 +186,106 @@ __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const float qa = cmp3(q, a);
-    if (qa < P.clamp_lo[a]) set3(d, a, P.clamp_lo[a] - cmp3(x, a));
-    else if (qa > P.clamp_hi[a]) set3(d, a, P.clamp_hi[a] - cmp3(x, a));
+    if (qa < P.clamp_lo[a]) {
+      set3(d, a, P.clamp_lo[a] - cmp3(x, a));
+      if (REC) rc |= 1u << (12 + a);
+    } else if (qa > P.clamp_hi[a]) {
+      set3(d, a, P.clamp_hi[a] - cmp3(x, a));
+      if (REC) rc |= 1u << (12 + a);
+    }
   }
+  if (REC) *code = rc;
+}
+
+// Reverse of a recorded collision with its active set fixed. p = x* before the move,
+// D = the requested displacement, g = adjoint of x* after the move; returns the
+// adjoints of p (*pb) and of D (*db). A stop moves p to p1 = p + tau D with
+// tau = (c - p[a]) / D[a] (p1[a] = c); tau is 0 when the stop distance was clamped.
+// The slide adds kappa tan, tan = D without its a component, T = |tan|,
+// kappa = |D| (1 - tau) / (2 T); a second stop on axis a2 at c2 instead adds sigma tan
+// with sigma = (c2 - p1[a2]) / tan[a2] and puts p2[a2] = c2. Coordinates the clamp
+// box pinned pass no adjoint.
+__device__ __forceinline__ void collide_reverse(uint32_t code, const float3 p, const float3 D, float3 g,
+                                                const SceneDesc& sc, const DevParams& P, float3* pb,
+                                                float3* db) {
+  const uint32_t cl = coll_clamped(code);
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    if (cl & (1u << a)) set3(g, a, 0.0f);
+  const uint32_t kind = coll_kind(code);
+  if (kind == kCollNone) {
+    *pb = g;
+    *db = make_float3(0.f, 0.f, 0.f);
+    return;
+  }
+  if (kind == kCollFree) {
+    *pb = g;
+    *db = g;
+    return;
+  }
+  const uint32_t idx = coll_index(code);
+  int a;
+  float c;
+  if (code & kCollClipBit) {
+    a = P.clip_axis[idx];
+    c = P.clip_value[idx];
+  } else {
+    a = static_cast<int>(idx >> 1);
+    c = wall_value(sc, static_cast<int>(idx));
+  }
+  const bool tau0 = (code & kCollTau0Bit) != 0u;
+  const float Da = cmp3(D, a);
+  const float tau = tau0 ? 0.0f : (c - cmp3(p, a)) / Da;
+  float3 g1 = g, dbar = make_float3(0.f, 0.f, 0.f);
+  float taub = 0.0f;
+  if (kind >= kCollSlide) {
+    float3 tan = D;
+    set3(tan, a, 0.0f);
+    const float T = sqrtf(dot3(tan, tan));
+    float3 tanb;
+    if (kind == kCollSlide) {
+      const float L = sqrtf(dot3(D, D));
+      const float kappa = L * (1.0f - tau) / (2.0f * T);
+      const float kb = dot3(g, tan);
+      tanb = g * kappa;
+      const float Lb = kb * (1.0f - tau) / (2.0f * T);
+      taub -= kb * L / (2.0f * T);
+      const float Tb = -kb * kappa / T;
+      tanb = tanb + tan * (Tb / T);
+      dbar = dbar + D * (Lb / L);
+    } else {
+      const int w2 = static_cast<int>(coll_wall2(code));
+      const int a2 = w2 >> 1;
+      set3(g1, a2, 0.0f);
+      tanb = make_float3(0.f, 0.f, 0.f);
+      if (!(code & kCollTau2Bit)) {
+        const float ta2 = cmp3(tan, a2);
+        const float p1a2 = cmp3(p, a2) + tau * cmp3(D, a2);
+        const float sigma = (wall_value(sc, w2) - p1a2) / ta2;
+        float3 gm = g;
+        set3(gm, a2, 0.0f);
+        const float sb = dot3(gm, tan);
+        tanb = gm * sigma;
+        set3(g1, a2, -sb / ta2);
+        set3(tanb, a2, -sb * sigma / ta2);
+      }
+    }
+    set3(tanb, a, 0.0f);
+    dbar = dbar + tanb;
+  }
+  // p1 = p + tau D, p1[a] = c
+  float3 pbar = g1;
+  set3(pbar, a, 0.0f);
+  if (!tau0) {
+    float3 gm = g1;
+    set3(gm, a, 0.0f);
+    dbar = dbar + gm * tau;
+    taub += dot3(gm, D);
+    set3(pbar, a, -taub / Da);
+    set3(dbar, a, cmp3(dbar, a) - taub * tau / Da);
+  }
+  *pb = pbar;
+  *db = dbar;
 }
 
 // ---- neighbour lists -----------------------------------------------------------
@@ -208,5 +354,15 @@ __device__ __forceinline__ bool spiky_s(float r2, float h, float* s) {
 }
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// Instantiates a neighbour-pass kernel launch for the tuned block size.
+#define PBF_BLOCK_SWITCH(block, ...)                          \
+  switch (block) {                                            \
+    case 64: { constexpr int BLOCK = 64; __VA_ARGS__; } break;   \
+    case 128: { constexpr int BLOCK = 128; __VA_ARGS__; } break; \
+    case 512: { constexpr int BLOCK = 512; __VA_ARGS__; } break; \
+    default: { constexpr int BLOCK = 256; __VA_ARGS__; } break;  \
+  }
+
 
 }  // namespace pbf

@@ -52,6 +52,7 @@ struct Handle {
   bool snap_valid = false;
   uint64_t snap_steps = 0;
   double snap_time = 0;
+  Tape tape;                 // recording + work arrays of the adjoint (first use)
   double phase_ms[kNumPhases] = {};
   uint64_t phase_launches[kNumPhases] = {};
 
@@ -60,6 +61,8 @@ struct Handle {
   pbf_status alloc_all();
   void free_all();
   pbf_status ensure_scratch(size_t bytes);
+  pbf_status ensure_tape();
+  void free_tape();
   pbf_status enqueue_steps(float dt, int nsteps);
   pbf_status sync_and_check();
   void drop_graphs();

@@ -96,6 +96,28 @@ struct Buffers {
   float* io2 = nullptr;
 };
 
+// Recording of one step for its reverse mode, plus the adjoint work arrays (cell
+// order of that step; allocated on the first adjoint call).
+struct Tape {
+  size_t n = 0;
+  int iters = 0;
+  float4* x = nullptr;    // step input x (w: scene id bits)
+  float4* v = nullptr;    // step input v (w: the prediction's collision record)
+  float4* xs = nullptr;   // (iters + 1) n: x* before each iteration (w: lambda),
+                          // then the final x* (w: |omega|)
+  float4* dp = nullptr;   // iters n: requested displacement (w: collision record)
+  float4* gxs = nullptr;  // adjoint of the current x*
+  float4* pl[2] = {nullptr, nullptr};  // (adjoint of the unscaled delta-p sum, lambda), ping-pong
+  float4* gr = nullptr;   // (sum of grad W / rho0, adjoint of rho)
+  float4* gvo = nullptr;  // adjoint of the output velocity
+  float4* gx = nullptr;   // adjoint of the input x
+  float4* wb = nullptr;   // adjoint of omega
+  float4* eb = nullptr;   // adjoint of eta (vorticity location vector)
+  float* r0 = nullptr;    // per-particle parts of the rest-density adjoint
+  double* r0_part = nullptr;  // block sums of r0
+};
+constexpr int kAdjReduceBlocks = 256;
+
 // Launch shapes picked by the autotuner (threads per block per kernel family).
 struct Tuning {
   int block_predict = 256;
@@ -137,9 +159,18 @@ struct PhaseMarks {
 // ---- launchers (pbf_kernels.cu) ----
 // cur: index of the buffers holding the current (sorted) state; the step
 // writes the next state into 1 - cur.
+// With a tape, the step is the recording forward of the adjoint (same arithmetic).
 cudaError_t launch_step(const Buffers& b, const DevParams& p, const Tuning& t, int cur,
                         float dt, int iters, bool keep_pred, cudaStream_t s,
-                        PhaseMarks* marks = nullptr);
+                        PhaseMarks* marks = nullptr, const Tape* tape = nullptr);
+// ---- reverse mode (pbf_adjoint.cu) ----
+// After launch_step(..., tape) from buffers cur (the step's output now in 1 - cur):
+// adjoints of the step's inputs from those of its outputs, all original order
+// (n, 3) device arrays; gx_out / gv_out may be null (zero); *g_rho0 (device) receives
+// the rest-density adjoint.
+cudaError_t launch_adjoint(const Buffers& b, const DevParams& p, const Tuning& t, int cur, float dt,
+                           const Tape& tape, const float* gx_out, const float* gv_out, float* gx_in,
+                           float* gv_in, double* g_rho0, cudaStream_t s);
 cudaError_t launch_resort(const Buffers& b, const DevParams& p, const Tuning& t, int cur,
                           cudaStream_t s);
 cudaError_t launch_upload(const Buffers& b, int cur, const float* xyz, const float* vel,

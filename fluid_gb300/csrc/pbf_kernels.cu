@@ -41,6 +41,8 @@ __device__ __forceinline__ int scene_of_slot(const float4& p) { return __float_a
 // ---------------------------------------------------------------------------
 // prediction + cell count
 // ---------------------------------------------------------------------------
+// REC (recording forward of the adjoint) also stores the collision record in disp.w.
+template <bool REC>
 __global__ void k_predict(const float4* __restrict__ pos, const float4* __restrict__ vel,
                           float4* __restrict__ disp_out, uint32_t* __restrict__ key_out,
                           uint32_t* __restrict__ rank_out, uint32_t* __restrict__ cell_count,
@@ -56,10 +58,9 @@ __global__ void k_predict(const float4* __restrict__ pos, const float4* __restri
     float3 d = make_float3(0.f, 0.f, 0.f);
     if (move) {
       const float4 v4 = vel[i];
-      // applyForceVelocity, particles.cpp:180: v += g dt
-      const float3 v = make_float3(v4.x + P.g[0] * dt, v4.y + P.g[1] * dt, v4.z + P.g[2] * dt);
-      collide(x, d, v * dt, true, sc, P);
-      disp_out[i] = make_float4(d.x, d.y, d.z, 0.f);
+      uint32_t code = 0u;
+      collide<REC>(x, d, predict_delta(v4, P, dt), true, sc, P, &code);
+      disp_out[i] = make_float4(d.x, d.y, d.z, REC ? __uint_as_float(code) : 0.f);
     }
     key = cell_key(cell_of(x + d, sc, P.inv_cell), sc);
     key_out[i] = key;
@@ -193,12 +194,18 @@ __global__ void k_gather(const uint32_t* __restrict__ perm, const float4* __rest
   const float4 x = pos_a[i];
   pos_b[s] = x;
   id_b[s] = id_a[i];
+  float rec = 0.f;
   if (disp_a) {
     const float4 d = disp_a[i];
     disp_b[s] = d;
     xs_b[s] = make_float4(x.x + d.x, x.y + d.y, x.z + d.z, 0.f);
+    rec = d.w;
   }
-  if (vel_a) vel_b[s] = vel_a[i];
+  if (vel_a) {  // with disp_a (recording forward): w carries the prediction's collision record
+    float4 v = vel_a[i];
+    v.w = rec;
+    vel_b[s] = v;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -300,15 +307,16 @@ __global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs, const uint4* __res
 }
 
 // (lambda_i + lambda_j + s_corr) grad W summed over neighbours; N4 specialises the
-// tensile exponent N = 4 of particles.cpp:40.
-template <int BLOCK, bool N4>
+// tensile exponent N = 4 of particles.cpp:40. REC (recording forward of the adjoint)
+// also stores the requested displacement and the collision record in dp_rec.
+template <int BLOCK, bool N4, bool REC>
 __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
                                                   const float4* __restrict__ pos,
                                                   const uint4* __restrict__ hdr,
                                                   const uint32_t* __restrict__ words,
                                                   const SceneDesc* __restrict__ scenes,
                                                   float4* __restrict__ disp, float4* __restrict__ xs_next,
-                                                  DevParams P, int n) {
+                                                  float4* __restrict__ dp_rec, DevParams P, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 xi = xs[i];
@@ -336,7 +344,9 @@ __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
   const float4 d4 = disp[i];
   float3 d = f3(d4);
   const float3 x = f3(x4);
-  collide(x, d, dp, false, sc, P);
+  uint32_t code = 0u;
+  collide<REC>(x, d, dp, false, sc, P, &code);
+  if (REC) dp_rec[i] = make_float4(dp.x, dp.y, dp.z, __uint_as_float(code));
   disp[i] = make_float4(d.x, d.y, d.z, 0.f);
   xs_next[i] = make_float4(x.x + d.x, x.y + d.y, x.z + d.z, 0.f);
 }
@@ -633,13 +643,17 @@ inline unsigned blocks_for(size_t n, int block) { return static_cast<unsigned>((
 
 // Shared front half of a step and of a resort: keys, counts, scan, slots.
 cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& t, int cur, float dt,
-                            bool move, cudaStream_t s, PhaseMarks* mk = nullptr) {
+                            bool move, cudaStream_t s, PhaseMarks* mk = nullptr, bool rec = false) {
   const int n = static_cast<int>(b.n);
   const uint32_t m = b.n_cells;
   cudaError_t e = cudaMemsetAsync(b.cell_count, 0, sizeof(uint32_t) * m, s);
   if (e != cudaSuccess) return e;
-  k_predict<<<blocks_for(n, t.block_predict), t.block_predict, 0, s>>>(
-      b.pos[cur], b.vel[cur], b.disp[0], b.key, b.rank, b.cell_count, b.scenes, P, dt, move ? 1 : 0, n);
+  if (rec)
+    k_predict<true><<<blocks_for(n, t.block_predict), t.block_predict, 0, s>>>(
+        b.pos[cur], b.vel[cur], b.disp[0], b.key, b.rank, b.cell_count, b.scenes, P, dt, move ? 1 : 0, n);
+  else
+    k_predict<false><<<blocks_for(n, t.block_predict), t.block_predict, 0, s>>>(
+        b.pos[cur], b.vel[cur], b.disp[0], b.key, b.rank, b.cell_count, b.scenes, P, dt, move ? 1 : 0, n);
   if (mk) mk->mark(kPhasePredict, s);
   const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
   k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(b.cell_count, b.cell_start, b.scan_tmp, m);
@@ -654,54 +668,64 @@ cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& 
 
 }  // namespace
 
-#define PBF_BLOCK_SWITCH(block, ...)                          \
-  switch (block) {                                            \
-    case 64: { constexpr int BLOCK = 64; __VA_ARGS__; } break;   \
-    case 128: { constexpr int BLOCK = 128; __VA_ARGS__; } break; \
-    case 512: { constexpr int BLOCK = 512; __VA_ARGS__; } break; \
-    default: { constexpr int BLOCK = 256; __VA_ARGS__; } break;  \
-  }
-
 cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, int cur, float dt,
-                        int iters, bool keep_pred, cudaStream_t s, PhaseMarks* mk) {
+                        int iters, bool keep_pred, cudaStream_t s, PhaseMarks* mk, const Tape* tape) {
   const int n = static_cast<int>(b.n);
   if (n == 0) return cudaSuccess;
   const int A = cur, B = 1 - cur;
+  const bool rec = tape != nullptr;
   if (mk) mk->mark(-1, s);
   if (P.stats) k_stats_init<<<1, 1, 0, s>>>(b.stats);
   if (mk) mk->mark(kPhaseStats, s);
-  cudaError_t e = sort_into_cells(b, P, t, A, dt, true, s, mk);
+  cudaError_t e = sort_into_cells(b, P, t, A, dt, true, s, mk, rec);
   if (e != cudaSuccess) return e;
+  float4* xs0 = rec ? tape->xs : b.xs[0];
   k_gather<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(
-      b.perm, b.pos[A], b.disp[0], nullptr, b.id[A], b.pos[B], b.disp[1], b.xs[0], nullptr, b.id[B], n);
+      b.perm, b.pos[A], b.disp[0], rec ? b.vel[A] : nullptr, b.id[A], b.pos[B], b.disp[1], xs0,
+      rec ? tape->v : nullptr, b.id[B], n);
+  if (rec) {
+    e = cudaMemcpyAsync(tape->x, b.pos[B], sizeof(float4) * b.n, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  }
   if (keep_pred && b.pred) {
-    e = cudaMemcpyAsync(b.pred, b.xs[0], sizeof(float4) * b.n, cudaMemcpyDeviceToDevice, s);
+    e = cudaMemcpyAsync(b.pred, xs0, sizeof(float4) * b.n, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return e;
   }
   if (mk) mk->mark(kPhaseGather, s);
   PBF_BLOCK_SWITCH(t.block_nbr,
                    k_nbr_build<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                       b.xs[0], b.pos[B], b.cell_start, b.scenes, b.nbr_hdr, b.nbr_w, b.err, P, n));
+                       xs0, b.pos[B], b.cell_start, b.scenes, b.nbr_hdr, b.nbr_w, b.err, P, n));
   if (mk) mk->mark(kPhaseNeighbors, s);
   for (int it = 0; it < iters; ++it) {
-    float4* xcur = b.xs[it & 1];
-    float4* xnext = b.xs[(it + 1) & 1];
+    float4* xcur = rec ? tape->xs + static_cast<size_t>(it) * b.n : b.xs[it & 1];
+    float4* xnext = rec ? tape->xs + static_cast<size_t>(it + 1) * b.n : b.xs[(it + 1) & 1];
+    float4* dprec = rec ? tape->dp + static_cast<size_t>(it) * b.n : nullptr;
     PBF_BLOCK_SWITCH(t.block_solve,
                      k_lambda<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
                          xcur, b.nbr_hdr, b.nbr_w, b.lam, (it == 0 && P.stats) ? b.rho_iter0 : nullptr, P, n));
     if (mk) mk->mark(kPhaseLambda, s);
-    if (P.scorr_n == 4) {
+    if (rec) {
+      if (P.scorr_n == 4) {
+        PBF_BLOCK_SWITCH(t.block_solve,
+                         (k_deltap<BLOCK, true, true><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                             xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, dprec, P, n)));
+      } else {
+        PBF_BLOCK_SWITCH(t.block_solve,
+                         (k_deltap<BLOCK, false, true><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                             xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, dprec, P, n)));
+      }
+    } else if (P.scorr_n == 4) {
       PBF_BLOCK_SWITCH(t.block_solve,
-                       (k_deltap<BLOCK, true><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                           xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, P, n)));
+                       (k_deltap<BLOCK, true, false><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                           xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, nullptr, P, n)));
     } else {
       PBF_BLOCK_SWITCH(t.block_solve,
-                       (k_deltap<BLOCK, false><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                           xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, P, n)));
+                       (k_deltap<BLOCK, false, false><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                           xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, nullptr, P, n)));
     }
     if (mk) mk->mark(kPhaseDeltaP, s);
   }
-  float4* fin = b.xs[iters & 1];
+  float4* fin = rec ? tape->xs + static_cast<size_t>(iters) * b.n : b.xs[iters & 1];
   PBF_BLOCK_SWITCH(t.block_solve,
                    k_xsph<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
                        fin, b.disp[1], b.nbr_hdr, b.nbr_w, b.vel[B], b.omega, b.rho, P, 1.0f / dt, n));

@@ -89,6 +89,7 @@ def _declare(L):
         "pbf_num_phases": (ctypes.c_int, []),
         "pbf_phase_name": (ctypes.c_char_p, [ctypes.c_int]),
         "pbf_density_noalloc": (st, [P, sz, P, P, P]),
+        "pbf_adjoint_step_device": (st, [P, ctypes.c_double, P, P, P, P, P, P, P, P, P, P]),
         "pbf_size": (sz, [P]),
         "pbf_num_scenes": (ctypes.c_int, [P]),
         "pbf_last_error": (ctypes.c_char_p, [P]),
@@ -224,6 +225,21 @@ class Simulator:
         self._check(lib().pbf_get_state_device(self._h, P(pos_ptr) if pos_ptr else None,
                                                P(vel_ptr) if vel_ptr else None,
                                                P(rho_ptr) if rho_ptr else None, P(stream) if stream else None))
+
+    def adjoint_step_device(self, dt: float, pos_ptr: int | None, vel_ptr: int | None,
+                            gx_out_ptr: int | None, gv_out_ptr: int | None, gx_in_ptr: int, gv_in_ptr: int,
+                            g_rho0_ptr: int, pos_out_ptr: int | None = None, vel_out_ptr: int | None = None,
+                            stream: int = 0):
+        """pbf_adjoint_step_device: one recorded step from (pos, vel) and its reverse mode.
+
+        All pointers are device addresses of (n, 3) float32 arrays in original order
+        (``g_rho0_ptr``: one float64). ``pos_ptr`` None steps from the current state.
+        """
+        def opt(q):
+            return P(q) if q else None
+        self._check(lib().pbf_adjoint_step_device(
+            self._h, dt, opt(pos_ptr), opt(vel_ptr), opt(gx_out_ptr), opt(gv_out_ptr), P(gx_in_ptr),
+            P(gv_in_ptr), P(g_rho0_ptr), opt(pos_out_ptr), opt(vel_out_ptr), opt(stream)))
 
     def estimate_densities(self) -> np.ndarray:
         """Particles::estimateDensities (particles.cpp:440-444): self term included."""

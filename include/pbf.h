@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define PBF_ABI_VERSION 1
+#define PBF_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define PBF_API __attribute__((visibility("default")))
@@ -242,6 +242,32 @@ PBF_API const char* pbf_last_error(const pbf_handle* h);
  * cells of size h over the box; larger inputs return PBF_ERR_INVALID with the
  * reason in pbf_last_error(NULL).
  */
+/*
+ * pbf_adjoint_step_device -- no counterpart in the reference (which has no
+ * gradients); the reverse mode of one Particles::timeStep (particles.cpp:250-297).
+ *
+ * Runs one step from the state (xyz, vel) -- recording what its reverse needs --
+ * then its reverse mode with the step's neighbour sets held fixed and every
+ * collision differentiated with its active set fixed. All arrays are DEVICE
+ * pointers in original particle order, (n, 3) float32:
+ *   xyz, vel         the step's input state (xyz NULL: the handle's current state;
+ *                    vel NULL: zero)
+ *   gx_out, gv_out   adjoints of the step's output positions / velocities (NULL: 0)
+ *   gx_in, gv_in     receive the adjoints of the input positions / velocities
+ *   g_rho0           one double, receives the adjoint of params.rest_density
+ *   xyz_out, vel_out receive the step's outputs (NULL: not written)
+ * The handle's state becomes the step's output (simulate_time is not advanced).
+ * The work is enqueued on `stream` (a cudaStream_t, NULL for the legacy default
+ * stream) without waiting; pbf_sync reports capacity and non-finite errors.
+ * Device memory for the recording (about (48 + 32 iters) bytes per particle plus
+ * 150 bytes of work arrays) is allocated on the first call. The sums are
+ * evaluated in a fixed order: repeated calls give identical results.
+ */
+PBF_API pbf_status pbf_adjoint_step_device(pbf_handle* h, double dt, const float* xyz, const float* vel,
+                                           const float* gx_out, const float* gv_out, float* gx_in,
+                                           float* gv_in, double* g_rho0, float* xyz_out, float* vel_out,
+                                           void* stream);
+
 #define PBF_NOALLOC_MAX_PARTICLES 65536
 #define PBF_NOALLOC_MAX_CELLS 262144
 PBF_API pbf_status pbf_density_noalloc(const pbf_params* params, size_t n,

@@ -1,0 +1,168 @@
+"""GPU adjoint (pbf_adjoint_step_device) against the FP64 reference gradient.
+
+The reference gradient (oracle/pbf_oracle_adj.c, pinned to FP64 central differences by
+tests/test_oracle_adjoint.py) runs on the GPU step's own neighbour sets, from the same
+FP32 inputs. Bar: 1e-4 normwise relative error of the position and velocity adjoints
+and of the rest-density adjoint (the FP32 forward differs from the FP64 one by ~1e-6,
+and the collision reverse divides by the normal component of the displacement).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from fluid_gb300 import scenes
+from tests.helpers import adjoint_corner_scene, adjoint_fall_scene, adjoint_free_scene, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL_ADJ = 1e-4
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+
+    from fluid_gb300 import pbf
+
+    pbf.lib()
+    assert torch.cuda.is_available()
+    return pbf, torch
+
+
+def _f32(a):
+    return np.asarray(a, dtype=np.float32).astype(np.float64)
+
+
+def _gpu_adjoint(env, sim, pos, vel, gx, gv, dt):
+    pbf, torch = env
+    t = lambda a: torch.tensor(np.asarray(a, dtype=np.float32), device="cuda")  # noqa: E731
+    x, v, gxo, gvo = t(pos), t(vel), t(gx), t(gv)
+    gxi, gvi = torch.empty_like(x), torch.empty_like(x)
+    xo, vo = torch.empty_like(x), torch.empty_like(x)
+    r = torch.zeros(1, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    sim.adjoint_step_device(dt, x.data_ptr(), v.data_ptr(), gxo.data_ptr(), gvo.data_ptr(), gxi.data_ptr(),
+                            gvi.data_ptr(), r.data_ptr(), xo.data_ptr(), vo.data_ptr(), stream=s)
+    sim.sync()
+    torch.cuda.synchronize()
+    return {"gx": gxi.cpu().numpy(), "gv": gvi.cpu().numpy(), "grho0": float(r.item()),
+            "pos": xo.cpu().numpy(), "vel": vo.cpu().numpy()}
+
+
+def _case(name):
+    if name == "fall":
+        return adjoint_fall_scene()
+    if name == "corner":
+        return adjoint_corner_scene()
+    if name == "free":
+        return adjoint_free_scene(6)
+    sc = scenes.block4096(1)
+    return sc.pos, sc.vel, sc.params
+
+
+@pytest.mark.parametrize("name", ["fall", "corner", "free", "block4096"])
+def test_one_step_adjoint_matches_fp64_reference_gradient(env, oracle_lib, name):
+    pbf, _ = env
+    p, v, prm = _case(name)
+    pos, vel = _f32(p), _f32(v)
+    rng = np.random.default_rng(11)
+    gx = rng.standard_normal(pos.shape).astype(np.float32).astype(np.float64)
+    gv = rng.standard_normal(pos.shape).astype(np.float32).astype(np.float64)
+    with pbf.Simulator(pos, vel, prm) as sim:
+        g = _gpu_adjoint(env, sim, pos, vel, gx, gv, prm.dt)
+        nb = sim.neighbors()
+    ref = oracle_lib.step_adjoint(pos, vel, prm, gx, gv, given_neighbors=nb)
+    ex, ev = rel_err(g["pos"], ref["pos"]), rel_err(g["vel"], ref["vel"])
+    egx, egv = rel_err(g["gx"], ref["gx"]), rel_err(g["gv"], ref["gv"])
+    er0 = abs(g["grho0"] - ref["grho0"]) / abs(ref["grho0"])
+    print(f"{name}: kinds {ref['kinds'].tolist()} forward pos {ex:.2e} vel {ev:.2e}; "
+          f"adjoint x {egx:.2e} v {egv:.2e} rho0 {er0:.2e}")
+    assert ex < 1e-5 and ev < 1e-5
+    assert egx < TOL_ADJ and egv < TOL_ADJ and er0 < TOL_ADJ
+
+
+def test_adjoint_is_deterministic_and_leaves_the_step_output(env, oracle_lib):
+    pbf, _ = env
+    p, v, prm = adjoint_fall_scene()
+    pos, vel = _f32(p), _f32(v)
+    rng = np.random.default_rng(12)
+    gx = rng.standard_normal(pos.shape)
+    gv = rng.standard_normal(pos.shape)
+    with pbf.Simulator(pos, vel, prm) as sim:
+        a = _gpu_adjoint(env, sim, pos, vel, gx, gv, prm.dt)
+        after = sim.positions()
+        b = _gpu_adjoint(env, sim, pos, vel, gx, gv, prm.dt)
+    assert np.array_equal(a["gx"], b["gx"]) and np.array_equal(a["gv"], b["gv"]) and a["grho0"] == b["grho0"]
+    assert np.array_equal(after, a["pos"])
+    with pbf.Simulator(pos, vel, prm) as sim:
+        sim.time_step(prm.dt, 1)
+        assert np.array_equal(sim.positions(), a["pos"]) and np.array_equal(sim.velocities(), a["vel"])
+
+
+def test_adjoint_of_a_batch_is_the_adjoint_of_each_scene(env):
+    pbf, _ = env
+    p1, v1, prm = adjoint_fall_scene(5, seed=21)
+    p2, v2, _ = adjoint_corner_scene(seed=22)
+    pos = _f32(np.concatenate([p1, p2]))
+    vel = _f32(np.concatenate([v1, v2]))
+    rng = np.random.default_rng(13)
+    gx = rng.standard_normal(pos.shape)
+    gv = rng.standard_normal(pos.shape)
+    box = ((0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
+    with pbf.Simulator(pos, vel, prm, counts=[len(p1), len(p2)], boxes=[box, box]) as sim:
+        both = _gpu_adjoint(env, sim, pos, vel, gx, gv, prm.dt)
+    n1 = len(p1)
+    parts = []
+    for sl in (slice(0, n1), slice(n1, None)):
+        with pbf.Simulator(pos[sl], vel[sl], prm) as sim:
+            parts.append(_gpu_adjoint(env, sim, pos[sl], vel[sl], gx[sl], gv[sl], prm.dt))
+    assert np.array_equal(both["gx"], np.concatenate([q["gx"] for q in parts]))
+    assert np.array_equal(both["gv"], np.concatenate([q["gv"] for q in parts]))
+    assert abs(both["grho0"] - sum(q["grho0"] for q in parts)) <= 1e-6 * abs(both["grho0"])
+
+
+def test_autograd_rollout_matches_fp64_reference_gradient(env, oracle_lib):
+    """Three checkpointed steps through torch.autograd (loss: mean squared distance to a
+    target rollout with perturbed initial velocities) against the FP64 reference
+    gradient of the same rollout, with respect to v0 and rho0."""
+    from fluid_gb300.autograd import rollout
+
+    pbf, torch = env
+    p, v, prm = adjoint_free_scene(6)
+    pos, vel = _f32(p), _f32(v)
+    steps = 3
+    vt = vel + _f32(scenes.normal(5, vel.size, 0.1, stream=7).reshape(vel.shape))
+    target = oracle_lib.step(pos, vt, prm, steps)["pos"]
+    with pbf.Simulator(pos, vel, prm) as sim:
+        x0 = torch.tensor(pos, dtype=torch.float32, device="cuda")
+        v0 = torch.tensor(vel, dtype=torch.float32, device="cuda", requires_grad=True)
+        rho0 = torch.tensor(prm.rest_density, dtype=torch.float64, requires_grad=True)
+        xT, vT = rollout(sim, x0, v0, rho0, steps)
+        tgt = torch.tensor(target, dtype=torch.float32, device="cuda")
+        loss = ((xT - tgt) ** 2).mean()
+        loss.backward()
+        gv0 = v0.grad.cpu().numpy()
+        gr0 = float(rho0.grad)
+        xT_np = xT.detach().cpu().numpy()
+    fin = oracle_lib.step(pos, vel, prm, steps)["pos"]
+    gx = 2.0 * (fin - target) / fin.size
+    ref = oracle_lib.rollout_adjoint(pos, vel, prm, steps, gx, np.zeros_like(gx))
+    e_fwd = rel_err(xT_np, fin)
+    e_v = rel_err(gv0, ref["gv"])
+    e_r = abs(gr0 - ref["grho0"]) / abs(ref["grho0"])
+    print(f"{steps}-step rollout: forward {e_fwd:.2e} grad v0 {e_v:.2e} grad rho0 {e_r:.2e}")
+    assert e_fwd < 1e-5
+    assert e_v < 1e-3 and e_r < 1e-3
+
+
+def test_adjoint_argument_errors(env):
+    pbf, torch = env
+    p, v, prm = adjoint_fall_scene(3)
+    with pbf.Simulator(p, v, prm) as sim:
+        x = torch.zeros((sim.n, 3), dtype=torch.float32, device="cuda")
+        r = torch.zeros(1, dtype=torch.float64, device="cuda")
+        with pytest.raises(pbf.PbfError):
+            sim.adjoint_step_device(prm.dt, None, None, None, None, x.data_ptr(), x.data_ptr(), 0)
+        with pytest.raises(pbf.PbfError):
+            sim.adjoint_step_device(prm.dt, None, None, None, None, 0, x.data_ptr(), r.data_ptr())
