@@ -18,6 +18,7 @@ from .params import CParams, PbfParams
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpbf.so"
 
 PBF_OK = 0
+ABI_VERSION = 2  # PBF_ABI_VERSION of include/pbf.h that these declarations follow
 STATUS = {0: "PBF_OK", 1: "PBF_ERR_INVALID", 2: "PBF_ERR_CUDA", 3: "PBF_ERR_TIMEOUT",
           4: "PBF_ERR_NONFINITE", 5: "PBF_ERR_CAPACITY", 6: "PBF_ERR_NOMEM"}
 
@@ -108,7 +109,10 @@ def lib():
         if not LIB_PATH.exists():
             raise FileNotFoundError(
                 f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
-        _lib = _declare(ctypes.CDLL(str(LIB_PATH)))
+        L = _declare(ctypes.CDLL(str(LIB_PATH)))
+        if L.pbf_abi_version() != ABI_VERSION:
+            raise ImportError(f"{LIB_PATH} has ABI version {L.pbf_abi_version()}, expected {ABI_VERSION}: rebuild it")
+        _lib = L
     return _lib
 
 

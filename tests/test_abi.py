@@ -45,7 +45,11 @@ def test_every_declared_symbol_is_exported(libpbf):
 
 
 def test_abi_version(libpbf):
-    assert libpbf.pbf_abi_version() == 2
+    from fluid_gb300.pbf import ABI_VERSION
+
+    header = (ROOT / "include" / "pbf.h").read_text()
+    assert int(re.search(r"#define PBF_ABI_VERSION (\d+)", header).group(1)) == ABI_VERSION
+    assert libpbf.pbf_abi_version() == ABI_VERSION
 
 
 def test_default_params_are_the_reference_constants(libpbf):
