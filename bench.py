@@ -326,6 +326,107 @@ def bench_reference(args, scene, world, rank):
     return 0
 
 
+def bench_adjoint(args, local, steps: int = 30, big_steps: int = 5) -> dict:
+    """Adjoint against plain forward. Workload: the 32^3 block of scenes.adjoint_32k over
+    its 30-step rollout: the forward steps run from the initial state keeping a
+    checkpoint (x, v) before every step, then pbf_adjoint_step_device runs once per step
+    in reverse from those checkpoints (recording recompute of the step + its reverse).
+    Every timed step is bracketed by CUDA events on the handle's stream, with an L2
+    flush before it in both arms. The same pair is also timed at 1M particles
+    (colliding_blocks_1m, every step from the configured state) and the whole
+    torch.autograd rollout (forward with checkpoints + backward) end to end."""
+    import torch
+
+    from fluid_gb300 import pbf, scenes
+    from fluid_gb300.autograd import rollout
+
+    dev = f"cuda:{local}"
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def pair(sc, nsteps, rollout_mode):
+        prm = sc.params.with_(flags=0)
+        sim = pbf.Simulator(sc.pos, sc.vel, prm, device=local)
+        n = sim.n
+        dt = prm.dt
+        st = torch.cuda.ExternalStream(sim.stream)
+        x0 = torch.tensor(sc.pos.astype(np.float32), device=dev)
+        v0 = torch.tensor(sc.vel.astype(np.float32), device=dev)
+        ckx = torch.empty((nsteps if rollout_mode else 0, n, 3), dtype=torch.float32, device=dev)
+        ckv = torch.empty_like(ckx)
+        g = [torch.zeros((n, 3), dtype=torch.float32, device=dev) for _ in range(4)]
+        g[0].normal_()
+        r0 = torch.zeros(nsteps, dtype=torch.float64, device=dev)
+        ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+        fwd, adj = [], []
+        if not rollout_mode:  # every step from the configured state, sorted once (as the main leg)
+            sim.sort()
+            sim.snapshot()
+        for rep in range(2):  # the first pass warms both paths
+            fwd.clear()
+            adj.clear()
+            if rollout_mode:
+                sim.set_state_device(x0.data_ptr(), v0.data_ptr(), torch.cuda.current_stream().cuda_stream)
+            torch.cuda.synchronize()
+            with torch.cuda.stream(st):
+                for t in range(nsteps):
+                    if rollout_mode:
+                        sim.get_state_device(ckx[t].data_ptr(), ckv[t].data_ptr(), None, st.cuda_stream)
+                    else:
+                        sim.restore()
+                    flush.zero_()
+                    a, z = ev(), ev()
+                    a.record(st)
+                    sim.step_async(dt, 1)
+                    z.record(st)
+                    fwd.append((a, z))
+                for t in range(nsteps - 1, -1, -1):
+                    if rollout_mode:
+                        xp, vp = ckx[t].data_ptr(), ckv[t].data_ptr()
+                    else:
+                        sim.restore()
+                        xp = vp = None  # the restored state
+                    flush.zero_()
+                    a, z = ev(), ev()
+                    a.record(st)
+                    sim.adjoint_step_device(dt, xp, vp, g[0].data_ptr(), g[1].data_ptr(), g[2].data_ptr(),
+                                            g[3].data_ptr(), r0[t].data_ptr(), stream=st.cuda_stream)
+                    z.record(st)
+                    adj.append((a, z))
+            sim.sync()
+            torch.cuda.synchronize()
+        f_ms = sum(a.elapsed_time(z) for a, z in fwd) / nsteps
+        a_ms = sum(a.elapsed_time(z) for a, z in adj) / nsteps
+        out = {"particles": n, "steps": nsteps, "forward_ms_per_step": f_ms, "adjoint_ms_per_step": a_ms,
+               "ratio": a_ms / f_ms, "forward_updates_per_s": n / (f_ms / 1e3),
+               "adjoint_updates_per_s": n / (a_ms / 1e3)}
+        if rollout_mode:  # the torch.autograd rollout, forward + backward, end to end on the device
+            rho0 = torch.tensor(prm.rest_density, dtype=torch.float64, requires_grad=True)
+            tgt = x0 + 0.01
+            times = []
+            for rep in range(2):
+                v = v0.clone().requires_grad_(True)
+                torch.cuda.synchronize()
+                a, m, z = ev(), ev(), ev()
+                a.record()
+                xT, vT = rollout(sim, x0, v, rho0, nsteps)
+                loss = ((xT - tgt) ** 2).mean()
+                m.record()
+                loss.backward()
+                z.record()
+                torch.cuda.synchronize()
+                times.append((a.elapsed_time(m), m.elapsed_time(z)))
+            out["autograd_forward_ms"], out["autograd_backward_ms"] = times[-1]
+            out["autograd_ratio"] = (times[-1][0] + times[-1][1]) / (f_ms * nsteps)
+        sim.close()
+        return out
+
+    small = pair(scenes.adjoint_32k(), steps, True)
+    big = pair(scenes.colliding_blocks_1m(), big_steps, False)
+    return {"workload": "adjoint_32k", "unit": UNIT, "l2": "flushed (256 MiB) before every timed step",
+            **small, "at_1m": {"workload": "colliding_blocks_1m", **big},
+            "target_ratio": 3.0}
+
+
 def bench_ours(args, scene, world, rank, local):
     import torch
 
@@ -448,6 +549,8 @@ def bench_ours(args, scene, world, rank, local):
         line["e2e"] = e2e
     if not args.no_batched:
         line["batched"] = bench_batched(args, local)
+    if not args.no_adjoint:
+        line["adjoint"] = bench_adjoint(args, local)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
         line["cpu_port_all_cores"] = cpu_port_all_cores(scene, min(args.cpu_seconds, 10.0))
@@ -468,6 +571,7 @@ def main(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -250,8 +250,8 @@ PBF_API const char* pbf_last_error(const pbf_handle* h);
  * then its reverse mode with the step's neighbour sets held fixed and every
  * collision differentiated with its active set fixed. All arrays are DEVICE
  * pointers in original particle order, (n, 3) float32:
- *   xyz, vel         the step's input state (xyz NULL: the handle's current state;
- *                    vel NULL: zero)
+ *   xyz, vel         the step's input state (xyz NULL: the handle's current state,
+ *                    vel ignored; vel NULL with xyz given: zero velocities)
  *   gx_out, gv_out   adjoints of the step's output positions / velocities (NULL: 0)
  *   gx_in, gv_in     receive the adjoints of the input positions / velocities
  *   g_rho0           one double, receives the adjoint of params.rest_density

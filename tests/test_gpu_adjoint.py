@@ -2,9 +2,13 @@
 
 The reference gradient (oracle/pbf_oracle_adj.c, pinned to FP64 central differences by
 tests/test_oracle_adjoint.py) runs on the GPU step's own neighbour sets, from the same
-FP32 inputs. Bar: 1e-4 normwise relative error of the position and velocity adjoints
-and of the rest-density adjoint (the FP32 forward differs from the FP64 one by ~1e-6,
-and the collision reverse divides by the normal component of the displacement).
+FP32 inputs. Bar: 1e-4 normwise relative error of the position, velocity and
+rest-density adjoints -- or, where the gradient itself is worse conditioned than that,
+5x its sensitivity to one FP32 rounding of the inputs: the FP64 reference gradient
+recomputed from inputs perturbed by 2^-24 relative moves by that much, so no FP32
+evaluation can be held closer. (Stops against a wall scale the tangential motion by
+1 / normal component of the displacement; in the corner scene one input rounding moves
+the FP64 gradient by ~1e-4.)
 """
 from __future__ import annotations
 
@@ -76,10 +80,27 @@ def test_one_step_adjoint_matches_fp64_reference_gradient(env, oracle_lib, name)
     ex, ev = rel_err(g["pos"], ref["pos"]), rel_err(g["vel"], ref["vel"])
     egx, egv = rel_err(g["gx"], ref["gx"]), rel_err(g["gv"], ref["gv"])
     er0 = abs(g["grho0"] - ref["grho0"]) / abs(ref["grho0"])
+    sens = _fp32_sensitivity(oracle_lib, pos, vel, prm, gx, gv, nb, ref)
+    bar = max(TOL_ADJ, 5.0 * sens)
     print(f"{name}: kinds {ref['kinds'].tolist()} forward pos {ex:.2e} vel {ev:.2e}; "
-          f"adjoint x {egx:.2e} v {egv:.2e} rho0 {er0:.2e}")
+          f"adjoint x {egx:.2e} v {egv:.2e} rho0 {er0:.2e}; FP64 gradient moves {sens:.1e} "
+          f"under one input rounding -> bar {bar:.1e}")
     assert ex < 1e-5 and ev < 1e-5
-    assert egx < TOL_ADJ and egv < TOL_ADJ and er0 < TOL_ADJ
+    assert egx < bar and egv < bar and er0 < bar
+
+
+def _fp32_sensitivity(oracle_lib, pos, vel, prm, gx, gv, nb, ref):
+    """Median normwise change of the FP64 gradient over 3 input perturbations of 2^-24
+    relative (one FP32 rounding), on the same neighbour sets."""
+    rng = np.random.default_rng(5)
+    u = 2.0 ** -24
+    out = []
+    for _ in range(3):
+        pp = pos * (1 + u * rng.uniform(-1, 1, pos.shape))
+        vv = vel * (1 + u * rng.uniform(-1, 1, vel.shape))
+        a = oracle_lib.step_adjoint(pp, vv, prm, gx, gv, given_neighbors=nb)
+        out.append(max(rel_err(a["gx"], ref["gx"]), rel_err(a["gv"], ref["gv"])))
+    return float(np.median(out))
 
 
 def test_adjoint_is_deterministic_and_leaves_the_step_output(env, oracle_lib):
@@ -166,3 +187,46 @@ def test_adjoint_argument_errors(env):
             sim.adjoint_step_device(prm.dt, None, None, None, None, x.data_ptr(), x.data_ptr(), 0)
         with pytest.raises(pbf.PbfError):
             sim.adjoint_step_device(prm.dt, None, None, None, None, 0, x.data_ptr(), r.data_ptr())
+
+
+def test_adjoint_workload_against_fp64_finite_differences(env, oracle_lib):
+    """The adjoint workload (scenes.adjoint_32k: 32^3 block, loss = mean squared distance
+    of the final positions to a rollout from velocities perturbed by N(0, 0.1^2)):
+    the GPU gradient through the autograd rollout against the committed FP64 central
+    differences (eps = 1e-4, 64 velocity coordinates + the rest density;
+    tests/golden/make_adjoint_fd.py) and the FP64 reference gradient, per horizon.
+
+    One step: within 1e-4 of the differences. Longer horizons are reported: the block
+    sits on the floor, so perturbations of 1e-4 switch floor contacts and the
+    differences stop measuring the derivative (the FP64 reference gradient itself
+    leaves them at T = 2); there the GPU gradient is held to the FP64 reference
+    gradient at T = 2, and at T = 30 only reported (the dynamics amplify an input
+    rounding by ~3x per step, so no FP32 rollout gradient stays close that long)."""
+    import os
+
+    from fluid_gb300.autograd import rollout
+    from tests.golden.make_adjoint_fd import workload
+
+    pbf, torch = env
+    fx = np.load(os.path.join(os.path.dirname(__file__), "golden", "adjoint_32k_fd.npz"))
+    pos, vel, vt, prm = workload()
+    coords = fx["coords"]
+    report = {}
+    for T in fx["horizons"].tolist():
+        target = oracle_lib.step(pos, vt, prm, T)["pos"]
+        with pbf.Simulator(pos, vel, prm) as sim:
+            x0 = torch.tensor(pos, dtype=torch.float32, device="cuda")
+            v0 = torch.tensor(vel, dtype=torch.float32, device="cuda", requires_grad=True)
+            rho0 = torch.tensor(prm.rest_density, dtype=torch.float64, requires_grad=True)
+            xT, _ = rollout(sim, x0, v0, rho0, T)
+            loss = ((xT - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2).mean()
+            loss.backward()
+            g = v0.grad.cpu().numpy().reshape(-1)[coords].astype(np.float64)
+            gr = float(rho0.grad)
+        fd, ref = fx[f"fd_{T}"], fx[f"ref_{T}"]
+        report[T] = dict(gpu_vs_fd=rel_err(g, fd), ref_vs_fd=rel_err(ref, fd), gpu_vs_ref=rel_err(g, ref),
+                         rho0_gpu_vs_fd=abs(gr - fx[f"fd_rho0_{T}"]) / abs(fx[f"fd_rho0_{T}"]),
+                         rho0_gpu_vs_ref=abs(gr - fx[f"ref_rho0_{T}"]) / abs(fx[f"ref_rho0_{T}"]))
+        print(f"T={T}: " + " ".join(f"{k} {v:.2e}" for k, v in report[T].items()))
+    assert report[1]["gpu_vs_fd"] < TOL_ADJ and report[1]["rho0_gpu_vs_fd"] < TOL_ADJ
+    assert report[2]["gpu_vs_ref"] < 1e-3 and report[2]["rho0_gpu_vs_ref"] < 1e-3
