@@ -85,7 +85,9 @@ def test_one_step_adjoint_matches_fp64_reference_gradient(env, oracle_lib, name)
     print(f"{name}: kinds {ref['kinds'].tolist()} forward pos {ex:.2e} vel {ev:.2e}; "
           f"adjoint x {egx:.2e} v {egv:.2e} rho0 {er0:.2e}; FP64 gradient moves {sens:.1e} "
           f"under one input rounding -> bar {bar:.1e}")
-    assert ex < 1e-5 and ev < 1e-5
+    # the forward's own bar is in the parity suite; here velocities of the free block are
+    # differences of positions near 2 m over a 2.7e-3 m move (1e-4 per FP32 ulp)
+    assert ex < 1e-5 and ev < 1e-4
     assert egx < bar and egv < bar and er0 < bar
 
 
@@ -166,15 +168,29 @@ def test_autograd_rollout_matches_fp64_reference_gradient(env, oracle_lib):
         gv0 = v0.grad.cpu().numpy()
         gr0 = float(rho0.grad)
         xT_np = xT.detach().cpu().numpy()
-    fin = oracle_lib.step(pos, vel, prm, steps)["pos"]
-    gx = 2.0 * (fin - target) / fin.size
-    ref = oracle_lib.rollout_adjoint(pos, vel, prm, steps, gx, np.zeros_like(gx))
+    def ref_grad(p0, v0_):
+        fin = oracle_lib.step(p0, v0_, prm, steps)["pos"]
+        gx = 2.0 * (fin - target) / fin.size
+        return fin, oracle_lib.rollout_adjoint(p0, v0_, prm, steps, gx, np.zeros_like(gx))
+
+    fin, ref = ref_grad(pos, vel)
     e_fwd = rel_err(xT_np, fin)
     e_v = rel_err(gv0, ref["gv"])
     e_r = abs(gr0 - ref["grho0"]) / abs(ref["grho0"])
-    print(f"{steps}-step rollout: forward {e_fwd:.2e} grad v0 {e_v:.2e} grad rho0 {e_r:.2e}")
+    # conditioning: the FP64 rollout gradient from inputs moved by one FP32 rounding
+    rng = np.random.default_rng(6)
+    u = 2.0 ** -24
+    sens_v, sens_r = [], []
+    for _ in range(3):
+        _, a = ref_grad(pos * (1 + u * rng.uniform(-1, 1, pos.shape)), vel)
+        sens_v.append(rel_err(a["gv"], ref["gv"]))
+        sens_r.append(abs(a["grho0"] - ref["grho0"]) / abs(ref["grho0"]))
+    bar_v = max(1e-4, 5.0 * float(np.median(sens_v)))
+    bar_r = max(1e-4, 5.0 * float(np.median(sens_r)))
+    print(f"{steps}-step rollout: forward {e_fwd:.2e} grad v0 {e_v:.2e} (bar {bar_v:.1e}) "
+          f"grad rho0 {e_r:.2e} (bar {bar_r:.1e})")
     assert e_fwd < 1e-5
-    assert e_v < 1e-3 and e_r < 1e-3
+    assert e_v < bar_v and e_r < bar_r
 
 
 def test_adjoint_argument_errors(env):
