@@ -256,7 +256,9 @@ pbf_status Handle::sync_and_check() {
   if (host_err_word & PBF_ERRBIT_NEIGHBOR_CAPACITY)
     return fail(PBF_ERR_CAPACITY, "a particle had more neighbours than max_neighbors");
   if (host_err_word & PBF_ERRBIT_ROW_CAPACITY)
-    return fail(PBF_ERR_CAPACITY, "more than 256 particles in one 3-cell row");
+    return fail(PBF_ERR_CAPACITY,
+                "more than 4096 particles in one 3-cell row, or a neighbour more than 16383 slots past its "
+                "z-slab's first candidate");
   return PBF_OK;
 }
 

@@ -24,7 +24,7 @@
 
 namespace pbf {
 
-constexpr int kMaxRowCandidates = 256;  // u8 offsets within one 3-cell row
+constexpr int kMaxRowCandidates = 4096;  // bound on the candidates scanned in one 3-cell row
 constexpr int kNeighborAlert = 18;      // NUM_NEIGHBOR_ALERT_THRESHOLD, particles.cpp:32
 constexpr float kEps = 1e-11f;          // EPS_D, CGL/include/CGL/misc.h:11
 

@@ -206,13 +206,13 @@ def adjoint_32k(seed: int = 5) -> Scene:
 
     Four Jacobi iterations cannot hold the 0.8 m column up: it compresses to ~3.3x the
     rest density by step 30 (the FP64 restatement does the same), with up to ~230
-    neighbours per particle, so the neighbour capacity is 256."""
+    neighbours per particle, so the neighbour capacity is 512."""
     h = 0.05
     s = h / 2
     p = lattice(32, 32, 32, s, corner=(0.1, 0.0, 0.1))
     p += uniform(seed, p.size, -0.008 * s, 0.008 * s).reshape(p.shape)
-    return Scene("adjoint_32k", p, np.zeros_like(p), physical_params(h, s, max_neighbors=256), 30, seed,
-                 notes="column compresses under 4 Jacobi iterations; max_neighbors 256")
+    return Scene("adjoint_32k", p, np.zeros_like(p), physical_params(h, s, max_neighbors=512), 30, seed,
+                 notes="column compresses under 4 Jacobi iterations; max_neighbors 512")
 
 
 SCENES = {
