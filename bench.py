@@ -572,6 +572,8 @@ def main(argv=None):
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="run only the adjoint leg and print its object (a profiling aid, not a bench line)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -584,6 +586,12 @@ def main(argv=None):
 
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
+    if args.adjoint_only:
+        import torch
+
+        torch.cuda.set_device(local)
+        print(json.dumps({"adjoint": bench_adjoint(args, local)}))
+        return 0
     build = scenes.SCENES[args.workload]
     scene = build() if args.seed is None else build(args.seed)
     try:

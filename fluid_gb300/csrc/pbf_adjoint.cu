@@ -57,6 +57,17 @@ __device__ __forceinline__ float3 pair_rev(const PairD& p, float wsum, const flo
 }
 
 __device__ __forceinline__ float4 f4(const float3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+
+// what one neighbour contributes to a reverse pass, gathered ahead of its use
+struct F2 {
+  float4 a, b;
+};
+struct F3 {
+  float4 a, b, c;
+};
+struct F4 {
+  float4 a, b, c, d;
+};
 __device__ __forceinline__ int scene_of(const float4& x) { return __float_as_int(x.w); }
 
 // ---------------------------------------------------------------------------
@@ -89,8 +100,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_vort_a(const float4* __restrict__
   if (i >= n) return;
   const float4 xi = xs[i];
   float3 eta = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
-    const float4 xj = __ldg(&xs[j]);
+  for_each_neighbor_x<true>(i, n, hdr[i], words, xs, [&](uint32_t, const float4& xj) {
     const Pair p = pair_of(xi, xj, P.h, P.h2);
     eta = eta + p.r * (xj.w * p.s);
   });
@@ -122,9 +132,11 @@ __global__ void __launch_bounds__(BLOCK) k_adj_vort_b(const float4* __restrict__
   const float3 ebi = f3(eb[i]);
   float mwb = 0.f;
   float3 acc = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
-    const float4 xj = __ldg(&xs[j]);
-    const float3 ebj = f3(__ldg(&eb[j]));
+  for_each_neighbor_pf<4>(
+      i, n, hdr[i], words, [&](uint32_t j) { return F2{__ldg(&xs[j]), __ldg(&eb[j])}; },
+      [&](uint32_t, const F2& a) {
+    const float4 xj = a.a;
+    const float3 ebj = f3(a.b);
     const PairD p = pair_d(xi, xj, P.h, P.h2);
     mwb -= P.spiky_c * p.s * dot3(ebj, p.r);
     acc = acc + pair_rev(p, 0.f, ebi * xj.w - ebj * xi.w, P);
@@ -207,11 +219,14 @@ __global__ void __launch_bounds__(BLOCK) k_adj_xsph(const float4* __restrict__ x
   const float3 cbi = vbi * P.xsph_c;
   const float3 wbi = f3(wb[i]);
   float3 ub = vbi, acc = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
-    const float4 xj = __ldg(&xs[j]);
-    const float3 du = f3(__ldg(&disp[j])) * inv_dt - ui;
-    const float3 cbj = f3(__ldg(&gvo[j])) * P.xsph_c;
-    const float3 ws = wbi + f3(__ldg(&wb[j]));
+  for_each_neighbor_pf<2>(
+      i, n, hdr[i], words,
+      [&](uint32_t j) { return F4{__ldg(&xs[j]), __ldg(&disp[j]), __ldg(&gvo[j]), __ldg(&wb[j])}; },
+      [&](uint32_t, const F4& a) {
+    const float4 xj = a.a;
+    const float3 du = f3(a.b) * inv_dt - ui;
+    const float3 cbj = f3(a.c) * P.xsph_c;
+    const float3 ws = wbi + f3(a.d);
     const PairD p = pair_d(xi, xj, P.h, P.h2);
     const float W = P.poly6_c * (p.q * p.q * p.q);
     const float3 G = p.r * (P.spiky_c * p.s);
@@ -241,9 +256,11 @@ __global__ void __launch_bounds__(BLOCK) k_adj_lambda(const float4* __restrict__
   const float3 sbi = f3(ai);
   float qsum = 0.f, g2 = 0.f, lb = 0.f;
   float3 gs = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
-    const float4 xj = __ldg(&xs[j]);
-    const float3 sbj = f3(__ldg(&pl[j]));
+  for_each_neighbor_pf<4>(
+      i, n, hdr[i], words, [&](uint32_t j) { return F2{__ldg(&xs[j]), __ldg(&pl[j])}; },
+      [&](uint32_t, const F2& a) {
+    const float4 xj = a.a;
+    const float3 sbj = f3(a.b);
     const Pair p = pair_of(xi, xj, P.h, P.h2);
     const float3 rs = p.r * p.s;
     qsum += p.q * p.q * p.q;
@@ -279,10 +296,12 @@ __global__ void __launch_bounds__(BLOCK) k_adj_pos(const float4* __restrict__ xs
   const float wt = P.poly6_c * P.tis;
   const float ks = -P.scorr_k * P.tis;  // d s_corr / dW = ks * n (W tis)^(n-1)
   float3 acc = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
-    const float4 xj = __ldg(&xs[j]);
-    const float4 aj = __ldg(&pl[j]);
-    const float4 gj = __ldg(&gr[j]);
+  for_each_neighbor_pf<2>(
+      i, n, hdr[i], words, [&](uint32_t j) { return F3{__ldg(&xs[j]), __ldg(&pl[j]), __ldg(&gr[j])}; },
+      [&](uint32_t, const F3& nb) {
+    const float4 xj = nb.a;
+    const float4 aj = nb.b;
+    const float4 gj = nb.c;
     const PairD p = pair_d(xi, xj, P.h, P.h2);
     const float q3 = p.q * p.q * p.q;
     const float a = wt * q3;  // W tis

@@ -323,6 +323,57 @@ __device__ __forceinline__ void for_each_neighbor(int i, int n, const uint4 h,
   }
 }
 
+// As for_each_neighbor, with each neighbour's data gathered ahead of the computation:
+// load(j) returns what f needs of neighbour j; per round D list entries are decoded and
+// their loads issued before f runs on any of them, so every thread keeps D independent
+// gathers in flight. Calls f(j, load(j)) in the same (ascending) order. D = 2 or 4.
+template <int D, typename L, typename F>
+__device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h,
+                                                     const uint32_t* __restrict__ words, L&& load, F&& f) {
+  const int total = nbr_total(h);
+  const size_t sn = static_cast<size_t>(n);
+  const uint32_t* wp = words + i;
+  int k = 0;
+  if (D == 4) {
+    for (; k + 3 < total; k += 4) {
+      const uint32_t w0 = __ldg(wp), w1 = __ldg(wp + sn);
+      wp += 2 * sn;
+      const uint32_t j0 = nbr_decode(h, w0 & 0xffffu), j1 = nbr_decode(h, w0 >> 16);
+      const uint32_t j2 = nbr_decode(h, w1 & 0xffffu), j3 = nbr_decode(h, w1 >> 16);
+      const auto a0 = load(j0);
+      const auto a1 = load(j1);
+      const auto a2 = load(j2);
+      const auto a3 = load(j3);
+      f(j0, a0);
+      f(j1, a1);
+      f(j2, a2);
+      f(j3, a3);
+    }
+  }
+  for (; k + 1 < total; k += 2) {
+    const uint32_t w = __ldg(wp);
+    wp += sn;
+    const uint32_t j0 = nbr_decode(h, w & 0xffffu), j1 = nbr_decode(h, w >> 16);
+    const auto a0 = load(j0);
+    const auto a1 = load(j1);
+    f(j0, a0);
+    f(j1, a1);
+  }
+  if (k < total) {
+    const uint32_t j0 = nbr_decode(h, __ldg(wp) & 0xffffu);
+    f(j0, load(j0));
+  }
+}
+
+// The common case: the neighbours' x* (NC: through the read-only path, for buffers no
+// thread writes during the kernel), four in flight; calls f(j, x_j).
+template <bool NC, typename F>
+__device__ __forceinline__ void for_each_neighbor_x(int i, int n, const uint4 h,
+                                                    const uint32_t* __restrict__ words,
+                                                    const float4* xs, F&& f) {
+  for_each_neighbor_pf<4>(i, n, h, words, [&](uint32_t j) -> float4 { return NC ? __ldg(&xs[j]) : xs[j]; }, f);
+}
+
 // Pair geometry shared by every neighbour pass, branch-free:
 //   r = x_i - x_j, r2 = |r|^2,
 //   q = max(h2 - r2, 0)       so W = poly6_c * q^3     (particles.cpp:134-141)

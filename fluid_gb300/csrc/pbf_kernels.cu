@@ -291,8 +291,8 @@ __global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs, const uint4* __res
   const float4 xi = xs[i];
   float qsum = 0.f, g2 = 0.f;
   float3 gs = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
-    const Pair p = pair_of(xi, xs[j], P.h, P.h2);
+  for_each_neighbor_x<false>(i, n, hdr[i], words, xs, [&](uint32_t, const float4& xj) {
+    const Pair p = pair_of(xi, xj, P.h, P.h2);
     qsum += p.q * p.q * p.q;
     gs = gs + p.r * p.s;
     g2 += p.s * p.s * p.r2;
@@ -323,8 +323,7 @@ __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
   const float li = xi.w;  // lambda_i (k_lambda stores it in x*.w)
   const float wt = P.poly6_c * P.tis;
   float3 dp = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
-    const float4 xj = __ldg(&xs[j]);
+  for_each_neighbor_x<true>(i, n, hdr[i], words, xs, [&](uint32_t, const float4& xj) {
     const Pair p = pair_of(xi, xj, P.h, P.h2);
     const float a = wt * (p.q * p.q * p.q);  // W / W(dq)
     float an;
@@ -368,9 +367,14 @@ __global__ void __launch_bounds__(BLOCK) k_xsph(float4* xs, const float4* __rest
   const float3 vi = f3(disp[i]) * inv_dt;  // updateVelocity, particles.cpp:215-217
   float qsum = 0.f;
   float3 visc = make_float3(0.f, 0.f, 0.f), w = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
-    const Pair p = pair_of(xi, xs[j], P.h, P.h2);
-    const float3 vij = f3(__ldg(&disp[j])) * inv_dt - vi;
+  struct XD {
+    float4 x, d;
+  };
+  for_each_neighbor_pf<4>(
+      i, n, hdr[i], words, [&](uint32_t j) { return XD{xs[j], __ldg(&disp[j])}; },
+      [&](uint32_t, const XD& a) {
+    const Pair p = pair_of(xi, a.x, P.h, P.h2);
+    const float3 vij = f3(a.d) * inv_dt - vi;
     const float q3 = p.q * p.q * p.q;
     visc = visc + vij * q3;
     qsum += q3;
@@ -398,8 +402,7 @@ __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
   if (i >= n) return;
   const float4 xi = xs[i];
   float3 eta = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor(i, n, hdr[i], words, [&](uint32_t j) {
-    const float4 xj = __ldg(&xs[j]);
+  for_each_neighbor_x<true>(i, n, hdr[i], words, xs, [&](uint32_t, const float4& xj) {
     const Pair p = pair_of(xi, xj, P.h, P.h2);
     eta = eta + p.r * (xj.w * p.s);  // |omega_j| (k_xsph stores it in x*.w)
   });
