@@ -326,7 +326,7 @@ __device__ __forceinline__ void for_each_neighbor(int i, int n, const uint4 h,
 // As for_each_neighbor, with each neighbour's data gathered ahead of the computation:
 // load(j) returns what f needs of neighbour j; per round D list entries are decoded and
 // their loads issued before f runs on any of them, so every thread keeps D independent
-// gathers in flight. Calls f(j, load(j)) in the same (ascending) order. D = 2 or 4.
+// gathers in flight. Calls f(j, load(j)) in the same (ascending) order. D = 2, 4 or 8.
 template <int D, typename L, typename F>
 __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h,
                                                      const uint32_t* __restrict__ words, L&& load, F&& f) {
@@ -334,7 +334,33 @@ __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h
   const size_t sn = static_cast<size_t>(n);
   const uint32_t* wp = words + i;
   int k = 0;
-  if (D == 4) {
+  if (D == 8) {
+    for (; k + 7 < total; k += 8) {
+      const uint32_t w0 = __ldg(wp), w1 = __ldg(wp + sn), w2 = __ldg(wp + 2 * sn), w3 = __ldg(wp + 3 * sn);
+      wp += 4 * sn;
+      const uint32_t j0 = nbr_decode(h, w0 & 0xffffu), j1 = nbr_decode(h, w0 >> 16);
+      const uint32_t j2 = nbr_decode(h, w1 & 0xffffu), j3 = nbr_decode(h, w1 >> 16);
+      const uint32_t j4 = nbr_decode(h, w2 & 0xffffu), j5 = nbr_decode(h, w2 >> 16);
+      const uint32_t j6 = nbr_decode(h, w3 & 0xffffu), j7 = nbr_decode(h, w3 >> 16);
+      const auto a0 = load(j0);
+      const auto a1 = load(j1);
+      const auto a2 = load(j2);
+      const auto a3 = load(j3);
+      const auto a4 = load(j4);
+      const auto a5 = load(j5);
+      const auto a6 = load(j6);
+      const auto a7 = load(j7);
+      f(j0, a0);
+      f(j1, a1);
+      f(j2, a2);
+      f(j3, a3);
+      f(j4, a4);
+      f(j5, a5);
+      f(j6, a6);
+      f(j7, a7);
+    }
+  }
+  if (D >= 4) {
     for (; k + 3 < total; k += 4) {
       const uint32_t w0 = __ldg(wp), w1 = __ldg(wp + sn);
       wp += 2 * sn;

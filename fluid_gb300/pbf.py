@@ -9,13 +9,15 @@ the library has not been built.
 from __future__ import annotations
 
 import ctypes
+import os
 from pathlib import Path
 
 import numpy as np
 
 from .params import CParams, PbfParams
 
-LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpbf.so"
+# PBF_LIB, when set, names another build of the library (for comparing builds)
+LIB_PATH = Path(os.environ.get("PBF_LIB") or Path(__file__).resolve().parent / "_lib" / "libpbf.so")
 
 PBF_OK = 0
 ABI_VERSION = 2  # PBF_ABI_VERSION of include/pbf.h that these declarations follow
