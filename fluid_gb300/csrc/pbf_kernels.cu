@@ -348,7 +348,8 @@ __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
   const float li = xi.w;  // lambda_i (k_lambda stores it in x*.w)
   const float wt = P.poly6_c * P.tis;
   float3 dp = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor_x<true>(i, n, hdr[i], words, xs, [&](uint32_t, const float4& xj) {
+  for_each_neighbor_pf<8>(i, n, hdr[i], words, [&](uint32_t j) -> float4 { return __ldg(&xs[j]); },
+                          [&](uint32_t, const float4& xj) {
     const Pair p = pair_of(xi, xj, P.h, P.h2);
     const float a = wt * (p.q * p.q * p.q);  // W / W(dq)
     float an;
@@ -395,7 +396,7 @@ __global__ void __launch_bounds__(BLOCK) k_xsph(float4* xs, const float4* __rest
   struct XD {
     float4 x, d;
   };
-  for_each_neighbor_pf<4>(
+  for_each_neighbor_pf<8>(
       i, n, hdr[i], words, [&](uint32_t j) { return XD{xs[j], __ldg(&disp[j])}; },
       [&](uint32_t, const XD& a) {
     const Pair p = pair_of(xi, a.x, P.h, P.h2);
@@ -427,7 +428,8 @@ __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
   if (i >= n) return;
   const float4 xi = xs[i];
   float3 eta = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor_x<true>(i, n, hdr[i], words, xs, [&](uint32_t, const float4& xj) {
+  for_each_neighbor_pf<8>(i, n, hdr[i], words, [&](uint32_t j) -> float4 { return __ldg(&xs[j]); },
+                          [&](uint32_t, const float4& xj) {
     const Pair p = pair_of(xi, xj, P.h, P.h2);
     eta = eta + p.r * (xj.w * p.s);  // |omega_j| (k_xsph stores it in x*.w)
   });
