@@ -270,25 +270,31 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
       }
       const uint32_t gb = gbase[g];
       const uint32_t gbits = static_cast<uint32_t>(g) << kOffsetBits;
-      for (uint32_t j = start; j < end; ++j) {
-        if (j == static_cast<uint32_t>(i)) continue;
-        const float4 xj = __ldg(&xs[j]);
-        if (dist2_rn(xi, xj) <= P.h2) {
-          const uint32_t off = j - gb;
-          if (off > kOffsetMask) {
-            flags |= PBF_ERRBIT_ROW_CAPACITY;
-          } else if (total < cap) {
-            const uint32_t e = gbits | off;
-            if ((total & 1) == 0) {
-              word = e;
+      // the own slot splits the row: [start, i) and (i, end)
+      const uint32_t ui = static_cast<uint32_t>(i);
+      const uint32_t mid0 = ui < start ? start : (ui < end ? ui : end);
+      const uint32_t mid1 = ui < start ? start : (ui < end ? ui + 1 : end);
+      for (int half = 0; half < 2; ++half) {
+        const uint32_t a = half ? mid1 : start, b = half ? end : mid0;
+        for (uint32_t j = a; j < b; ++j) {
+          const float4 xj = __ldg(&xs[j]);
+          if (dist2_rn(xi, xj) <= P.h2) {
+            const uint32_t off = j - gb;
+            if (off > kOffsetMask) {
+              flags |= PBF_ERRBIT_ROW_CAPACITY;
+            } else if (total < cap) {
+              const uint32_t e = gbits | off;
+              if ((total & 1) == 0) {
+                word = e;
+              } else {
+                word |= e << 16;
+                *wptr = word;
+                wptr += n;
+              }
+              ++total;
             } else {
-              word |= e << 16;
-              *wptr = word;
-              wptr += n;
+              flags |= PBF_ERRBIT_NEIGHBOR_CAPACITY;
             }
-            ++total;
-          } else {
-            flags |= PBF_ERRBIT_NEIGHBOR_CAPACITY;
           }
         }
       }
