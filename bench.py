@@ -6,16 +6,21 @@ lattices, h = 0.0125, 4 Jacobi iterations, FP32), synthetic and seeded. A step i
 full PBF time step of every particle (Particles::timeStep, particles.cpp:250-297).
 
 * ``value``: particle-updates/s with the state resident in HBM, device time of exactly
-  K steps from CUDA events on the simulator's stream. Every timed step advances the
-  configured initial state (cell-sorted once, then restored from a device snapshot
-  between steps), so each step does the full work of one PBF step over the configured
-  input; the reference's formulas are not stable for long rollouts at this resolution.
+  K steps, each replayed as one CUDA graph, from CUDA events on the simulator's stream.
+  Every timed step advances the configured initial state (cell-sorted once, then
+  restored from a device snapshot between steps), so each step does the full work of
+  one PBF step over the configured input: with the configured tensile k = 0.1 the
+  reference's formulas blow the blocks apart within one step (FP64 restatement: median
+  displacement several particle spacings), so a rollout would not keep that work.
   Snapshot restore and an L2 flush (256 MiB write) run between steps, outside the events.
+* ``phases_ms_per_step``: the same K steps timed again, launched stream-ordered with
+  CUDA events between phases (``phases_pass``).
 * ``e2e``: the same metric through the C ABI with host buffers: per step
   pbf_set_state (H2D of positions and velocities from pinned memory), pbf_step, and
   pbf_get_positions + pbf_get_velocities (D2H), wall-clocked.
 * ``roofline``: the dominant kernel's algorithmic bytes per launch over its average
-  event-timed launch duration, against the measured HBM copy bandwidth.
+  event-timed launch duration in the phase pass, against the measured HBM copy
+  bandwidth.
 * ``cpu_baseline``: the reference's own step (built from its sources) on a bounded
   sample of the workload on the host cores, else the FP64 restatement.
 * ``--impl reference``: the reference CPU step alone, on the same config and metric.
@@ -431,10 +436,11 @@ def bench_ours(args, scene, world, rank, local):
     import torch
 
     from fluid_gb300 import pbf
-    from fluid_gb300.params import PBF_FLAG_STATS
+    from fluid_gb300.params import PBF_FLAG_GRAPH, PBF_FLAG_STATS
 
     torch.cuda.set_device(local)
-    prm = scene.params.with_(flags=PBF_FLAG_STATS)
+    # the timed region replays each step as one CUDA graph (events only around steps)
+    prm = scene.params.with_(flags=PBF_FLAG_STATS | PBF_FLAG_GRAPH)
     sim = pbf.Simulator(scene.pos, scene.vel, prm, device=local)
     n = sim.n
     dt = prm.dt
@@ -456,33 +462,51 @@ def bench_ours(args, scene, world, rank, local):
             gpu_index = int(vis.split(",")[local])
         except ValueError:
             pass
+
+    def timed_steps(s, st, steps):
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        barrier(world)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(st):
+            for k in range(steps):
+                s.restore()
+                flush.zero_()
+                starts[k].record(st)
+                s.step_async(dt, 1)
+                ends[k].record(st)
+        s.sync()
+        torch.cuda.synchronize()
+        barrier(world)
+        return [a.elapsed_time(z) for a, z in zip(starts, ends)]
+
     clocks = ClockSampler(gpu_index)
     time.sleep(0.3)
-    sim.set_profiling(True)
-    sim.reset_phase_times()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    barrier(world)
-    torch.cuda.synchronize()
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            sim.restore()
-            flush.zero_()
-            starts[k].record(stream)
-            sim.step_async(dt, 1)
-            ends[k].record(stream)
-    sim.sync()
-    torch.cuda.synchronize()
-    barrier(world)
+    step_ms = timed_steps(sim, stream, args.steps)
     clk = clocks.stop()
-    phases = sim.phase_times()
-    sim.set_profiling(False)
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = reduce_max(sum(step_ms), world)
     value = world * n * args.steps / (total_ms / 1e3)
     stats = sim.stats()
 
-    # dominant kernel (by device time in the timed region) and its roofline
+    # phase breakdown: the same K steps again, launched stream-ordered (no graph) with
+    # CUDA events between phases on the simulator's stream
+    psim = pbf.Simulator(scene.pos, scene.vel, scene.params.with_(flags=PBF_FLAG_STATS), device=local)
+    psim.set_tuning(**tuning)
+    psim.sort()
+    psim.snapshot()
+    pstream = torch.cuda.ExternalStream(psim.stream)
+    psim.set_profiling(True)
+    for _ in range(args.warmup):
+        psim.restore()
+        psim.step_async(dt, 1)
+    psim.sync()
+    psim.reset_phase_times()
+    prof_ms = timed_steps(psim, pstream, args.steps)
+    phases = psim.phase_times()
+    psim.set_profiling(False)
+    psim.close()
+
+    # dominant kernel (by device time in the phase pass) and its roofline
     peak, peak_kind = peaks()
     dom = max((k for k in phases if ALGO_BYTES.get(k, 0) > 0), key=lambda k: phases[k][0])
     dom_ms, dom_launches = phases[dom]
@@ -532,13 +556,15 @@ def bench_ours(args, scene, world, rank, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(scene),
+        "config": workload_config(scene, {"launch": "CUDA graph replay of each step"}),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": None if traffic is None else traffic * n,
                      "algo_bytes_per_launch": algo, "avg_launch_ms": per_launch_s * 1e3,
                      "step_frac": step_bytes / (total_ms / args.steps / 1e3) / 1e9 / peak},
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items()},
+        "phases_pass": {"launch": "stream-ordered with events between phases (no graph)",
+                        "ms_per_step": sum(prof_ms) / args.steps},
         "tuning": tuning,
         "gpu_launches": launches,
         "clocks": clk,

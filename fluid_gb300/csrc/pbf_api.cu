@@ -296,6 +296,12 @@ pbf_status Handle::collect_phase_times() {
 }
 
 void Handle::free_profiling() {
+  for (int q = 0; q < 2; ++q) {
+    for (auto& g : prof_graph[q])
+      if (g) cudaGraphExecDestroy(g);
+    prof_graph[q].clear();
+    prof_graph_count[q].clear();
+  }
   for (auto& set : prof_events)
     for (auto& e : set)
       if (e) cudaEventDestroy(e);
@@ -305,32 +311,59 @@ void Handle::free_profiling() {
   prof_used = 0;
 }
 
+// Capture one step (launch_step with the given marks) into an executable graph.
+static pbf_status capture_step(Handle* h, float dt, bool keep_pred, PhaseMarks* m, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  pbf_status st = h->cuda(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+  if (st != PBF_OK) return st;
+  cudaError_t le = launch_step(h->b, h->dp, h->tune, h->cur, dt, h->params.iters, keep_pred, h->stream, m);
+  cudaError_t ee = cudaStreamEndCapture(h->stream, &g);
+  if (le != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return h->cuda(le, "capture step");
+  }
+  st = h->cuda(ee, "end capture");
+  if (st != PBF_OK) return st;
+  st = h->cuda(cudaGraphInstantiate(out, g, 0), "instantiate graph");
+  cudaGraphDestroy(g);
+  return st;
+}
+
 pbf_status Handle::enqueue_steps(float dt, int nsteps) {
-  const bool use_graph = (params.flags & PBF_FLAG_GRAPH) != 0 && !profiling;
+  const bool use_graph = (params.flags & PBF_FLAG_GRAPH) != 0;
   const bool keep_pred = b.pred != nullptr;
+  const int it = params.iters;
+  const uint64_t per_step[kNumPhases] = {1, 3, 2, 1, 1, static_cast<uint64_t>(it), static_cast<uint64_t>(it),
+                                         1, 1, dp.stats ? 2u : 0u};
   for (int k = 0; k < nsteps; ++k) {
-    if (use_graph) {
-      if (graph_dt != dt) {
-        for (int q = 0; q < 2; ++q) {
-          if (graph[q]) cudaGraphExecDestroy(graph[q]);
-          graph[q] = nullptr;
-        }
-        graph_dt = dt;
+    if (use_graph && graph_dt != dt) {
+      drop_graphs();
+      graph_dt = dt;
+    }
+    if (use_graph && profiling) {
+      PhaseMarks m = next_marks();
+      m.in_graph = true;
+      const size_t set = prof_used;
+      if (prof_graph[cur].size() <= set) {
+        prof_graph[cur].resize(set + 1, nullptr);
+        prof_graph_count[cur].resize(set + 1, 0);
       }
+      if (!prof_graph[cur][set]) {
+        pbf_status st = capture_step(this, dt, keep_pred, &m, &prof_graph[cur][set]);
+        if (st != PBF_OK) return st;
+        prof_graph_count[cur][set] = m.count;
+      }
+      pbf_status st = cuda(cudaGraphLaunch(prof_graph[cur][set], stream), "cudaGraphLaunch");
+      if (st != PBF_OK) return st;
+      prof_count[prof_used++] = prof_graph_count[cur][set];
+      for (int q = 0; q < kNumPhases; ++q) phase_launches[q] += per_step[q];
+      if (prof_used >= 64) {
+        st = collect_phase_times();
+        if (st != PBF_OK) return st;
+      }
+    } else if (use_graph) {
       if (!graph[cur]) {
-        cudaGraph_t g = nullptr;
-        pbf_status st = cuda(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-        if (st != PBF_OK) return st;
-        cudaError_t le = launch_step(b, dp, tune, cur, dt, params.iters, keep_pred, stream);
-        cudaError_t ee = cudaStreamEndCapture(stream, &g);
-        if (le != cudaSuccess) {
-          if (g) cudaGraphDestroy(g);
-          return cuda(le, "capture step");
-        }
-        st = cuda(ee, "end capture");
-        if (st != PBF_OK) return st;
-        st = cuda(cudaGraphInstantiate(&graph[cur], g, 0), "instantiate graph");
-        cudaGraphDestroy(g);
+        pbf_status st = capture_step(this, dt, keep_pred, nullptr, &graph[cur]);
         if (st != PBF_OK) return st;
       }
       pbf_status st = cuda(cudaGraphLaunch(graph[cur], stream), "cudaGraphLaunch");
@@ -341,9 +374,6 @@ pbf_status Handle::enqueue_steps(float dt, int nsteps) {
           cuda(launch_step(b, dp, tune, cur, dt, params.iters, keep_pred, stream, &m), "launch step");
       if (st != PBF_OK) return st;
       prof_count[prof_used++] = m.count;
-      const int it = params.iters;
-      const uint64_t per_step[kNumPhases] = {1, 3, 2, 1, 1, static_cast<uint64_t>(it), static_cast<uint64_t>(it),
-                                             1, 1, dp.stats ? 2u : 0u};
       for (int q = 0; q < kNumPhases; ++q) phase_launches[q] += per_step[q];
       if (prof_used >= 256) {
         st = collect_phase_times();
@@ -364,6 +394,10 @@ void Handle::drop_graphs() {
   for (int q = 0; q < 2; ++q) {
     if (graph[q]) cudaGraphExecDestroy(graph[q]);
     graph[q] = nullptr;
+    for (auto& g : prof_graph[q])
+      if (g) cudaGraphExecDestroy(g);
+    prof_graph[q].clear();
+    prof_graph_count[q].clear();
   }
   graph_dt = -1.f;
 }
@@ -930,6 +964,10 @@ pbf_status pbf_autotune(pbf_handle* hh, double dt, int reps, pbf_tuning* out) {
   const double snap_time0 = h->snap_time;
   pbf_status st = pbf_snapshot(hh);
   if (st != PBF_OK) return st;
+  // candidates are timed launched stream-ordered (no graph), each with its own shapes
+  const int flags0 = h->params.flags;
+  h->params.flags &= ~PBF_FLAG_GRAPH;
+  h->drop_graphs();
   h->profiling = true;
   static const int kCand[4] = {64, 128, 256, 512};
   pbf::Tuning best = h->tune;
@@ -950,6 +988,7 @@ pbf_status pbf_autotune(pbf_handle* hh, double dt, int reps, pbf_tuning* out) {
       *reinterpret_cast<int*>(reinterpret_cast<char*>(&trial) +
                               (reinterpret_cast<char*>(f.field) - reinterpret_cast<char*>(&best))) = c;
       h->tune = trial;
+      h->drop_graphs();
       double ms[pbf::kNumPhases] = {};
       st = time_phases(h, static_cast<float>(d), 1, ms);  // warm the shape
       if (st == PBF_OK) st = time_phases(h, static_cast<float>(d), reps, ms);
@@ -967,6 +1006,7 @@ pbf_status pbf_autotune(pbf_handle* hh, double dt, int reps, pbf_tuning* out) {
   }
   h->tune = best;
   h->profiling = had_prof;
+  h->params.flags = flags0;
   pbf_status st2 = pbf_restore(hh);
   if (st == PBF_OK) st = st2;
   if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "sync");

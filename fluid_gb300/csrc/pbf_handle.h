@@ -45,6 +45,10 @@ struct Handle {
   std::vector<std::vector<int>> prof_phase;
   std::vector<int> prof_count;
   size_t prof_used = 0;
+  // with PBF_FLAG_GRAPH and profiling: one graph per event set and buffer parity, the
+  // phase events being event-record nodes of that graph
+  std::vector<cudaGraphExec_t> prof_graph[2];
+  std::vector<int> prof_graph_count[2];
   // device-side snapshot (pbf_snapshot / pbf_restore)
   float4* snap_pos = nullptr;
   float4* snap_vel = nullptr;

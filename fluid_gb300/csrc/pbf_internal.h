@@ -147,9 +147,13 @@ struct PhaseMarks {
   int* phase = nullptr;
   int count = 0;
   int cap = 0;
+  bool in_graph = false;  // recorded while capturing a graph: event-record nodes
   void mark(int ph, cudaStream_t s) {
     if (ev && count < cap) {
-      cudaEventRecord(ev[count], s);
+      if (in_graph)
+        cudaEventRecordWithFlags(ev[count], s, cudaEventRecordExternal);
+      else
+        cudaEventRecord(ev[count], s);
       phase[count] = ph;
       ++count;
     }

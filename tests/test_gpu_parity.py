@@ -177,6 +177,29 @@ def test_determinism_and_graph_replay(pbf):
             assert np.array_equal(a, b)
 
 
+def test_profiled_graph_replay_matches_and_times_every_phase(pbf):
+    """Profiling inside graph replay (phase events as graph nodes, one graph per event set
+    and buffer parity): same results as plain launches, and every phase timed."""
+    sc = scenes.block4096(3)
+    pos, vel = _f32(sc.pos), _f32(sc.vel)
+    ref = _run_gpu(pbf, pos, vel, sc.params.with_(flags=PBF_FLAG_STATS), steps=6)
+    with pbf.Simulator(pos, vel, sc.params.with_(flags=PBF_FLAG_STATS | PBF_FLAG_GRAPH)) as sim:
+        sim.set_profiling(True)
+        sim.time_step(sc.params.dt, 3)
+        sim.set_profiling(False)
+        sim.time_step(sc.params.dt, 1)
+        sim.set_profiling(True)
+        sim.time_step(sc.params.dt, 2)
+        ph = sim.phase_times()
+        out = (sim.positions(), sim.velocities(), sim.densities())
+    for a, b in zip(ref[:3], out):
+        assert np.array_equal(a, b)
+    for name in ("predict", "neighbors", "lambda", "deltap", "xsph", "vorticity"):
+        ms, launches = ph[name]
+        assert ms > 0 and launches > 0, name
+    assert ph["lambda"][1] == 5 * sc.params.iters
+
+
 def test_rollout_block4096_density_error(pbf, oracle_lib):
     """20-step config-1 rollout: density-constraint statistics against the oracle ensemble."""
     sc = scenes.block4096(1)
