@@ -89,6 +89,8 @@ struct Buffers {
   uint32_t* cell_count = nullptr;
   uint32_t* cell_start = nullptr;  // n_cells + 1
   uint32_t* scan_tmp = nullptr;    // block sums
+  uint32_t* big_cells = nullptr;   // cells over kSmallCell particles this step (worklist)
+  uint32_t* big_count = nullptr;   // entries in big_cells
   SceneDesc* scenes = nullptr;
   DevStats* stats = nullptr;
   unsigned int* err = nullptr;     // sticky PBF_ERRBIT_* word

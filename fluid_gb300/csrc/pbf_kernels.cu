@@ -28,7 +28,10 @@ namespace {
 constexpr int kScanItems = 4;
 constexpr int kScanThreads = 256;
 constexpr int kScanTile = kScanItems * kScanThreads;
-constexpr uint32_t kMaxSortedCell = 256;
+constexpr uint32_t kSmallCell = 32;       // cells up to this size: insertion sort by one thread
+constexpr uint32_t kMaxSortedCell = 4096;  // larger cells: rank sort by one block (in shared memory)
+constexpr int kBigSortThreads = 256;
+constexpr int kBigSortBlocks = 304;
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
@@ -162,15 +165,20 @@ __global__ void k_scatter(const uint32_t* __restrict__ key, const uint32_t* __re
   if (i < n) perm[cell_start[key[i]] + rank[i]] = static_cast<uint32_t>(i);
 }
 
-// Insertion sort of each cell's slots by original particle index, so the
-// cell order (hence every neighbour sum) is independent of atomic timing.
-// Cells above kMaxSortedCell particles keep the atomic order (bounded time).
+// Order each cell's slots by original particle index, so the cell order (hence every
+// neighbour sum) is independent of atomic timing. Cells up to kSmallCell particles are
+// insertion-sorted by one thread; larger ones go to a worklist for k_cellsort_big.
 __global__ void k_cellsort(const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ perm,
-                           const uint32_t* __restrict__ id, uint32_t m) {
+                           const uint32_t* __restrict__ id, uint32_t* __restrict__ big_cells,
+                           uint32_t* __restrict__ big_count, uint32_t m) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m) return;
   const uint32_t b = cell_start[c], e = cell_start[c + 1];
-  if (e - b < 2 || e - b > kMaxSortedCell) return;
+  if (e - b < 2) return;
+  if (e - b > kSmallCell) {
+    big_cells[atomicAdd(big_count, 1u)] = c;
+    return;
+  }
   for (uint32_t x = b + 1; x < e; ++x) {
     const uint32_t v = perm[x];
     const uint32_t kv = id[v];
@@ -180,6 +188,38 @@ __global__ void k_cellsort(const uint32_t* __restrict__ cell_start, uint32_t* __
       --y;
     }
     perm[y] = v;
+  }
+}
+
+// Rank sort of the worklist's cells, one block per cell: the rank of an element is the
+// number of the cell's elements with a smaller original index (indices are distinct).
+// Cells over kMaxSortedCell particles keep the atomic order (bounded time).
+__global__ void __launch_bounds__(kBigSortThreads) k_cellsort_big(const uint32_t* __restrict__ cell_start,
+                                                                 uint32_t* __restrict__ perm,
+                                                                 const uint32_t* __restrict__ id,
+                                                                 const uint32_t* __restrict__ big_cells,
+                                                                 const uint32_t* __restrict__ big_count) {
+  __shared__ uint32_t slot[kMaxSortedCell];
+  __shared__ uint32_t key[kMaxSortedCell];
+  const uint32_t cnt = *big_count;
+  for (uint32_t w = blockIdx.x; w < cnt; w += gridDim.x) {
+    const uint32_t c = big_cells[w];
+    const uint32_t b = cell_start[c], e = cell_start[c + 1];
+    const uint32_t m = e - b;
+    if (m > kMaxSortedCell) continue;  // uniform across the block
+    for (uint32_t t = threadIdx.x; t < m; t += blockDim.x) {
+      const uint32_t v = perm[b + t];
+      slot[t] = v;
+      key[t] = id[v];
+    }
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < m; t += blockDim.x) {
+      const uint32_t k = key[t];
+      uint32_t r = 0;
+      for (uint32_t u = 0; u < m; ++u) r += key[u] < k ? 1u : 0u;
+      perm[b + r] = slot[t];
+    }
+    __syncthreads();
   }
 }
 
@@ -697,7 +737,12 @@ cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& 
   k_scan_add<<<tiles, kScanThreads, 0, s>>>(b.cell_start, b.scan_tmp, m);
   if (mk) mk->mark(kPhaseScan, s);
   k_scatter<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(b.key, b.rank, b.cell_start, b.perm, n);
-  k_cellsort<<<blocks_for(m, t.block_misc), t.block_misc, 0, s>>>(b.cell_start, b.perm, b.id[cur], m);
+  e = cudaMemsetAsync(b.big_count, 0, sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  k_cellsort<<<blocks_for(m, t.block_misc), t.block_misc, 0, s>>>(b.cell_start, b.perm, b.id[cur], b.big_cells,
+                                                                   b.big_count, m);
+  k_cellsort_big<<<kBigSortBlocks, kBigSortThreads, 0, s>>>(b.cell_start, b.perm, b.id[cur], b.big_cells,
+                                                             b.big_count);
   if (mk) mk->mark(kPhaseSort, s);
   return cudaGetLastError();
 }

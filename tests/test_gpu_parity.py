@@ -165,6 +165,30 @@ def test_neighbor_sets_and_cells_bitexact(pbf, oracle_lib):
     assert rel_err(xs, ref["pred"]) < 1e-6
 
 
+def test_crowded_cells_sort_deterministically(pbf):
+    """600 particles inside about one cell of size h (a compressed clump): the cell sort
+    takes its block-wide path (cells over 32 particles); the step is bit-identical from run
+    to run and the neighbour sets match the host FP32 check."""
+    rng = np.random.default_rng(8)
+    prm = scenes.physical_params(0.1, 0.05, max_neighbors=1023,
+                                 flags=PBF_FLAG_STATS | PBF_FLAG_KEEP_PREDICTED)
+    pos = np.stack([rng.uniform(0.41, 0.49, 600), rng.uniform(0.01, 0.09, 600), rng.uniform(0.41, 0.49, 600)], 1)
+    pos = _f32(pos)
+    vel = np.zeros_like(pos)
+    runs = []
+    for _ in range(3):
+        with pbf.Simulator(pos, vel, prm) as sim:
+            sim.time_step(prm.dt, 1)
+            runs.append((sim.positions(), sim.velocities(), sim.densities(), sim.predicted(), sim.neighbors()))
+    for r in runs[1:]:
+        for a, b in zip(runs[0][:4], r[:4]):
+            assert np.array_equal(a, b)
+    off, ids = runs[0][4]
+    e_off, e_ids = neighbor_sets_fp32(runs[0][3], prm.h2)
+    assert np.array_equal(off, e_off) and np.array_equal(ids.astype(np.int64), e_ids)
+    assert np.diff(off).max() > 400
+
+
 def test_determinism_and_graph_replay(pbf):
     sc = scenes.block4096(2)
     pos, vel = _f32(sc.pos), _f32(sc.vel)
