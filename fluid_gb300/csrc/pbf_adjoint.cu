@@ -6,8 +6,8 @@
 // evaluated in gather form: the neighbour relation is symmetric, so particle i sums
 // the contributions of the pairs (i, j) and (j, i) itself and writes only its own
 // adjoints. Launch chain after the recording forward (I iterations):
-//   k_adj_in        adjoints of the outputs into cell order
-//   k_adj_vort_a    eta_i, the adjoints of omega_i (direct) and of eta_i
+//   k_adj_in        adjoints of the outputs into cell order; the adjoints of omega_i
+//                   (direct part) and of eta_i from the recorded eta
 //   k_adj_vort_b    |omega| adjoint, pair terms of eta
 //   k_adj_xsph      XSPH + vorticity pair terms, u = (x* - x) / dt, then the reverse of
 //                   the last iteration's collision
@@ -74,52 +74,39 @@ __device__ __forceinline__ int scene_of(const float4& x) { return __float_as_int
 // adjoints of the outputs into cell order
 // ---------------------------------------------------------------------------
 __global__ void k_adj_in(const uint32_t* __restrict__ id, const float* __restrict__ gx_out,
-                         const float* __restrict__ gv_out, float4* __restrict__ gxs, float4* __restrict__ gvo,
-                         float* __restrict__ r0, int n) {
+                         const float* __restrict__ gv_out, const float4* __restrict__ eta_rec,
+                         const float4* __restrict__ omega, float4* __restrict__ gxs, float4* __restrict__ gvo,
+                         float4* __restrict__ eb, float4* __restrict__ wb, float* __restrict__ r0, DevParams P,
+                         float dt, int n) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const uint32_t o = id[s];
   gxs[s] = gx_out ? make_float4(gx_out[3 * o], gx_out[3 * o + 1], gx_out[3 * o + 2], 0.f)
                   : make_float4(0.f, 0.f, 0.f, 0.f);
-  gvo[s] = gv_out ? make_float4(gv_out[3 * o], gv_out[3 * o + 1], gv_out[3 * o + 2], 0.f)
-                  : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float3 vb = gv_out ? make_float3(gv_out[3 * o], gv_out[3 * o + 1], gv_out[3 * o + 2])
+                           : make_float3(0.f, 0.f, 0.f);
+  gvo[s] = f4(vb, 0.f);
   r0[s] = 0.f;
-}
-
-// ---------------------------------------------------------------------------
-// vorticity confinement: v'' = v' + dt eps_v (eta / |eta|) x omega_i,
-// eta_i = sum_j |omega_j| G(r_ij)   (particles.cpp:236-248)
-// ---------------------------------------------------------------------------
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_adj_vort_a(const float4* __restrict__ xs, const float4* __restrict__ omega,
-                                                      const uint4* __restrict__ hdr,
-                                                      const uint32_t* __restrict__ words,
-                                                      const float4* __restrict__ gvo, float4* __restrict__ eb,
-                                                      float4* __restrict__ wb, DevParams P, float dt, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4 xi = xs[i];
-  float3 eta = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor_x<true>(i, n, hdr[i], words, xs, [&](uint32_t, const float4& xj) {
-    const Pair p = pair_of(xi, xj, P.h, P.h2);
-    eta = eta + p.r * (xj.w * p.s);
-  });
-  eta = eta * P.spiky_c;
+  // vorticity confinement v'' = v' + a (eta / |eta|) x omega, a = dt eps_v (particles.cpp:236-248):
+  // adjoints of omega (direct part) and of eta, from the eta the recording forward kept
+  const float3 eta = f3(eta_rec[s]);
   const float en = sqrtf(dot3(eta, eta));
   float3 wbar = make_float3(0.f, 0.f, 0.f), ebar = make_float3(0.f, 0.f, 0.f);
   if (en > kEps) {
     const float3 nh = eta * (1.0f / en);
     const float a = dt * P.vort_eps;
-    const float3 vb = f3(gvo[i]);
-    const float3 w = f3(omega[i]);
+    const float3 w = f3(omega[s]);
     wbar = cross3(vb, nh) * a;
     const float3 nb = cross3(w, vb) * a;
     ebar = (nb - nh * dot3(nb, nh)) * (1.0f / en);
   }
-  eb[i] = f4(ebar, 0.f);
-  wb[i] = f4(wbar, 0.f);
+  eb[s] = f4(ebar, 0.f);
+  wb[s] = f4(wbar, 0.f);
 }
 
+// ---------------------------------------------------------------------------
+// eta_i = sum_j |omega_j| G(r_ij)   (particles.cpp:236-248)
+// ---------------------------------------------------------------------------
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_adj_vort_b(const float4* __restrict__ xs, const float4* __restrict__ omega,
                                                       const uint4* __restrict__ hdr,
@@ -132,7 +119,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_vort_b(const float4* __restrict__
   const float3 ebi = f3(eb[i]);
   float mwb = 0.f;
   float3 acc = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor_pf<4>(
+  for_each_neighbor_pf<8>(
       i, n, hdr[i], words, [&](uint32_t j) { return F2{__ldg(&xs[j]), __ldg(&eb[j])}; },
       [&](uint32_t, const F2& a) {
     const float4 xj = a.a;
@@ -219,7 +206,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_xsph(const float4* __restrict__ x
   const float3 cbi = vbi * P.xsph_c;
   const float3 wbi = f3(wb[i]);
   float3 ub = vbi, acc = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor_pf<2>(
+  for_each_neighbor_pf<4>(
       i, n, hdr[i], words,
       [&](uint32_t j) { return F4{__ldg(&xs[j]), __ldg(&disp[j]), __ldg(&gvo[j]), __ldg(&wb[j])}; },
       [&](uint32_t, const F4& a) {
@@ -256,7 +243,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_lambda(const float4* __restrict__
   const float3 sbi = f3(ai);
   float qsum = 0.f, g2 = 0.f, lb = 0.f;
   float3 gs = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor_pf<4>(
+  for_each_neighbor_pf<8>(
       i, n, hdr[i], words, [&](uint32_t j) { return F2{__ldg(&xs[j]), __ldg(&pl[j])}; },
       [&](uint32_t, const F2& a) {
     const float4 xj = a.a;
@@ -296,7 +283,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_pos(const float4* __restrict__ xs
   const float wt = P.poly6_c * P.tis;
   const float ks = -P.scorr_k * P.tis;  // d s_corr / dW = ks * n (W tis)^(n-1)
   float3 acc = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor_pf<2>(
+  for_each_neighbor_pf<4>(
       i, n, hdr[i], words, [&](uint32_t j) { return F3{__ldg(&xs[j]), __ldg(&pl[j]), __ldg(&gr[j])}; },
       [&](uint32_t, const F3& nb) {
     const float4 xj = nb.a;
@@ -386,10 +373,8 @@ cudaError_t launch_adjoint(const Buffers& b, const DevParams& P, const Tuning& t
   F.gx_in = gx_in;
   F.gv_in = gv_in;
   F.n = b.n;
-  k_adj_in<<<blocks_for(n, 256), 256, 0, s>>>(b.id[B], gx_out, gv_out, tp.gxs, tp.gvo, tp.r0, n);
-  PBF_BLOCK_SWITCH(t.block_solve,
-                   k_adj_vort_a<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                       fin, b.omega, b.nbr_hdr, b.nbr_w, tp.gvo, tp.eb, tp.wb, P, dt, n));
+  k_adj_in<<<blocks_for(n, 256), 256, 0, s>>>(b.id[B], gx_out, gv_out, tp.eta, b.omega, tp.gxs, tp.gvo, tp.eb,
+                                              tp.wb, tp.r0, P, dt, n);
   PBF_BLOCK_SWITCH(t.block_solve,
                    k_adj_vort_b<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
                        fin, b.omega, b.nbr_hdr, b.nbr_w, tp.eb, tp.wb, tp.gxs, P, n));

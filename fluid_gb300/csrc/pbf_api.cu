@@ -203,7 +203,7 @@ pbf_status Handle::alloc_all() {
 }
 
 void Handle::free_tape() {
-  void* ptrs[] = {tape.x, tape.v, tape.xs, tape.dp, tape.gxs, tape.pl[0], tape.pl[1], tape.gr,
+  void* ptrs[] = {tape.x, tape.v, tape.xs, tape.dp, tape.eta, tape.gxs, tape.pl[0], tape.pl[1], tape.gr,
                   tape.gvo, tape.gx, tape.wb, tape.eb, tape.r0, tape.r0_part};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -221,7 +221,7 @@ pbf_status Handle::ensure_tape() {
     size_t bytes;
   } list[] = {
       {(void**)&tape.x, f4}, {(void**)&tape.v, f4}, {(void**)&tape.xs, f4 * (it + 1)},
-      {(void**)&tape.dp, f4 * (it ? it : 1)}, {(void**)&tape.gxs, f4}, {(void**)&tape.pl[0], f4},
+      {(void**)&tape.dp, f4 * (it ? it : 1)}, {(void**)&tape.eta, f4}, {(void**)&tape.gxs, f4}, {(void**)&tape.pl[0], f4},
       {(void**)&tape.pl[1], f4}, {(void**)&tape.gr, f4}, {(void**)&tape.gvo, f4}, {(void**)&tape.gx, f4},
       {(void**)&tape.wb, f4}, {(void**)&tape.eb, f4}, {(void**)&tape.r0, sizeof(float) * n},
       {(void**)&tape.r0_part, sizeof(double) * kAdjReduceBlocks},

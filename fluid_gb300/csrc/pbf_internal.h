@@ -108,6 +108,7 @@ struct Tape {
   float4* xs = nullptr;   // (iters + 1) n: x* before each iteration (w: lambda),
                           // then the final x* (w: |omega|)
   float4* dp = nullptr;   // iters n: requested displacement (w: collision record)
+  float4* eta = nullptr;  // vorticity location vector eta of the step
   float4* gxs = nullptr;  // adjoint of the current x*
   float4* pl[2] = {nullptr, nullptr};  // (adjoint of the unscaled delta-p sum, lambda), ping-pong
   float4* gr = nullptr;   // (sum of grad W / rho0, adjoint of rho)

@@ -469,7 +469,7 @@ __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
                                                 const uint4* __restrict__ hdr,
                                                 const uint32_t* __restrict__ words,
                                                 float4* __restrict__ vel, unsigned* __restrict__ err,
-                                                DevParams P, float dt, int n) {
+                                                float4* __restrict__ eta_rec, DevParams P, float dt, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 xi = xs[i];
@@ -480,6 +480,7 @@ __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
     eta = eta + p.r * (xj.w * p.s);  // |omega_j| (k_xsph stores it in x*.w)
   });
   eta = eta * P.spiky_c;
+  if (eta_rec) eta_rec[i] = make_float4(eta.x, eta.y, eta.z, 0.f);  // recording forward of the adjoint
   float3 v = f3(vel[i]);
   const float en = sqrtf(dot3(eta, eta));
   if (en > kEps) {
@@ -813,7 +814,8 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
   if (mk) mk->mark(kPhaseXsph, s);
   PBF_BLOCK_SWITCH(t.block_solve,
                    k_vort<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                       fin, b.pos[B], b.omega, b.nbr_hdr, b.nbr_w, b.vel[B], b.err, P, dt, n));
+                       fin, b.pos[B], b.omega, b.nbr_hdr, b.nbr_w, b.vel[B], b.err, rec ? tape->eta : nullptr,
+                       P, dt, n));
   if (mk) mk->mark(kPhaseVorticity, s);
   if (P.stats)
     k_stats<<<min(blocks_for(n, 256), 1216u), 256, 0, s>>>(b.rho, b.rho_iter0, b.nbr_hdr, b.stats, P.inv_rho0, n);

@@ -259,7 +259,7 @@ PBF_API const char* pbf_last_error(const pbf_handle* h);
  * The handle's state becomes the step's output (simulate_time is not advanced).
  * The work is enqueued on `stream` (a cudaStream_t, NULL for the legacy default
  * stream) without waiting; pbf_sync reports capacity and non-finite errors.
- * Device memory for the recording (about (48 + 32 iters) bytes per particle plus
+ * Device memory for the recording (about (64 + 32 iters) bytes per particle plus
  * 150 bytes of work arrays) is allocated on the first call. The sums are
  * evaluated in a fixed order: repeated calls give identical results.
  */
