@@ -153,7 +153,7 @@ void Handle::free_all() {
   }
   void* ptrs[] = {b.pos[0], b.pos[1], b.disp[0], b.disp[1], b.xs[0], b.xs[1], b.vel[0], b.vel[1],
                   b.omega, b.pred, b.lam, b.rho, b.rho_iter0, b.id[0], b.id[1], b.key, b.rank,
-                  b.perm, b.nbr_hdr, b.nbr_w, b.cell_count, b.cell_start, b.scan_tmp, b.big_cells, b.big_count, b.scenes,
+                  b.perm, b.nbr_hdr, b.nbr_w, b.cell_count, b.cell_start, b.scan_tmp, b.big_cells, b.big_count, b.scenes, b.stats_part,
                   b.stats, b.err, b.io, b.io2, scratch, snap_pos, snap_vel, snap_id};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -188,6 +188,7 @@ pbf_status Handle::alloc_all() {
       {(void**)&b.big_cells, sizeof(uint32_t) * (b.n_cells ? b.n_cells : 1)},
       {(void**)&b.big_count, sizeof(uint32_t)},
       {(void**)&b.scenes, sizeof(SceneDesc) * b.n_scenes}, {(void**)&b.stats, sizeof(DevStats)},
+      {(void**)&b.stats_part, sizeof(DevStats) * 256},
       {(void**)&b.err, sizeof(unsigned)}, {(void**)&b.io, 3 * sizeof(float) * n},
       {(void**)&b.io2, 3 * sizeof(float) * n},
   };

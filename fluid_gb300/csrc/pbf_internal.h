@@ -93,6 +93,7 @@ struct Buffers {
   uint32_t* big_count = nullptr;   // entries in big_cells
   SceneDesc* scenes = nullptr;
   DevStats* stats = nullptr;
+  DevStats* stats_part = nullptr;  // per-block partial records of the stats pass
   unsigned int* err = nullptr;     // sticky PBF_ERRBIT_* word
   float* io = nullptr;             // (n, 3) staging for host/device packed transfers
   float* io2 = nullptr;

@@ -496,86 +496,89 @@ __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
 }
 
 // Step statistics (the prints of particles.cpp:267-295 and the neighbour
-// alert of :168-172, as numbers): one pass over densities and list headers.
-__global__ void __launch_bounds__(256) k_stats(const float* __restrict__ rho, const float* __restrict__ rho0,
-                                               const uint4* __restrict__ hdr, DevStats* __restrict__ st,
-                                               float inv_rho0, int n) {
-  double r = 0.0, r0 = 0.0, es = 0.0;
-  float em = 0.f;
-  unsigned cmin = 0xffffffffu, cmax = 0u;
-  unsigned long long csum = 0ull, low = 0ull;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float x = rho[i];
-    r += x;
-    r0 += rho0[i];
-    const float e = fabsf(x * inv_rho0 - 1.0f);
-    es += e;
-    em = fmaxf(em, e);
-    const unsigned c = static_cast<unsigned>(nbr_total(hdr[i]));
-    cmin = min(cmin, c);
-    cmax = max(cmax, c);
-    csum += c;
-    low += c < static_cast<unsigned>(kNeighborAlert) ? 1ull : 0ull;
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    r += __shfl_down_sync(0xffffffffu, r, o);
-    r0 += __shfl_down_sync(0xffffffffu, r0, o);
-    es += __shfl_down_sync(0xffffffffu, es, o);
-    em = fmaxf(em, __shfl_down_sync(0xffffffffu, em, o));
-    cmin = min(cmin, __shfl_down_sync(0xffffffffu, cmin, o));
-    cmax = max(cmax, __shfl_down_sync(0xffffffffu, cmax, o));
-    csum += __shfl_down_sync(0xffffffffu, csum, o);
-    low += __shfl_down_sync(0xffffffffu, low, o);
-  }
-  __shared__ double sd[3][8];
-  __shared__ float sem[8];
-  __shared__ unsigned smin[8], smax[8];
-  __shared__ unsigned long long ssum[8], slow[8];
-  const unsigned w = threadIdx.x >> 5;
-  if (lane_id() == 0) {
-    sd[0][w] = r;
-    sd[1][w] = r0;
-    sd[2][w] = es;
-    sem[w] = em;
-    smin[w] = cmin;
-    smax[w] = cmax;
-    ssum[w] = csum;
-    slow[w] = low;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (unsigned k = 1; k < (blockDim.x >> 5); ++k) {
-      r += sd[0][k];
-      r0 += sd[1][k];
-      es += sd[2][k];
-      em = fmaxf(em, sem[k]);
-      cmin = min(cmin, smin[k]);
-      cmax = max(cmax, smax[k]);
-      csum += ssum[k];
-      low += slow[k];
-    }
-    atomicAdd(&st->rho_sum, r);
-    atomicAdd(&st->rho_iter0_sum, r0);
-    atomicAdd(&st->err_sum, es);
-    atomicMax(&st->err_max_bits, __float_as_uint(em));
-    atomicMin(&st->nbr_min, cmin);
-    atomicMax(&st->nbr_max, cmax);
-    atomicAdd(&st->nbr_sum, csum);
-    atomicAdd(&st->low_cnt, low);
-  }
+// alert of :168-172, as numbers): one pass over densities and list headers, reduced in
+// a fixed shape (kStatsBlocks partial records, then one block), so the sums are
+// deterministic and no block contends on an atomic.
+constexpr int kStatsBlocks = 256;
+
+__device__ __forceinline__ void stats_merge(DevStats& a, const DevStats& b) {
+  a.rho_sum += b.rho_sum;
+  a.rho_iter0_sum += b.rho_iter0_sum;
+  a.err_sum += b.err_sum;
+  a.err_max_bits = max(a.err_max_bits, b.err_max_bits);  // non-negative floats order as their bits
+  a.nbr_min = min(a.nbr_min, b.nbr_min);
+  a.nbr_max = max(a.nbr_max, b.nbr_max);
+  a.nbr_sum += b.nbr_sum;
+  a.low_cnt += b.low_cnt;
 }
 
-__global__ void k_stats_init(DevStats* st) {
-  st->rho_iter0_sum = 0.0;
-  st->rho_sum = 0.0;
-  st->err_sum = 0.0;
-  st->err_max_bits = 0u;
-  st->nbr_min = 0xffffffffu;
-  st->nbr_max = 0u;
-  st->nbr_sum = 0ull;
-  st->low_cnt = 0ull;
+__device__ __forceinline__ DevStats stats_shfl_down(const DevStats& a, int o) {
+  DevStats b;
+  b.rho_sum = __shfl_down_sync(0xffffffffu, a.rho_sum, o);
+  b.rho_iter0_sum = __shfl_down_sync(0xffffffffu, a.rho_iter0_sum, o);
+  b.err_sum = __shfl_down_sync(0xffffffffu, a.err_sum, o);
+  b.err_max_bits = __shfl_down_sync(0xffffffffu, a.err_max_bits, o);
+  b.nbr_min = __shfl_down_sync(0xffffffffu, a.nbr_min, o);
+  b.nbr_max = __shfl_down_sync(0xffffffffu, a.nbr_max, o);
+  b.nbr_sum = __shfl_down_sync(0xffffffffu, a.nbr_sum, o);
+  b.low_cnt = __shfl_down_sync(0xffffffffu, a.low_cnt, o);
+  return b;
 }
+
+// Reduces the block's records into thread 0 (blockDim.x a multiple of 32, at most 1024).
+__device__ __forceinline__ DevStats stats_block_reduce(DevStats a) {
+  __shared__ DevStats sw[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) stats_merge(a, stats_shfl_down(a, o));
+  const unsigned w = threadIdx.x >> 5;
+  if (lane_id() == 0) sw[w] = a;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (unsigned k = 1; k < (blockDim.x >> 5); ++k) stats_merge(a, sw[k]);
+  return a;
+}
+
+__device__ __forceinline__ DevStats stats_zero() {
+  DevStats a;
+  a.rho_sum = a.rho_iter0_sum = a.err_sum = 0.0;
+  a.err_max_bits = 0u;
+  a.nbr_min = 0xffffffffu;
+  a.nbr_max = 0u;
+  a.pad = 0u;
+  a.nbr_sum = a.low_cnt = 0ull;
+  return a;
+}
+
+__global__ void __launch_bounds__(256) k_stats(const float* __restrict__ rho, const float* __restrict__ rho0,
+                                               const uint4* __restrict__ hdr, DevStats* __restrict__ part,
+                                               float inv_rho0, int n) {
+  DevStats a = stats_zero();
+  float em = 0.f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float x = rho[i];
+    a.rho_sum += x;
+    a.rho_iter0_sum += rho0[i];
+    const float e = fabsf(x * inv_rho0 - 1.0f);
+    a.err_sum += e;
+    em = fmaxf(em, e);
+    const unsigned c = static_cast<unsigned>(nbr_total(hdr[i]));
+    a.nbr_min = min(a.nbr_min, c);
+    a.nbr_max = max(a.nbr_max, c);
+    a.nbr_sum += c;
+    a.low_cnt += c < static_cast<unsigned>(kNeighborAlert) ? 1ull : 0ull;
+  }
+  a.err_max_bits = __float_as_uint(em);
+  a = stats_block_reduce(a);
+  if (threadIdx.x == 0) part[blockIdx.x] = a;
+}
+
+__global__ void __launch_bounds__(kStatsBlocks) k_stats_final(const DevStats* __restrict__ part,
+                                                              DevStats* __restrict__ st) {
+  DevStats a = part[threadIdx.x];
+  a = stats_block_reduce(a);
+  if (threadIdx.x == 0) *st = a;
+}
+
 
 // ---------------------------------------------------------------------------
 // transfers between original order and cell order
@@ -757,8 +760,6 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
   const int A = cur, B = 1 - cur;
   const bool rec = tape != nullptr;
   if (mk) mk->mark(-1, s);
-  if (P.stats) k_stats_init<<<1, 1, 0, s>>>(b.stats);
-  if (mk) mk->mark(kPhaseStats, s);
   cudaError_t e = sort_into_cells(b, P, t, A, dt, true, s, mk, rec);
   if (e != cudaSuccess) return e;
   float4* xs0 = rec ? tape->xs : b.xs[0];
@@ -817,8 +818,10 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
                        fin, b.pos[B], b.omega, b.nbr_hdr, b.nbr_w, b.vel[B], b.err, rec ? tape->eta : nullptr,
                        P, dt, n));
   if (mk) mk->mark(kPhaseVorticity, s);
-  if (P.stats)
-    k_stats<<<min(blocks_for(n, 256), 1216u), 256, 0, s>>>(b.rho, b.rho_iter0, b.nbr_hdr, b.stats, P.inv_rho0, n);
+  if (P.stats) {
+    k_stats<<<kStatsBlocks, 256, 0, s>>>(b.rho, b.rho_iter0, b.nbr_hdr, b.stats_part, P.inv_rho0, n);
+    k_stats_final<<<1, kStatsBlocks, 0, s>>>(b.stats_part, b.stats);
+  }
   if (mk) mk->mark(kPhaseStats, s);
   return cudaGetLastError();
 }
