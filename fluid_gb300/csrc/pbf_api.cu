@@ -188,7 +188,7 @@ pbf_status Handle::alloc_all() {
       {(void**)&b.big_cells, sizeof(uint32_t) * (b.n_cells ? b.n_cells : 1)},
       {(void**)&b.big_count, sizeof(uint32_t)},
       {(void**)&b.scenes, sizeof(SceneDesc) * b.n_scenes}, {(void**)&b.stats, sizeof(DevStats)},
-      {(void**)&b.stats_part, sizeof(DevStats) * 256},
+      {(void**)&b.stats_part, sizeof(DevStats) * kStatsBlocks},
       {(void**)&b.err, sizeof(unsigned)}, {(void**)&b.io, 3 * sizeof(float) * n},
       {(void**)&b.io2, 3 * sizeof(float) * n},
   };

@@ -132,8 +132,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* __r
   if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
 }
 
+// zero_word (or null): a counter the following phases need at zero (the cell sort's worklist)
 __global__ void __launch_bounds__(1024) k_scan_sums(uint32_t* __restrict__ tile_sum, uint32_t tiles,
-                                                     uint32_t* __restrict__ start, uint32_t m) {
+                                                     uint32_t* __restrict__ start, uint32_t m,
+                                                     uint32_t* __restrict__ zero_word) {
+  if (zero_word && threadIdx.x == 0) *zero_word = 0u;
   uint32_t carry = 0;
   for (uint32_t b = 0; b < tiles; b += blockDim.x) {
     const uint32_t idx = b + threadIdx.x;
@@ -499,7 +502,6 @@ __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
 // alert of :168-172, as numbers): one pass over densities and list headers, reduced in
 // a fixed shape (kStatsBlocks partial records, then one block), so the sums are
 // deterministic and no block contends on an atomic.
-constexpr int kStatsBlocks = 256;
 
 __device__ __forceinline__ void stats_merge(DevStats& a, const DevStats& b) {
   a.rho_sum += b.rho_sum;
@@ -737,12 +739,10 @@ cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& 
   if (mk) mk->mark(kPhasePredict, s);
   const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
   k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(b.cell_count, b.cell_start, b.scan_tmp, m);
-  k_scan_sums<<<1, 1024, 0, s>>>(b.scan_tmp, tiles, b.cell_start, m);
+  k_scan_sums<<<1, 1024, 0, s>>>(b.scan_tmp, tiles, b.cell_start, m, b.big_count);
   k_scan_add<<<tiles, kScanThreads, 0, s>>>(b.cell_start, b.scan_tmp, m);
   if (mk) mk->mark(kPhaseScan, s);
   k_scatter<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(b.key, b.rank, b.cell_start, b.perm, n);
-  e = cudaMemsetAsync(b.big_count, 0, sizeof(uint32_t), s);
-  if (e != cudaSuccess) return e;
   k_cellsort<<<blocks_for(m, t.block_misc), t.block_misc, 0, s>>>(b.cell_start, b.perm, b.id[cur], b.big_cells,
                                                                    b.big_count, m);
   k_cellsort_big<<<kBigSortBlocks, kBigSortThreads, 0, s>>>(b.cell_start, b.perm, b.id[cur], b.big_cells,
@@ -895,7 +895,7 @@ cudaError_t launch_exclusive_scan(const uint32_t* count, uint32_t* start, uint32
                                   cudaStream_t s) {
   const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
   k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(count, start, tile_sums, m);
-  k_scan_sums<<<1, 1024, 0, s>>>(tile_sums, tiles, start, m);
+  k_scan_sums<<<1, 1024, 0, s>>>(tile_sums, tiles, start, m, nullptr);
   k_scan_add<<<tiles, kScanThreads, 0, s>>>(start, tile_sums, m);
   return cudaGetLastError();
 }
