@@ -121,7 +121,7 @@ struct Tape {
   double* r0_part = nullptr;  // block sums of r0
 };
 constexpr int kAdjReduceBlocks = 256;
-constexpr int kStatsBlocks = 1024;  // partial records of the step statistics pass
+constexpr int kStatsBlocks = 256;  // partial records of the step statistics pass
 
 // Launch shapes picked by the autotuner (threads per block per kernel family).
 struct Tuning {

@@ -31,7 +31,7 @@ constexpr int kScanTile = kScanItems * kScanThreads;
 constexpr uint32_t kSmallCell = 32;       // cells up to this size: insertion sort by one thread
 constexpr uint32_t kMaxSortedCell = 4096;  // larger cells: rank sort by one block (in shared memory)
 constexpr int kBigSortThreads = 256;
-constexpr int kBigSortBlocks = 304;
+constexpr int kBigSortBlocks = 64;
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
