@@ -430,6 +430,34 @@ __device__ __forceinline__ bool spiky_s(float r2, float h, float* s) {
   return true;
 }
 
+// Particles::estimateDensityAt (particles.cpp:446-453): sum of poly6 over all particles
+// (self included for a particle's own position), gathered from the 27 cells of size
+// >= h around p in the cell order of `pos` (cell_start of that order).
+__device__ __forceinline__ float density_at_point(const float3 p, const float4* __restrict__ pos,
+                                                  const uint32_t* __restrict__ cell_start, const SceneDesc& sc,
+                                                  const DevParams& P) {
+  const CellCoord cc = cell_of(p, sc, P.inv_cell);
+  const int x0 = cc.x > 0 ? cc.x - 1 : 0;
+  const int x1 = cc.x + 1 < sc.dim[0] ? cc.x + 1 : sc.dim[0] - 1;
+  float qsum = 0.f;
+  for (int r = 0; r < 9; ++r) {
+    const int z = cc.z + r / 3 - 1, y = cc.y + r % 3 - 1;
+    if (z < 0 || z >= sc.dim[2] || y < 0 || y >= sc.dim[1]) continue;
+    const uint32_t row = sc.cell_off + static_cast<uint32_t>((z * sc.dim[1] + y) * sc.dim[0]);
+    const uint32_t e = __ldg(&cell_start[row + x1 + 1]);
+    for (uint32_t j = __ldg(&cell_start[row + x0]); j < e; ++j) {
+      const float4 xj = __ldg(&pos[j]);
+      const float3 d = make_float3(xj.x - p.x, xj.y - p.y, xj.z - p.z);
+      const float r2 = dot3(d, d);
+      if (r2 < P.h2) {
+        const float q = P.h2 - r2;
+        qsum += q * q * q;
+      }
+    }
+  }
+  return P.poly6_c * qsum;
+}
+
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
 // Instantiates a neighbour-pass kernel launch for the tuned block size.

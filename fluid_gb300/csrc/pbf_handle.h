@@ -57,6 +57,7 @@ struct Handle {
   uint64_t snap_steps = 0;
   double snap_time = 0;
   Tape tape;                 // recording + work arrays of the adjoint (first use)
+  SurfTable* surf_table_dev = nullptr;  // marching-cubes table (first pbf_surface)
   double phase_ms[kNumPhases] = {};
   uint64_t phase_launches[kNumPhases] = {};
 

@@ -123,6 +123,23 @@ struct Tape {
 constexpr int kAdjReduceBlocks = 256;
 constexpr int kStatsBlocks = 256;  // partial records of the step statistics pass
 
+// Marching-cubes triangulation table (pbf_surface.cu): for every cube configuration
+// (bit k set when corner k is below the iso level) the crossing edges, the triangle
+// count and the triangles as edge triples.
+struct SurfTable {
+  uint16_t edges[256];
+  uint8_t ntri[256];
+  int8_t tri[256][15];
+};
+// The surface grid of Particles::getSurfacePrims: cubes [x1, min(hi, x1 + step)] with
+// x1 = lo + i step, i = 0 .. nc - 1 per axis (nc = (int)((hi - lo) / step) + 1).
+struct SurfGrid {
+  double lo[3], hi[3], step;
+  int nc[3];
+};
+void build_table(SurfTable* t);
+const SurfTable& surf_table();
+
 // Launch shapes picked by the autotuner (threads per block per kernel family).
 struct Tuning {
   int block_predict = 256;
@@ -204,5 +221,15 @@ cudaError_t launch_exclusive_scan(const uint32_t* count, uint32_t* start, uint32
 uint32_t exclusive_scan_tiles(uint32_t m);
 cudaError_t launch_density_at(const Buffers& b, const DevParams& p, int cur, size_t m,
                               const float* pts, float* out, cudaStream_t s);
+// ---- surface (pbf_surface.cu), on the cell-sorted state in buffers cur ----
+// field: (nc+1)^3 corner values; count: per-cube triangle counts; first: their exclusive
+// scan (first[cubes] = total); tile_sums: exclusive_scan_tiles(cubes) entries.
+cudaError_t launch_surface_count(const Buffers& b, const DevParams& p, int cur, const SurfGrid& g, float iso,
+                                 const SurfTable* tab, float* field, uint32_t* count, uint32_t* first,
+                                 uint32_t* tile_sums, cudaStream_t s);
+// Triangles with index < cap: 9 floats of vertices and 9 of vertex normals each.
+cudaError_t launch_surface_emit(const Buffers& b, const DevParams& p, int cur, const SurfGrid& g, float iso,
+                                const SurfTable* tab, const float* field, const uint32_t* first, float* xyz,
+                                float* nrm, uint32_t cap, cudaStream_t s);
 
 }  // namespace pbf

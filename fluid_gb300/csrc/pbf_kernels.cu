@@ -698,27 +698,7 @@ __global__ void k_density_at(const float4* __restrict__ pos, const uint32_t* __r
                              float* __restrict__ out, DevParams P, int m) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= m) return;
-  const SceneDesc& sc = scenes[0];
-  const float3 p = make_float3(pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]);
-  const CellCoord cc = cell_of(p, sc, P.inv_cell);
-  float qsum = 0.f;
-  for (int r = 0; r < 9; ++r) {
-    const int z = cc.z + r / 3 - 1, y = cc.y + r % 3 - 1;
-    if (z < 0 || z >= sc.dim[2] || y < 0 || y >= sc.dim[1]) continue;
-    const uint32_t row = sc.cell_off + static_cast<uint32_t>((z * sc.dim[1] + y) * sc.dim[0]);
-    const int x0 = cc.x > 0 ? cc.x - 1 : 0;
-    const int x1 = cc.x + 1 < sc.dim[0] ? cc.x + 1 : sc.dim[0] - 1;
-    for (uint32_t j = cell_start[row + x0]; j < cell_start[row + x1 + 1]; ++j) {
-      const float4 xj = __ldg(&pos[j]);
-      const float3 d = make_float3(xj.x - p.x, xj.y - p.y, xj.z - p.z);
-      const float r2 = dot3(d, d);
-      if (r2 < P.h2) {
-        const float qq = P.h2 - r2;
-        qsum += qq * qq * qq;
-      }
-    }
-  }
-  out[q] = P.poly6_c * qsum;
+  out[q] = density_at_point(make_float3(pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]), pos, cell_start, scenes[0], P);
 }
 
 inline unsigned blocks_for(size_t n, int block) { return static_cast<unsigned>((n + block - 1) / block); }

@@ -20,7 +20,7 @@ from .params import CParams, PbfParams
 LIB_PATH = Path(os.environ.get("PBF_LIB") or Path(__file__).resolve().parent / "_lib" / "libpbf.so")
 
 PBF_OK = 0
-ABI_VERSION = 2  # PBF_ABI_VERSION of include/pbf.h that these declarations follow
+ABI_VERSION = 3  # PBF_ABI_VERSION of include/pbf.h that these declarations follow
 STATUS = {0: "PBF_OK", 1: "PBF_ERR_INVALID", 2: "PBF_ERR_CUDA", 3: "PBF_ERR_TIMEOUT",
           4: "PBF_ERR_NONFINITE", 5: "PBF_ERR_CAPACITY", 6: "PBF_ERR_NOMEM"}
 
@@ -93,6 +93,8 @@ def _declare(L):
         "pbf_phase_name": (ctypes.c_char_p, [ctypes.c_int]),
         "pbf_density_noalloc": (st, [P, sz, P, P, P]),
         "pbf_adjoint_step_device": (st, [P, ctypes.c_double, P, P, P, P, P, P, P, P, P, P]),
+        "pbf_surface": (st, [P, ctypes.c_double, ctypes.c_double, P, P, P, P, sz, P]),
+        "pbf_mc_table": (None, [P, P, P]),
         "pbf_size": (sz, [P]),
         "pbf_num_scenes": (ctypes.c_int, [P]),
         "pbf_last_error": (ctypes.c_char_p, [P]),
@@ -116,6 +118,16 @@ def lib():
             raise ImportError(f"{LIB_PATH} has ABI version {L.pbf_abi_version()}, expected {ABI_VERSION}: rebuild it")
         _lib = L
     return _lib
+
+
+def mc_table():
+    """The marching-cubes triangulation table of pbf_surface: (edges[256] u16, ntri[256] u8,
+    tri[256, 15] i8 as edge triples)."""
+    edges = np.zeros(256, dtype=np.uint16)
+    ntri = np.zeros(256, dtype=np.uint8)
+    tri = np.zeros((256, 15), dtype=np.int8)
+    lib().pbf_mc_table(_ptr(edges), _ptr(ntri), _ptr(tri))
+    return edges, ntri, tri
 
 
 def default_params_c() -> CParams:
@@ -246,6 +258,25 @@ class Simulator:
         self._check(lib().pbf_adjoint_step_device(
             self._h, dt, opt(pos_ptr), opt(vel_ptr), opt(gx_out_ptr), opt(gv_out_ptr), P(gx_in_ptr),
             P(gv_in_ptr), P(g_rho0_ptr), opt(pos_out_ptr), opt(vel_out_ptr), opt(stream)))
+
+    def surface(self, iso: float | None = None, step: float | None = None, lo=None, hi=None):
+        """Particles::getSurfacePrims (particles.cpp:352-385) on the current state: the
+        marching-cubes surface of the density field as (xyz, nrm), each (T, 3, 3) float32.
+        Defaults are updateSurface's (iso 0.95 rest density, step 0.5 h) and the
+        reference's fixed bounds [-1, 1] x [0, 1.5] x [-1, 1]."""
+        iso = 0.95 * self.params.rest_density if iso is None else float(iso)
+        step = 0.5 * self.params.h if step is None else float(step)
+        lo_a = None if lo is None else np.ascontiguousarray(lo, dtype=np.float64)
+        hi_a = None if hi is None else np.ascontiguousarray(hi, dtype=np.float64)
+        count = ctypes.c_size_t(0)
+        self._check(lib().pbf_surface(self._h, iso, step, _ptr(lo_a), _ptr(hi_a), None, None, 0,
+                                      ctypes.byref(count)))
+        t = count.value
+        xyz = np.zeros((max(t, 1), 3, 3), dtype=np.float32)
+        nrm = np.zeros((max(t, 1), 3, 3), dtype=np.float32)
+        self._check(lib().pbf_surface(self._h, iso, step, _ptr(lo_a), _ptr(hi_a), _ptr(xyz), _ptr(nrm), t,
+                                      ctypes.byref(count)))
+        return xyz[:t], nrm[:t]
 
     def estimate_densities(self) -> np.ndarray:
         """Particles::estimateDensities (particles.cpp:440-444): self term included."""

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define PBF_ABI_VERSION 2
+#define PBF_ABI_VERSION 3
 
 #if defined(__GNUC__)
 #define PBF_API __attribute__((visibility("default")))
@@ -267,6 +267,33 @@ PBF_API pbf_status pbf_adjoint_step_device(pbf_handle* h, double dt, const float
                                            const float* gx_out, const float* gv_out, float* gx_in,
                                            float* gv_in, double* g_rho0, float* xyz_out, float* vel_out,
                                            void* stream);
+
+/*
+ * pbf_surface -- Particles::getSurfacePrims (particles.cpp:352-385; updateSurface,
+ * :387-395, calls it with isolevel = 0.95 rest_density and step = 0.5 H) on the
+ * current state: a marching-cubes surface of the density field estimateDensityAt
+ * (:446-453) over the grid of cubes [x1, min(hi, x1 + step)], x1 = lo + i step,
+ * i = 0 .. (int)((hi - lo) / step) per axis, visited x outer, then y, then z; corners,
+ * edges and edge vertices as generateGridCell (:309-323) and vertexInterp
+ * (marching.cpp); vertex normals the normalized central differences of the field at
+ * +-0.001 (getVertexNormal, :399-412). The triangulation of each cube configuration is
+ * this library's table (pbf_mc_table), which closes the surface across cubes.
+ * lo / hi NULL: the reference's fixed bounds [-1, 1] x [0, 1.5] x [-1, 1]
+ * (:330-349). Scene 0 of a batch. xyz and nrm are HOST arrays of 9 floats per
+ * triangle (3 vertices); the first min(cap, total) triangles are written and *count
+ * receives the total (cap = 0 to query).
+ */
+PBF_API pbf_status pbf_surface(pbf_handle* h, double isolevel, double step, const double* lo, const double* hi,
+                               float* xyz, float* nrm, size_t cap, size_t* count);
+
+/*
+ * pbf_mc_table -- the triangulation table pbf_surface uses (no GPU needed): for each of
+ * the 256 cube configurations (bit k set when corner k is below the iso level; corners
+ * and edges numbered as generateGridCell and polygonise number them) the crossing-edge
+ * mask (edges[256]), the triangle count (ntri[256], at most 5) and the triangles as edge
+ * triples (tri[256 * 15]). Any pointer may be NULL.
+ */
+PBF_API void pbf_mc_table(uint16_t* edges, uint8_t* ntri, int8_t* tri);
 
 #define PBF_NOALLOC_MAX_PARTICLES 65536
 #define PBF_NOALLOC_MAX_CELLS 262144

@@ -68,6 +68,9 @@ def lib(fp32: bool = False, adjoint: bool = False):
         L.orc_estimate_density_at.argtypes = [P, ctypes.c_int64, P, ctypes.c_int64, P, P, ctypes.c_int]
         L.orc_estimate_density_at.restype = ctypes.c_int
         L.orc_max_threads.restype = ctypes.c_int
+        L.orc_surface.argtypes = [P, ctypes.c_int64, P, ctypes.c_double, ctypes.c_double, P, P, P, P, P, P, P,
+                                  ctypes.c_int64, ctypes.c_int]
+        L.orc_surface.restype = ctypes.c_int64
         _libs[path] = L
     return _libs[path]
 
@@ -199,6 +202,37 @@ def rollout_adjoint(pos, vel, params: PbfParams, steps: int, gx, gv, dt: float |
         a = step_adjoint(xs[s], vs[s], params, gx, gv, dt=dt, threads=threads)
         gx, gv, g0 = a["gx"], a["gv"], g0 + a["grho0"]
     return {"gx": gx, "gv": gv, "grho0": g0, "pos": xs[-1], "vel": vs[-1]}
+
+
+def surface(pos, params: PbfParams, ntri, tri, iso: float | None = None, step: float | None = None,
+            lo=(-1.0, 0.0, -1.0), hi=(1.0, 1.5, 1.0), threads: int = 0) -> dict:
+    """FP64 Particles::getSurfacePrims (particles.cpp:352-385) with the given triangulation
+    table (ntri[256], tri[256 * 15]); defaults are updateSurface's (iso 0.95 rest
+    density, step 0.5 h) and the reference's fixed bounds. Returns xyz / nrm (T, 3, 3)
+    and the cube index of every triangle."""
+    L = lib()
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    iso = 0.95 * params.rest_density if iso is None else iso
+    step = 0.5 * params.h if step is None else step
+    lo = np.ascontiguousarray(lo, dtype=np.float64)
+    hi = np.ascontiguousarray(hi, dtype=np.float64)
+    ntri = np.ascontiguousarray(ntri, dtype=np.uint8)
+    tri = np.ascontiguousarray(tri, dtype=np.int8)
+    cp = params.to_c()
+
+    def run(cap):
+        xyz = np.zeros((max(cap, 1), 3, 3))
+        nrm = np.zeros((max(cap, 1), 3, 3))
+        cube = np.zeros(max(cap, 1), dtype=np.int64)
+        total = L.orc_surface(ctypes.byref(cp), pos.shape[0], _ptr(pos), iso, step, _ptr(lo), _ptr(hi), _ptr(ntri),
+                              _ptr(tri), _ptr(xyz), _ptr(nrm), _ptr(cube), cap, threads)
+        if total < 0:
+            raise RuntimeError("orc_surface failed")
+        return total, xyz, nrm, cube
+
+    total, *_ = run(0)
+    total, xyz, nrm, cube = run(int(total))
+    return {"xyz": xyz[:total], "nrm": nrm[:total], "cube": cube[:total]}
 
 
 def max_threads() -> int:

@@ -637,3 +637,107 @@ int orc_estimate_density_at(const pbf_params* prm, int64_t n, const double* pos,
   free(c);
   return 0;
 }
+
+/* ---- surface (Particles::getSurfacePrims, particles.cpp:352-385) ------------------- */
+
+/* estimateDensityAt, particles.cpp:446-453: poly6 summed over every particle in index order */
+static real density_at(const ctx_t* c, int64_t n, const v3* x, v3 p) {
+  real d = 0.0;
+  for (int64_t i = 0; i < n; i++) d += poly6(c, vsub(x[i], p));
+  return d;
+}
+
+/* vertexInterp (marching.cpp) */
+static v3 vertex_interp(real iso, v3 p1, v3 p2, real v1, real v2) {
+  if (fabs(iso - v1) < 0.00001) return p1;
+  if (fabs(iso - v2) < 0.00001) return p2;
+  if (fabs(v1 - v2) < 0.00001) return p1;
+  real mu = (iso - v1) / (v2 - v1);
+  return V(p1.x + mu * (p2.x - p1.x), p1.y + mu * (p2.y - p1.y), p1.z + mu * (p2.z - p1.z));
+}
+
+/* getVertexNormal, particles.cpp:399-412 (GRADIENT_EPS = 0.001, :16) */
+static v3 vertex_normal(const ctx_t* c, int64_t n, const v3* x, v3 p) {
+  const real e = 0.001;
+  v3 g = V(density_at(c, n, x, V(p.x - e, p.y, p.z)) - density_at(c, n, x, V(p.x + e, p.y, p.z)),
+           density_at(c, n, x, V(p.x, p.y - e, p.z)) - density_at(c, n, x, V(p.x, p.y + e, p.z)),
+           density_at(c, n, x, V(p.x, p.y, p.z - e)) - density_at(c, n, x, V(p.x, p.y, p.z + e)));
+  if (vnorm(g) > 0) return unit(g);
+  return g;
+}
+
+/*
+ * The surface of the density field of `pos` with the caller's triangulation table
+ * (ntri[256], tri[256 * 15] as edge triples; corners and edges numbered as
+ * generateGridCell, particles.cpp:309-323, and polygonise, marching.cpp). The loops,
+ * corner points (x2 = min(hi, x1 + step)), corner values and edge vertices follow the
+ * reference; cubes in its order (x outer, y, z inner). Writes the first `cap`
+ * triangles (9 doubles of vertices and 9 of normals each) and the cube index of each
+ * (ix * ncy + iy) * ncz + iz; returns the total count, or -1 when out of memory.
+ */
+int64_t orc_surface(const pbf_params* prm, int64_t n, const double* pos, double iso, double step, const double* lo,
+                    const double* hi, const uint8_t* ntri, const int8_t* tri, double* xyz, double* nrm, int64_t* cube,
+                    int64_t cap, int nthreads) {
+  set_threads(nthreads);
+  ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+  v3* x = to_v3(pos, n);
+  if (!c || !x) return -1;
+  make_ctx(c, prm);
+  int steps[3], nc[3];
+  for (int a = 0; a < 3; a++) {
+    steps[a] = (int)((hi[a] - lo[a]) / step);
+    nc[a] = steps[a] + 1;
+  }
+  const int64_t ncubes = (int64_t)nc[0] * nc[1] * nc[2];
+  int* cnt = (int*)malloc(sizeof(int) * (size_t)(ncubes ? ncubes : 1));
+  int* cfg = (int*)malloc(sizeof(int) * (size_t)(ncubes ? ncubes : 1));
+  double* vals = (double*)malloc(sizeof(double) * 8 * (size_t)(ncubes ? ncubes : 1));
+  v3* pts = (v3*)malloc(sizeof(v3) * 8 * (size_t)(ncubes ? ncubes : 1));
+  if (!cnt || !cfg || !vals || !pts) return -1;
+  static const int corner[8][3] = {{0, 0, 0}, {0, 1, 0}, {1, 1, 0}, {1, 0, 0},
+                                   {0, 0, 1}, {0, 1, 1}, {1, 1, 1}, {1, 0, 1}};
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t q = 0; q < ncubes; q++) {
+    const int iz = (int)(q % nc[2]), iy = (int)((q / nc[2]) % nc[1]), ix = (int)(q / ((int64_t)nc[2] * nc[1]));
+    const real x1 = lo[0] + ix * step, y1 = lo[1] + iy * step, z1 = lo[2] + iz * step;
+    const real x2 = smin(hi[0], x1 + step), y2 = smin(hi[1], y1 + step), z2 = smin(hi[2], z1 + step);
+    const real xs[2] = {x1, x2}, ys[2] = {y1, y2}, zs[2] = {z1, z2};
+    int ci = 0;
+    for (int k = 0; k < 8; k++) {
+      v3 p = V(xs[corner[k][0]], ys[corner[k][1]], zs[corner[k][2]]);
+      pts[8 * q + k] = p;
+      vals[8 * q + k] = density_at(c, n, x, p);
+      if (vals[8 * q + k] < iso) ci |= 1 << k;
+    }
+    cfg[q] = ci;
+    cnt[q] = ntri[ci];
+  }
+  static const int edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
+                                  {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+  int64_t total = 0;
+  for (int64_t q = 0; q < ncubes; q++) {
+    for (int t = 0; t < cnt[q]; t++, total++) {
+      if (total >= cap) continue;
+      for (int v = 0; v < 3; v++) {
+        const int e = tri[15 * cfg[q] + 3 * t + v];
+        const int a = edge[e][0], b = edge[e][1];
+        v3 p = vertex_interp(iso, pts[8 * q + a], pts[8 * q + b], vals[8 * q + a], vals[8 * q + b]);
+        v3 m = vertex_normal(c, n, x, p);
+        xyz[9 * total + 3 * v] = p.x;
+        xyz[9 * total + 3 * v + 1] = p.y;
+        xyz[9 * total + 3 * v + 2] = p.z;
+        nrm[9 * total + 3 * v] = m.x;
+        nrm[9 * total + 3 * v + 1] = m.y;
+        nrm[9 * total + 3 * v + 2] = m.z;
+      }
+      if (cube) cube[total] = q;
+    }
+  }
+  free(cnt);
+  free(cfg);
+  free(vals);
+  free(pts);
+  free(x);
+  free(c);
+  return total;
+}

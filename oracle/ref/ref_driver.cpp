@@ -24,7 +24,9 @@
 // flags: 2 = dump neighbour lists of the last step, 4 = run
 // Particles::estimateDensities() (src/particles.cpp:440-444) before stepping,
 // 8 = restart: every step starts again from the input state (a fresh
-// Particles built untimed), so `seconds` times K steps of the same input.
+// Particles built untimed), so `seconds` times K steps of the same input,
+// 16 = surface: after the steps, the triangles of the reference's surface
+// (appended: i64 ntri, f64 xyz[9 ntri], f64 nrm[9 ntri], i64 cube[ntri]).
 // open_mask: bit per box face to leave out (0 x-lo, 1 x-hi, 2 y-lo, 3 y-hi,
 // 4 z-lo, 5 z-hi).
 #include <chrono>
@@ -38,7 +40,7 @@
 #include <unordered_map>
 #include <vector>
 
-#include "particles.h"
+#include "particles.h"  // includes marching.h (polygonise), which has no include guard
 #include "ref_params.h"
 #include "static_scene/marching_triangle.h"
 
@@ -252,6 +254,44 @@ int main(int argc, char** argv) {
       offsets[i + 1] = static_cast<int64_t>(idx.size());
     }
   }
+  // flag 16: the loop of Particles::getSurfacePrims (src/particles.cpp:352-385), which
+  // builds MarchingTriangle primitives whose vertices are private, run over the
+  // reference's own generateGridCell, polygonise (src/marching.cpp) and
+  // getVertexNormal, with updateSurface's arguments (src/particles.cpp:387-395):
+  // isolevel ISO_LEVEL_REST_DENSITY_RATIO (0.95, :14) x rest density, step
+  // FSTEPSIZE_RATIO (0.5, :18) x H.
+  std::vector<double> sxyz, snrm;
+  std::vector<int64_t> scube;
+  if (flags & 16) {
+    std::cout.rdbuf(sink.rdbuf());
+    const double iso = 0.95 * rest_density, fstep = pbf_ref_h * 0.5;
+    const double xmin = P.getParticlesAxisMin(0), ymin = P.getParticlesAxisMin(1), zmin = P.getParticlesAxisMin(2);
+    const double xmax = P.getParticlesAxisMax(0), ymax = P.getParticlesAxisMax(1), zmax = P.getParticlesAxisMax(2);
+    const int xsteps = (int)((xmax - xmin) / fstep), ysteps = (int)((ymax - ymin) / fstep),
+              zsteps = (int)((zmax - zmin) / fstep);
+    for (int ix = 0; ix <= xsteps; ix++)
+      for (int iy = 0; iy <= ysteps; iy++)
+        for (int iz = 0; iz <= zsteps; iz++) {
+          const double x1 = xmin + ix * fstep, x2 = std::min(xmax, x1 + fstep);
+          const double y1 = ymin + iy * fstep, y2 = std::min(ymax, y1 + fstep);
+          const double z1 = zmin + iz * fstep, z2 = std::min(zmax, z1 + fstep);
+          GridCell grid = P.generateGridCell(x1, x2, y1, y2, z1, z2);
+          std::vector<TriangleVertices*> tris = polygonise(grid, iso);
+          for (TriangleVertices* t : tris) {
+            for (int v = 0; v < 3; v++) {
+              Vector3D q = t->p[v];
+              Vector3D nq = P.getVertexNormal(q);
+              for (int k = 0; k < 3; k++) {
+                sxyz.push_back(q[k]);
+                snrm.push_back(nq[k]);
+              }
+            }
+            scube.push_back((static_cast<int64_t>(ix) * (ysteps + 1) + iy) * (zsteps + 1) + iz);
+            delete t;
+          }
+        }
+    std::cout.rdbuf(old_out);
+  }
   std::ofstream out(argv[2], std::ios::binary);
   out.write("PBFREFO1", 8);
   wr(out, &n, 1);
@@ -264,5 +304,12 @@ int main(int argc, char** argv) {
   wr(out, offsets.data(), offsets.size());
   wr(out, idx.data(), idx.size());
   wr(out, &seconds, 1);
+  if (flags & 16) {
+    const int64_t nt = static_cast<int64_t>(scube.size());
+    wr(out, &nt, 1);
+    wr(out, sxyz.data(), sxyz.size());
+    wr(out, snrm.data(), snrm.size());
+    wr(out, scube.data(), scube.size());
+  }
   return out ? 0 : 3;
 }

@@ -23,11 +23,14 @@ def available() -> bool:
 
 
 def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool = False,
-        load_density: bool = False, restart: bool = False, timeout: float | None = None) -> dict:
+        load_density: bool = False, restart: bool = False, timeout: float | None = None,
+        surface: bool = False) -> dict:
     """Run ``steps`` reference steps. ``params`` is a fluid_gb300.params.PbfParams.
 
     ``restart``: every step starts again from (pos, vel); ``seconds`` then times
-    ``steps`` steps of the same input.
+    ``steps`` steps of the same input. ``surface``: also the triangles of the
+    reference's surface after the steps (Particles::getSurfacePrims with
+    updateSurface's arguments): ``surf_xyz`` / ``surf_nrm`` (T, 3, 3), ``surf_cube``.
 
     The reference hard-codes gravity on -y, the clip planes z=1 / y=1.49 and the
     clamp box (particles.cpp:57-83, 180); params that disagree are rejected.
@@ -48,7 +51,7 @@ def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool 
     pos = np.ascontiguousarray(pos, dtype=np.float64)
     vel = np.ascontiguousarray(vel, dtype=np.float64)
     n = pos.shape[0]
-    flags = (2 if neighbors else 0) | (4 if load_density else 0) | (8 if restart else 0)
+    flags = (2 if neighbors else 0) | (4 if load_density else 0) | (8 if restart else 0) | (16 if surface else 0)
     with tempfile.TemporaryDirectory() as td:
         fin = Path(td) / "in.bin"
         fout = Path(td) / "out.bin"
@@ -87,4 +90,11 @@ def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool 
     out["nbr_offsets"] = take(np.int64, n + 1)
     out["nbr_idx"] = take(np.int64, nnz)
     (out["seconds"],) = struct.unpack_from("<d", buf, off)
+    off += 8
+    if surface:
+        (nt,) = struct.unpack_from("<q", buf, off)
+        off += 8
+        out["surf_xyz"] = take(np.float64, 9 * nt).reshape(nt, 3, 3)
+        out["surf_nrm"] = take(np.float64, 9 * nt).reshape(nt, 3, 3)
+        out["surf_cube"] = take(np.int64, nt)
     return out
