@@ -14,6 +14,7 @@
 //   p.timeStep(dt); p.timeStep();         // timeStep(double), timeStep()
 //   p.ps[i]->getPosition() / getNewPosition() / getLatestDensityEstimate()
 //   p.ps[i]->velocity, getDensityBasedColor(), p.estimateDensityAt(pos)
+//   p.updateSurface(); p.surface; p.getSurfacePrims(iso, step)   // marching cubes
 //
 // Differences, by design: the collider is the axis-aligned box of the pbf_params
 // (the reference casts rays against a BVH of scene triangles; `bvh` is kept as an
@@ -69,6 +70,14 @@ class Particle {
   double rest_density_;
 };
 
+// One triangle of the density-field surface with its vertex normals (the data of the
+// reference's MarchingTriangle, static_scene/marching_triangle.h).
+template <class V>
+struct SurfaceTriangle {
+  V p[3];
+  V n[3];
+};
+
 template <class V, class C = Rgba>
 class Particles {
  public:
@@ -78,6 +87,7 @@ class Particles {
   void* bvh = nullptr;  // the reference's BVHAccel*; the GPU collider is params().box_*
   double simulate_time = 0.0;
   const double rest_density;
+  std::vector<SurfaceTriangle<V>> surface;  // the reference's `surface` (MarchingTriangle primitives)
   bool surfaceUpToTimestep = false;
 
   explicit Particles(double rest_density_ = 1000.0, const pbf_params* params = nullptr, int device = 0)
@@ -136,6 +146,34 @@ class Particles {
     float out = 0.f;
     check(pbf_estimate_density_at(h_, 1, q, &out));
     return out;
+  }
+
+  // particles.cpp:352-385: the marching-cubes surface of the density field over the
+  // reference's fixed bounds [-1, 1] x [0, 1.5] x [-1, 1] (lo / hi override them).
+  std::vector<SurfaceTriangle<V>> getSurfacePrims(double isolevel, double fStepSize, const double* lo = nullptr,
+                                                  const double* hi = nullptr) {
+    std::vector<SurfaceTriangle<V>> out;
+    if (ps.empty()) return out;
+    ensure_handle();
+    size_t total = 0;
+    check(pbf_surface(h_, isolevel, fStepSize, lo, hi, nullptr, nullptr, 0, &total));
+    std::vector<float> xyz(9 * total), nrm(9 * total);
+    if (total) check(pbf_surface(h_, isolevel, fStepSize, lo, hi, xyz.data(), nrm.data(), total, &total));
+    out.resize(total);
+    for (size_t t = 0; t < total; ++t)
+      for (int v = 0; v < 3; ++v) {
+        const size_t k = 9 * t + 3 * v;
+        out[t].p[v] = V(xyz[k], xyz[k + 1], xyz[k + 2]);
+        out[t].n[v] = V(nrm[k], nrm[k + 1], nrm[k + 2]);
+      }
+    return out;
+  }
+
+  // particles.cpp:387-395: isolevel 0.95 rest density, step 0.5 H, once per time step.
+  void updateSurface() {
+    if (surfaceUpToTimestep) return;
+    surface = getSurfacePrims(0.95 * rest_density, 0.5 * prm_.h);
+    surfaceUpToTimestep = true;
   }
 
   const pbf_params& params() const { return prm_; }

@@ -13,7 +13,9 @@
 //   -d T  simulate T seconds, dumping every frame (the -d windowless mode)
 //
 // A frame dump is <dir>/frame_NNNNNN.bin: "PBFFRAME", int64 n, float64 time,
-// float32 positions (n, 3), float32 densities (n).
+// float32 positions (n, 3), float32 densities (n). With --surface every frame also
+// writes <dir>/frame_NNNNNN.obj, the surface updateSurface builds for the path tracer
+// (particles.cpp:387-395; vertices with their normals), in place of the rendered image.
 #include <cerrno>
 #include <cstdint>
 #include <cstdio>
@@ -46,19 +48,42 @@ struct Options {
   bool parse_only = false;
   bool quiet = false;
   bool graph = false;
+  bool surface = false;
 };
 
 void usage() {
   std::fprintf(stderr,
-               "usage: pbf_run -p particles.xml [-k keys] [-d seconds] [-o dir] [--graph] [--quiet]\n"
+               "usage: pbf_run -p particles.xml [-k keys] [-d seconds] [-o dir] [--graph] [--surface] [--quiet]\n"
                "       pbf_run -p particles.xml --parse-only\n"
                "  keys: m = one step, c = one second, g / h = one second with a frame dump per step\n");
 }
 
 int frame_no = 0;
 
+bool dump_surface = false;
+
+bool write_obj(Sim& sim, const std::string& path) {
+  sim.surfaceUpToTimestep = false;
+  sim.updateSurface();
+  std::FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) return false;
+  for (const auto& t : sim.surface)
+    for (int v = 0; v < 3; ++v) std::fprintf(f, "v %.7g %.7g %.7g\n", t.p[v].x, t.p[v].y, t.p[v].z);
+  for (const auto& t : sim.surface)
+    for (int v = 0; v < 3; ++v) std::fprintf(f, "vn %.7g %.7g %.7g\n", t.n[v].x, t.n[v].y, t.n[v].z);
+  for (size_t t = 0; t < sim.surface.size(); ++t) {
+    const size_t a = 3 * t + 1;
+    std::fprintf(f, "f %zu//%zu %zu//%zu %zu//%zu\n", a, a, a + 1, a + 1, a + 2, a + 2);
+  }
+  return std::fclose(f) == 0;
+}
+
 bool dump(Sim& sim, const std::string& dir) {
   char name[64];
+  if (dump_surface) {
+    std::snprintf(name, sizeof(name), "/frame_%06d.obj", frame_no);
+    if (!write_obj(sim, dir + name)) return false;
+  }
   std::snprintf(name, sizeof(name), "/frame_%06d.bin", frame_no++);
   std::FILE* f = std::fopen((dir + name).c_str(), "wb");
   if (!f) return false;
@@ -110,6 +135,7 @@ int main(int argc, char** argv) {
     else if (a == "--parse-only") o.parse_only = true;
     else if (a == "--quiet") o.quiet = true;
     else if (a == "--graph") o.graph = true;
+    else if (a == "--surface") o.surface = true;
     else {
       usage();
       return 2;
@@ -132,6 +158,7 @@ int main(int argc, char** argv) {
   }
   pbf_params prm = pf.params;
   if (o.graph) prm.flags |= PBF_FLAG_GRAPH;
+  dump_surface = o.surface;
   try {
     Sim sim(pf.rest_density, &prm);
     sim.set_verbose(!o.quiet);

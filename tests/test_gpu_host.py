@@ -68,3 +68,39 @@ def test_reference_fixture_keys(pbf_run, tmp_path):
     assert r.stderr.count("Time: ") == 1 + 63
     assert r.stdout.count("avg rho: ") == 64
     assert "Time: 0 => 0.016" in r.stderr
+
+
+def read_obj(path):
+    v, vn, f = [], [], []
+    for line in Path(path).read_text().splitlines():
+        if line.startswith("v "):
+            v.append([float(t) for t in line.split()[1:]])
+        elif line.startswith("vn "):
+            vn.append([float(t) for t in line.split()[1:]])
+        elif line.startswith("f "):
+            f.append([int(t.split("//")[0]) - 1 for t in line.split()[1:]])
+    return np.array(v), np.array(vn), np.array(f)
+
+
+def test_surface_dumps_match_the_surface_call(pbf_run, tmp_path):
+    """pbf_run --surface writes the surface updateSurface builds (the reference's rendering
+    input) for every dumped frame; it is the Simulator.surface of the same state."""
+    from fluid_gb300 import pbf
+
+    g = np.load(GOLDEN / "surface_p_default_0step.npz")
+    prm = params_from_json(str(g["params"]))
+    pos = g["pos"].astype(np.float32).astype(np.float64)
+    f = tmp_path / "p.xml"
+    scenes.write_xml(f, pos, np.zeros_like(pos), prm.rest_density, prm)
+    out = tmp_path / "frames"
+    r = subprocess.run([pbf_run, "-p", str(f), "-d", str(prm.dt * 0.5), "-o", str(out), "--surface", "--quiet"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    objs = sorted(out.glob("frame_*.obj"))
+    assert len(objs) == 2
+    v, vn, fc = read_obj(objs[0])
+    with pbf.Simulator(pos, np.zeros_like(pos), prm.with_(rest_density=float(np.float32(prm.rest_density)))) as sim:
+        xyz, nrm = sim.surface()
+    assert len(fc) == len(xyz) > 100
+    assert np.abs(v.reshape(-1, 3, 3) - xyz).max() < 1e-5
+    assert np.abs(vn.reshape(-1, 3, 3) - nrm).max() < 1e-5
