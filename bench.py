@@ -432,6 +432,47 @@ def bench_adjoint(args, local, steps: int = 30, big_steps: int = 5) -> dict:
             "target_ratio": 3.0}
 
 
+def bench_surface(sim, prm) -> dict:
+    """The marching-cubes surface (pbf_surface) of the workload's configured state over the
+    collider box at updateSurface's settings (iso 0.95 rest density, step 0.5 h): one call,
+    wall-clocked after a warm-up call (cell sort of the state, corner field, classify,
+    scan, emit with normals, D2H of the triangles)."""
+    import ctypes
+
+    from fluid_gb300 import pbf
+
+    L = pbf.lib()
+    iso, step = 0.95 * prm.rest_density, 0.5 * prm.h
+    lo = np.ascontiguousarray(prm.box_lo, dtype=np.float64)
+    hi = np.ascontiguousarray(prm.box_hi, dtype=np.float64)
+    count = ctypes.c_size_t(0)
+    sim.restore()
+    rc = L.pbf_surface(sim._h, iso, step, lo.ctypes.data_as(pbf.P), hi.ctypes.data_as(pbf.P), None, None, 0,
+                       ctypes.byref(count))
+    if rc:
+        raise RuntimeError(L.pbf_last_error(sim._h).decode())
+    t = count.value
+    xyz = np.zeros((max(t, 1), 9), dtype=np.float32)
+    nrm = np.zeros((max(t, 1), 9), dtype=np.float32)
+    times = []
+    for _ in range(3):
+        sim.restore()
+        sim.sync()
+        t0 = time.perf_counter()
+        rc = L.pbf_surface(sim._h, iso, step, lo.ctypes.data_as(pbf.P), hi.ctypes.data_as(pbf.P),
+                           xyz.ctypes.data_as(pbf.P), nrm.ctypes.data_as(pbf.P), t, ctypes.byref(count))
+        times.append(time.perf_counter() - t0)
+        if rc:
+            raise RuntimeError(L.pbf_last_error(sim._h).decode())
+    cubes = 1
+    for a in range(3):
+        cubes *= int((prm.box_hi[a] - prm.box_lo[a]) / step) + 1
+    ms = min(times[1:]) * 1e3
+    return {"workload": "surface of the configured state over the collider box", "iso": iso, "step": step,
+            "cubes": cubes, "triangles": t, "ms": ms, "cubes_per_s": cubes / (ms / 1e3),
+            "timing": "wall clock of one pbf_surface call with host output, best of 2 after a warm-up"}
+
+
 def bench_ours(args, scene, world, rank, local):
     import torch
 
@@ -487,6 +528,7 @@ def bench_ours(args, scene, world, rank, local):
     total_ms = reduce_max(sum(step_ms), world)
     value = world * n * args.steps / (total_ms / 1e3)
     stats = sim.stats()
+    surface = bench_surface(sim, prm) if not args.no_surface else None
 
     # phase breakdown: the same K steps again, launched stream-ordered (no graph) with
     # CUDA events between phases on the simulator's stream
@@ -568,11 +610,19 @@ def bench_ours(args, scene, world, rank, local):
         "tuning": tuning,
         "gpu_launches": launches,
         "clocks": clk,
+        "pair_rate": {"neighbour_pairs_per_step": stats["mean_neighbors"] * n * (2 * prm.iters + 2),
+                      "pairs_per_s": stats["mean_neighbors"] * n * (2 * prm.iters + 2) / (total_ms / args.steps / 1e3),
+                      "passes": 2 * prm.iters + 2,
+                      "note": "every pass over the fixed neighbour sets (lambda and delta-p per iteration, XSPH, "
+                              "vorticity) evaluates each (i, j) from i's side; the build's candidate tests are "
+                              "not counted"},
         "stats": {"mean_density_over_rho0": stats["mean_density"] / prm.rest_density,
                   "mean_neighbors": stats["mean_neighbors"], "max_neighbors": stats["max_neighbors"]},
     }
     if e2e:
         line["e2e"] = e2e
+    if surface:
+        line["surface"] = surface
     if not args.no_batched:
         line["batched"] = bench_batched(args, local)
     if not args.no_adjoint:
@@ -598,6 +648,7 @@ def main(argv=None):
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-surface", action="store_true")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="run only the adjoint leg and print its object (a profiling aid, not a bench line)")
     args = ap.parse_args(argv)
