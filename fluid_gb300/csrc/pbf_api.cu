@@ -86,6 +86,7 @@ bool make_dev_params(const pbf_params& p, DevParams* d, double* cell_out, std::s
   }
   std::memset(d, 0, sizeof(*d));
   const double cell = std::sqrt(p.h2) * 1.001;
+  *d = DevParams();
   d->h = static_cast<float>(p.h);
   d->h2 = static_cast<float>(p.h2);
   d->cell = static_cast<float>(cell);
@@ -161,6 +162,8 @@ void Handle::free_all() {
   free_tape();
   if (surf_table_dev) cudaFree(surf_table_dev);
   surf_table_dev = nullptr;
+  if (mesh_dev) cudaFree(mesh_dev);
+  mesh_dev = nullptr;
   snap_pos = snap_vel = nullptr;
   snap_id = nullptr;
   snap_valid = false;
@@ -598,6 +601,7 @@ pbf_status pbf_adjoint_step_device(pbf_handle* hh, double dt, const float* xyz, 
   const double d = dt > 0 ? dt : h->params.dt;
   if (!(d > 0) || !std::isfinite(d)) return h->fail(PBF_ERR_INVALID, "dt must be positive");
   if (!g_rho0) return h->fail(PBF_ERR_INVALID, "g_rho0 is NULL");
+  if (h->dp.n_mesh > 0) return h->fail(PBF_ERR_INVALID, "the adjoint step supports the box collider only");
   if (h->b.n && (!gx_in || !gv_in)) return h->fail(PBF_ERR_INVALID, "gx_in / gv_in is NULL");
   pbf::DeviceGuard g(h->device);
   pbf_status st = h->ensure_tape();
@@ -720,6 +724,55 @@ pbf_status pbf_estimate_densities(pbf_handle* hh, float* rho) {
   st = h->cuda(pbf::launch_density_self(h->b, h->dp, h->tune, h->cur, h->b.rho, h->stream), "density");
   if (st != PBF_OK) return st;
   return download(h, nullptr, nullptr, rho);
+}
+
+pbf_status pbf_set_collider_mesh(pbf_handle* hh, size_t n, const float* tri) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (n > static_cast<size_t>(pbf::kMaxMeshTriangles))
+    return h->fail(PBF_ERR_INVALID, "at most 1024 collider triangles");
+  if (n && !tri) return h->fail(PBF_ERR_INVALID, "tri is NULL");
+  std::vector<float4> packed(4 * n);
+  for (size_t t = 0; t < n; ++t) {
+    double p[3][3];
+    for (int v = 0; v < 3; ++v)
+      for (int k = 0; k < 3; ++k) {
+        p[v][k] = tri[9 * t + 3 * v + k];
+        if (!std::isfinite(p[v][k])) return h->fail(PBF_ERR_INVALID, "collider triangles must be finite");
+      }
+    double e1[3], e2[3];
+    for (int k = 0; k < 3; ++k) {
+      e1[k] = p[1][k] - p[0][k];
+      e2[k] = p[2][k] - p[0][k];
+    }
+    const double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    const double cn = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    if (!(cn > 0)) return h->fail(PBF_ERR_INVALID, "degenerate collider triangle");
+    packed[4 * t] = make_float4(static_cast<float>(p[0][0]), static_cast<float>(p[0][1]), static_cast<float>(p[0][2]), 0.f);
+    packed[4 * t + 1] = make_float4(static_cast<float>(e1[0]), static_cast<float>(e1[1]), static_cast<float>(e1[2]), 0.f);
+    packed[4 * t + 2] = make_float4(static_cast<float>(e2[0]), static_cast<float>(e2[1]), static_cast<float>(e2[2]), 0.f);
+    packed[4 * t + 3] = make_float4(static_cast<float>(c[0] / cn), static_cast<float>(c[1] / cn),
+                                    static_cast<float>(c[2] / cn), 0.f);
+  }
+  pbf::DeviceGuard g(h->device);
+  pbf_status st = h->cuda(cudaStreamSynchronize(h->stream), "sync");
+  if (st != PBF_OK) return st;
+  if (h->mesh_dev) cudaFree(h->mesh_dev);
+  h->mesh_dev = nullptr;
+  h->dp.n_mesh = 0;
+  h->dp.mesh = nullptr;
+  if (n) {
+    st = h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->mesh_dev), sizeof(float4) * packed.size()),
+                 "cudaMalloc(mesh)");
+    if (st != PBF_OK) return st;
+    st = h->cuda(cudaMemcpy(h->mesh_dev, packed.data(), sizeof(float4) * packed.size(), cudaMemcpyHostToDevice),
+                 "H2D mesh");
+    if (st != PBF_OK) return st;
+    h->dp.n_mesh = static_cast<int>(n);
+    h->dp.mesh = h->mesh_dev;
+  }
+  h->drop_graphs();  // the captured steps hold the old parameters
+  return PBF_OK;
 }
 
 void pbf_mc_table(uint16_t* edges, uint8_t* ntri, int8_t* tri) {

@@ -91,6 +91,36 @@ __device__ __forceinline__ float3 predict_delta(const float4& v4, const DevParam
   return v * dt;
 }
 
+// Nearest collider-mesh triangle hit by p + s dir, s in [0, tmax] (Moller-Trumbore as
+// MarchingTriangle::intersect, static_scene/marching_triangle.cpp:21-45, with the
+// triangle's normal at all three vertices). Returns s, or tmax when nothing is hit.
+__device__ __forceinline__ float mesh_hit(const float3 p, const float3 dir, float tmax, const DevParams& P,
+                                          float3* nrm, bool* hit) {
+  float t = tmax;
+  *hit = false;
+  for (int m = 0; m < P.n_mesh; ++m) {
+    const float4 a = __ldg(&P.mesh[4 * m]), b = __ldg(&P.mesh[4 * m + 1]), c = __ldg(&P.mesh[4 * m + 2]);
+    const float3 e1 = f3(b), e2 = f3(c), sv = p - f3(a);
+    const float3 s1 = cross3(dir, e2), s2 = cross3(sv, e1);
+    const float den = dot3(s1, e1);
+    if (den == 0.0f) continue;
+    const float tt = dot3(s2, e2) / den;
+    if (tt < 0.0f || tt > t) continue;
+    const float u = dot3(s1, sv) / den, v = dot3(s2, dir) / den, w = 1.0f - u - v;
+    if (u < 0.0f || u > 1.0f || v < 0.0f || v > 1.0f || w < 0.0f || w > 1.0f) continue;
+    t = tt;
+    *hit = true;
+    *nrm = f3(__ldg(&P.mesh[4 * m + 3]));
+  }
+  return t;
+}
+
+// Distance to keep from a mesh triangle after a stop (the reference backs off by EPS_D =
+// 1e-11 in FP64, below FP32 resolution): 4 ulps of the point's largest coordinate.
+__device__ __forceinline__ float mesh_backoff(const float3 p) {
+  return 4.0f * 1.1920929e-7f * fmaxf(1.0f, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
+}
+
 // Collision record (written by the recording forward of the adjoint): the branch
 // collide() took, enough to apply its reverse with the active set fixed.
 //   bits 0-2  kind: 0 no move (|delta| <= EPS_D), 1 free, 2 stop, 3 stop + slide,
@@ -139,6 +169,46 @@ __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 
   uint32_t rc = kCollFree;
   int wall;
   const float t = wall_hit(p, dir, l, sc, P.open_mask, &wall);
+  if (P.n_mesh > 0) {  // a collider triangle nearer than the wall or clip plane stops the move instead
+    float3 mn;
+    bool mh;
+    const float tm = mesh_hit(p, dir, t, P, &mn, &mh);
+    if (mh && tm < t) {
+      float3 nd = d + dir * fmaxf(tm - mesh_backoff(p), 0.0f);
+      // slide as clamp_response does (particles.cpp:118-124): half the remaining length along
+      // the triangle, unless a clip plane was crossed
+      if (slide && !intersect && dot3(dir, mn) > -1.0f) {
+        const float3 tan = delta - mn * dot3(delta, mn);
+        const float tl = sqrtf(dot3(tan, tan));
+        if (tl > 0.0f) {
+          const float3 dir2 = tan * (1.0f / tl);
+          const float l2 = (total - tm) * 0.5f;
+          const float3 p1 = x + nd;
+          int wall2;
+          const float t2 = wall_hit(p1, dir2, l2, sc, P.open_mask, &wall2);
+          float3 mn2;
+          bool mh2;
+          const float tm2 = mesh_hit(p1, dir2, t2, P, &mn2, &mh2);
+          if (mh2 && tm2 < t2) {
+            nd = nd + dir2 * fmaxf(tm2 - mesh_backoff(p1), 0.0f);
+          } else {
+            nd = nd + dir2 * t2;
+            if (wall2 >= 0) set3(nd, wall2 >> 1, wall_value(sc, wall2) - cmp3(x, wall2 >> 1));
+          }
+        }
+      }
+      d = nd;
+      const float3 q = x + d;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float qa = cmp3(q, a);
+        if (qa < P.clamp_lo[a]) set3(d, a, P.clamp_lo[a] - cmp3(x, a));
+        else if (qa > P.clamp_hi[a]) set3(d, a, P.clamp_hi[a] - cmp3(x, a));
+      }
+      if (REC) *code = kCollNone;  // not recorded: the adjoint takes box colliders only
+      return;
+    }
+  }
   if (wall >= 0 || intersect) {
     float3 nd = d + dir * t;
     if (REC) {
@@ -165,6 +235,23 @@ __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 
           int wall2;
           const float3 p1 = x + nd;
           const float t2 = wall_hit(p1, dir2, l2, sc, P.open_mask, &wall2);
+          if (P.n_mesh > 0) {  // the slide stops at a collider triangle before the wall
+            float3 mn2;
+            bool mh2;
+            const float tm2 = mesh_hit(p1, dir2, t2, P, &mn2, &mh2);
+            if (mh2 && tm2 < t2) {
+              d = nd + dir2 * fmaxf(tm2 - mesh_backoff(p1), 0.0f);
+              if (REC) *code = kCollNone;  // not recorded: the adjoint takes box colliders only
+              const float3 q = x + d;
+#pragma unroll
+              for (int a = 0; a < 3; ++a) {
+                const float qa = cmp3(q, a);
+                if (qa < P.clamp_lo[a]) set3(d, a, P.clamp_lo[a] - cmp3(x, a));
+                else if (qa > P.clamp_hi[a]) set3(d, a, P.clamp_hi[a] - cmp3(x, a));
+              }
+              return;
+            }
+          }
           nd = nd + dir2 * t2;
           if (REC) {
             rc = (rc & ~7u) | kCollSlide;

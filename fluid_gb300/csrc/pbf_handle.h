@@ -58,6 +58,7 @@ struct Handle {
   double snap_time = 0;
   Tape tape;                 // recording + work arrays of the adjoint (first use)
   SurfTable* surf_table_dev = nullptr;  // marching-cubes table (first pbf_surface)
+  float4* mesh_dev = nullptr;           // collider triangles (pbf_set_collider_mesh)
   double phase_ms[kNumPhases] = {};
   uint64_t phase_launches[kNumPhases] = {};
 

@@ -51,7 +51,10 @@ struct DevParams {
   float clamp_lo[3], clamp_hi[3];
   int scorr_n, n_clip, clip_axis[2], open_mask, max_words;
   int stats;
+  int n_mesh;                // collider triangles besides the box walls (pbf_set_collider_mesh)
+  const float4* mesh;        // 4 float4 per triangle: p1, p2 - p1, p3 - p1, normal
 };
+constexpr int kMaxMeshTriangles = 1024;
 
 // Step statistics accumulated on the device (reset every step).
 struct DevStats {

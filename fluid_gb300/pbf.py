@@ -20,7 +20,7 @@ from .params import CParams, PbfParams
 LIB_PATH = Path(os.environ.get("PBF_LIB") or Path(__file__).resolve().parent / "_lib" / "libpbf.so")
 
 PBF_OK = 0
-ABI_VERSION = 3  # PBF_ABI_VERSION of include/pbf.h that these declarations follow
+ABI_VERSION = 4  # PBF_ABI_VERSION of include/pbf.h that these declarations follow
 STATUS = {0: "PBF_OK", 1: "PBF_ERR_INVALID", 2: "PBF_ERR_CUDA", 3: "PBF_ERR_TIMEOUT",
           4: "PBF_ERR_NONFINITE", 5: "PBF_ERR_CAPACITY", 6: "PBF_ERR_NOMEM"}
 
@@ -95,6 +95,7 @@ def _declare(L):
         "pbf_adjoint_step_device": (st, [P, ctypes.c_double, P, P, P, P, P, P, P, P, P, P]),
         "pbf_surface": (st, [P, ctypes.c_double, ctypes.c_double, P, P, P, P, sz, P]),
         "pbf_mc_table": (None, [P, P, P]),
+        "pbf_set_collider_mesh": (st, [P, sz, P]),
         "pbf_size": (sz, [P]),
         "pbf_num_scenes": (ctypes.c_int, [P]),
         "pbf_last_error": (ctypes.c_char_p, [P]),
@@ -258,6 +259,14 @@ class Simulator:
         self._check(lib().pbf_adjoint_step_device(
             self._h, dt, opt(pos_ptr), opt(vel_ptr), opt(gx_out_ptr), opt(gv_out_ptr), P(gx_in_ptr),
             P(gv_in_ptr), P(g_rho0_ptr), opt(pos_out_ptr), opt(vel_out_ptr), opt(stream)))
+
+    def set_collider_mesh(self, tri=None):
+        """Collider triangles besides the box walls: (m, 9) p1 p2 p3 (None or empty removes them)."""
+        if tri is None or len(tri) == 0:
+            self._check(lib().pbf_set_collider_mesh(self._h, 0, None))
+            return
+        t = np.ascontiguousarray(tri, dtype=np.float32).reshape(-1, 9)
+        self._check(lib().pbf_set_collider_mesh(self._h, t.shape[0], _ptr(t)))
 
     def surface(self, iso: float | None = None, step: float | None = None, lo=None, hi=None):
         """Particles::getSurfacePrims (particles.cpp:352-385) on the current state: the

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define PBF_ABI_VERSION 3
+#define PBF_ABI_VERSION 4
 
 #if defined(__GNUC__)
 #define PBF_API __attribute__((visibility("default")))
@@ -285,6 +285,19 @@ PBF_API pbf_status pbf_adjoint_step_device(pbf_handle* h, double dt, const float
  */
 PBF_API pbf_status pbf_surface(pbf_handle* h, double isolevel, double step, const double* lo, const double* hi,
                                float* xyz, float* nrm, size_t cap, size_t* count);
+
+/*
+ * pbf_set_collider_mesh -- triangles the particles collide with besides the box walls,
+ * as the reference's colliders are the triangles of its scene's BVH (clamp and
+ * clamp_response, particles.cpp:51-132). tri: n triangles of 9 floats (p1, p2, p3, host
+ * memory); each triangle's normal is unit((p2 - p1) x (p3 - p1)), used for the slide of
+ * the predicted move. A move stops at the nearest wall, clip plane or triangle; after a
+ * triangle stop the particle keeps 4 FP32 ulps from it (the reference keeps EPS_D =
+ * 1e-11, below FP32 resolution). n = 0 removes the mesh. At most 1024 triangles, each
+ * tested by every ray (no hierarchy). pbf_adjoint_step_device refuses a handle with a
+ * mesh (its collision reverse is for axis-aligned walls).
+ */
+PBF_API pbf_status pbf_set_collider_mesh(pbf_handle* h, size_t n, const float* tri);
 
 /*
  * pbf_mc_table -- the triangulation table pbf_surface uses (no GPU needed): for each of

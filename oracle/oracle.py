@@ -68,6 +68,8 @@ def lib(fp32: bool = False, adjoint: bool = False):
         L.orc_estimate_density_at.argtypes = [P, ctypes.c_int64, P, ctypes.c_int64, P, P, ctypes.c_int]
         L.orc_estimate_density_at.restype = ctypes.c_int
         L.orc_max_threads.restype = ctypes.c_int
+        L.orc_set_mesh.argtypes = [ctypes.c_int64, P]
+        L.orc_set_mesh.restype = ctypes.c_int
         L.orc_surface.argtypes = [P, ctypes.c_int64, P, ctypes.c_double, ctypes.c_double, P, P, P, P, P, P, P,
                                   ctypes.c_int64, ctypes.c_int]
         L.orc_surface.restype = ctypes.c_int64
@@ -202,6 +204,18 @@ def rollout_adjoint(pos, vel, params: PbfParams, steps: int, gx, gv, dt: float |
         a = step_adjoint(xs[s], vs[s], params, gx, gv, dt=dt, threads=threads)
         gx, gv, g0 = a["gx"], a["gv"], g0 + a["grho0"]
     return {"gx": gx, "gv": gv, "grho0": g0, "pos": xs[-1], "vel": vs[-1]}
+
+
+def set_mesh(tri=None, fp32: bool = False) -> None:
+    """Collider triangles besides the box walls ((m, 9) p1 p2 p3, None to clear) for the
+    following calls (process-wide in the restatement)."""
+    L = lib(fp32)
+    if tri is None or len(tri) == 0:
+        L.orc_set_mesh(0, None)
+        return
+    t = np.ascontiguousarray(tri, dtype=np.float64).reshape(-1, 9)
+    if L.orc_set_mesh(t.shape[0], _ptr(t)) != 0:
+        raise ValueError("at most 1024 collider triangles")
 
 
 def surface(pos, params: PbfParams, ntri, tri, iso: float | None = None, step: float | None = None,

@@ -78,6 +78,9 @@ static inline real intpow(real b, int e) {
   return r;
 }
 
+#define ORC_MAX_MESH 1024
+#define ORC_MAX_TRI (12 + ORC_MAX_MESH)
+
 typedef struct {
   real h, h2, h6, h9, tis;
   real epsilon, k, vort_eps, xsph_c, rest_density;
@@ -87,8 +90,8 @@ typedef struct {
   int n_clip, clip_axis[2];
   real clip_value[2];
   int ntri;
-  v3 tp[12][3];
-  v3 tn[12];
+  v3 tp[ORC_MAX_TRI][3];  /* the box walls (up to 12), then the collider mesh */
+  v3 tn[ORC_MAX_TRI];
 } ctx_t;
 
 /* poly6_kernel, particles.cpp:134-141 */
@@ -325,6 +328,31 @@ static int find_neighbors(const ctx_t* c, int64_t n, const v3* xs, nbrs_t* out) 
   return 0;
 }
 
+/* Collider triangles besides the box walls (orc_set_mesh), as the reference's BVH holds
+ * the scene's triangles: each a MarchingTriangle with the normal unit((p2 - p1) x (p3 - p1))
+ * at all three vertices. Process-wide: set it before the calls that should see it. */
+static int64_t g_mesh_n = 0;
+static double g_mesh[9 * ORC_MAX_MESH];
+
+int orc_set_mesh(int64_t n, const double* tri) {
+  if (n < 0 || n > ORC_MAX_MESH) return -1;
+  g_mesh_n = n;
+  if (n) memcpy(g_mesh, tri, sizeof(double) * 9 * (size_t)n);
+  return 0;
+}
+
+static void add_mesh(ctx_t* c) {
+  for (int64_t m = 0; m < g_mesh_n; m++) {
+    const double* q = g_mesh + 9 * m;
+    v3 p1 = V(q[0], q[1], q[2]), p2 = V(q[3], q[4], q[5]), p3 = V(q[6], q[7], q[8]);
+    int t = c->ntri++;
+    c->tp[t][0] = p1;
+    c->tp[t][1] = p2;
+    c->tp[t][2] = p3;
+    c->tn[t] = unit(cross(vsub(p2, p1), vsub(p3, p1)));
+  }
+}
+
 /* ---- the step ---------------------------------------------------------------- */
 
 static void make_ctx(ctx_t* c, const pbf_params* p) {
@@ -351,6 +379,7 @@ static void make_ctx(ctx_t* c, const pbf_params* p) {
     c->clip_value[i] = p->clip_value[i];
   }
   build_box(c, p->box_lo, p->box_hi, p->box_open_mask);
+  add_mesh(c);
   /* Particle::tensile_instability_scale, particles.cpp:151 */
   c->tis = 1.0 / poly6(c, V(0, 0, p->scorr_dq * p->h));
 }

@@ -26,7 +26,10 @@
 // 8 = restart: every step starts again from the input state (a fresh
 // Particles built untimed), so `seconds` times K steps of the same input,
 // 16 = surface: after the steps, the triangles of the reference's surface
-// (appended: i64 ntri, f64 xyz[9 ntri], f64 nrm[9 ntri], i64 cube[ntri]).
+// (appended: i64 ntri, f64 xyz[9 ntri], f64 nrm[9 ntri], i64 cube[ntri]),
+// 32 = collider mesh: the input continues with i64 m, f64 tri[9 m]; each
+// triangle joins the box in the BVH as a MarchingTriangle with the normal
+// ((p2 - p1) x (p3 - p1)).unit() at its three vertices.
 // open_mask: bit per box face to leave out (0 x-lo, 1 x-hi, 2 y-lo, 3 y-hi,
 // 4 z-lo, 5 z-hi).
 #include <chrono>
@@ -195,6 +198,18 @@ int main(int argc, char** argv) {
   (void)devnull;
 
   std::vector<Primitive*> prims = box_triangles(lo, hi, static_cast<int>(open_mask));
+  if (flags & 32) {
+    int64_t m = 0;
+    rd(in, &m, 1);
+    std::vector<double> tri(9 * m);
+    rd(in, tri.data(), tri.size());
+    for (int64_t t = 0; t < m; t++) {
+      const double* q = tri.data() + 9 * t;
+      Vector3D p1(q[0], q[1], q[2]), p2(q[3], q[4], q[5]), p3(q[6], q[7], q[8]);
+      Vector3D nn = cross(p2 - p1, p3 - p1).unit();
+      prims.push_back(new MarchingTriangle(p1, p2, p3, nn, nn, nn, nullptr));
+    }
+  }
   BVHAccel* bvh = new BVHAccel(prims);
 
   auto make = [&]() {

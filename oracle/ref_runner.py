@@ -24,13 +24,15 @@ def available() -> bool:
 
 def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool = False,
         load_density: bool = False, restart: bool = False, timeout: float | None = None,
-        surface: bool = False) -> dict:
+        surface: bool = False, mesh=None) -> dict:
     """Run ``steps`` reference steps. ``params`` is a fluid_gb300.params.PbfParams.
 
     ``restart``: every step starts again from (pos, vel); ``seconds`` then times
     ``steps`` steps of the same input. ``surface``: also the triangles of the
     reference's surface after the steps (Particles::getSurfacePrims with
     updateSurface's arguments): ``surf_xyz`` / ``surf_nrm`` (T, 3, 3), ``surf_cube``.
+    ``mesh``: (m, 9) collider triangles added to the box (the reference's BVH holds them
+    as MarchingTriangles with the normal ((p2 - p1) x (p3 - p1)).unit()).
 
     The reference hard-codes gravity on -y, the clip planes z=1 / y=1.49 and the
     clamp box (particles.cpp:57-83, 180); params that disagree are rejected.
@@ -51,7 +53,8 @@ def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool 
     pos = np.ascontiguousarray(pos, dtype=np.float64)
     vel = np.ascontiguousarray(vel, dtype=np.float64)
     n = pos.shape[0]
-    flags = (2 if neighbors else 0) | (4 if load_density else 0) | (8 if restart else 0) | (16 if surface else 0)
+    flags = ((2 if neighbors else 0) | (4 if load_density else 0) | (8 if restart else 0) | (16 if surface else 0)
+             | (32 if mesh is not None else 0))
     with tempfile.TemporaryDirectory() as td:
         fin = Path(td) / "in.bin"
         fout = Path(td) / "out.bin"
@@ -65,6 +68,10 @@ def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool 
             f.write(struct.pack("<3d", *params.box_hi))
             f.write(pos.tobytes())
             f.write(vel.tobytes())
+            if mesh is not None:
+                m = np.ascontiguousarray(mesh, dtype=np.float64).reshape(-1, 9)
+                f.write(struct.pack("<q", m.shape[0]))
+                f.write(m.tobytes())
         subprocess.run([str(DRIVER), str(fin), str(fout)], check=True, timeout=timeout)
         buf = fout.read_bytes()
     assert buf[:8] == b"PBFREFO1"

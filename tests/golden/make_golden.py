@@ -45,10 +45,10 @@ def load_reference_xml(path: Path):
     return np.array(pos), np.array(vel), rho0
 
 
-def save_case(name: str, pos, vel, params: PbfParams, steps: int, neighbors: bool = True) -> None:
+def save_case(name: str, pos, vel, params: PbfParams, steps: int, neighbors: bool = True, mesh=None) -> None:
     jac = ref_runner.run(pos, vel, params, steps=steps, mode="jacobi", neighbors=neighbors,
-                         load_density=True)
-    lit = ref_runner.run(pos, vel, params, steps=steps, mode="literal")
+                         load_density=True, mesh=mesh)
+    lit = ref_runner.run(pos, vel, params, steps=steps, mode="literal", mesh=mesh)
     data = dict(
         params=json.dumps(dataclasses.asdict(params)),
         steps=np.int64(steps),
@@ -57,11 +57,34 @@ def save_case(name: str, pos, vel, params: PbfParams, steps: int, neighbors: boo
         load_density=jac["load_density"],
         literal_pos=lit["pos"], literal_vel=lit["vel"], literal_density=lit["density"],
     )
+    if mesh is not None:
+        data["mesh"] = np.asarray(mesh, dtype=np.float64).reshape(-1, 9)
     if neighbors:
         data["nbr_offsets"] = jac["nbr_offsets"].astype(np.int32)
         data["nbr_idx"] = jac["nbr_idx"].astype(np.int32)
     np.savez_compressed(HERE / f"{name}.npz", **data)
     print(f"{name}: n={pos.shape[0]} steps={steps}")
+
+
+# A slanted ramp of two triangles across the [0,1]^3 box (collider mesh besides the walls).
+RAMP = np.array([[0.05, 0.25, 0.0, 0.95, 0.05, 0.0, 0.95, 0.05, 1.0],
+                 [0.05, 0.25, 0.0, 0.95, 0.05, 1.0, 0.05, 0.25, 1.0]])
+
+
+def ramp_scene():
+    """8^3 block (s = 0.05, h = 0.1) just above the ramp, moving down and along x."""
+    s = 0.05
+    p = scenes.lattice(8, 8, 8, s, corner=(0.3, 0.22, 0.3))
+    p += scenes.uniform(5, p.size, -0.001, 0.001).reshape(p.shape)
+    v = np.zeros_like(p)
+    v[:, 0] = 0.3
+    v[:, 1] = -2.0
+    return p, v, scenes.physical_params(0.1, s)
+
+
+def mesh_case():
+    p, v, prm = ramp_scene()
+    save_case("ramp_block512_2step", p, v, prm, 2, mesh=RAMP)
 
 
 def params_from_json(text: str) -> PbfParams:
@@ -89,6 +112,8 @@ def main(argv):
     # Scale-consistent constants: a 20-step collapse against the floor and walls (past about
     # 20 steps the clumping rate of the reference's formulation depends on the precision).
     save_case("block512_mass_20step", p, np.zeros_like(p), scenes.physical_params(0.1, s), 20)
+
+    mesh_case()
 
     for xml_name, steps in (("p.xml", 1), ("p.xml", 3), ("spheres_p.xml", 1)):
         pos, vel, rho0 = load_reference_xml(reference / "particles" / xml_name)

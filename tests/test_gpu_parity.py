@@ -316,3 +316,55 @@ def test_autotune_keeps_state_and_results(pbf):
         sim.set_tuning(block_nbr=512, block_solve=64, block_predict=128, block_misc=64)
         sim.time_step(sc.params.dt, 5)
         assert np.array_equal(sim.positions(), xa)
+
+
+def test_collider_mesh_matches_oracle(pbf, oracle_lib):
+    """A block dropped onto a two-triangle ramp (pbf_set_collider_mesh) against the FP64
+    restatement with the same triangles (pinned to the reference build by
+    tests/golden/ramp_block512_2step.npz), one step on identical neighbour sets. The GPU
+    backs off 4 FP32 ulps from a triangle where the reference backs off 1e-11, which
+    moves stopped particles by ~5e-7."""
+    from tests.golden.make_golden import RAMP, ramp_scene
+
+    p, v, prm = ramp_scene()
+    pos, vel = _f32(p), _f32(v)
+    ramp = RAMP.astype(np.float32)
+    with pbf.Simulator(pos, vel, prm) as sim:
+        sim.set_collider_mesh(ramp)
+        sim.time_step(prm.dt, 1)
+        x, v1, rho = sim.positions(), sim.velocities(), sim.densities()
+        nb = sim.neighbors()
+    with pbf.Simulator(pos, vel, prm) as sim:
+        sim.time_step(prm.dt, 1)
+        x_free = sim.positions()
+    oracle_lib.set_mesh(ramp.astype(np.float64))
+    try:
+        ref = oracle_lib.step(pos, vel, prm, 1, given_neighbors=nb)
+    finally:
+        oracle_lib.set_mesh(None)
+    ex, ev, er = rel_err(x, ref["pos"]), rel_err(v1, ref["vel"]), rel_err(rho, ref["density"])
+    moved = np.abs(x - x_free).max()
+    print(f"ramp 1 step FP32 vs FP64: pos {ex:.2e} vel {ev:.2e} rho {er:.2e}; ramp moves particles by {moved:.2e}")
+    assert moved > 1e-3
+    assert ex < 1e-5 and ev < 1e-4 and er < 1e-4
+    assert np.all(x[:, 1] >= ref["pos"][:, 1].min() - 1e-5)
+
+
+def test_collider_mesh_arguments(pbf):
+    import torch
+
+    sc = scenes.block4096(1)
+    with pbf.Simulator(_f32(sc.pos), _f32(sc.vel), sc.params) as sim:
+        with pytest.raises(pbf.PbfError):
+            sim.set_collider_mesh(np.zeros((1, 9), dtype=np.float32))  # degenerate
+        with pytest.raises(pbf.PbfError):
+            sim.set_collider_mesh(np.ones((1025, 9), dtype=np.float32))
+        from tests.golden.make_golden import RAMP
+
+        sim.set_collider_mesh(RAMP)
+        x = torch.zeros((sim.n, 3), dtype=torch.float32, device="cuda")
+        r = torch.zeros(1, dtype=torch.float64, device="cuda")
+        with pytest.raises(pbf.PbfError):  # the adjoint takes the box collider only
+            sim.adjoint_step_device(sc.params.dt, None, None, None, None, x.data_ptr(), x.data_ptr(), r.data_ptr())
+        sim.set_collider_mesh(None)
+        sim.time_step(sc.params.dt, 1)

@@ -25,8 +25,11 @@ def _case_id(path):
 
 
 @pytest.fixture(params=GOLDEN, ids=_case_id)
-def golden(request):
-    return np.load(request.param)
+def golden(request, oracle_lib):
+    g = np.load(request.param)
+    oracle_lib.set_mesh(g["mesh"] if "mesh" in g.files else None)  # collider triangles of the case
+    yield g
+    oracle_lib.set_mesh(None)
 
 
 def test_golden_files_present():
@@ -67,6 +70,7 @@ def test_load_time_density_matches_reference(golden, oracle_lib):
 
 
 def test_oracle_thread_count_independent(oracle_lib):
+    oracle_lib.set_mesh(None)
     g = np.load(GOLDEN[0])
     prm = params_from_json(str(g["params"]))
     a = oracle_lib.step(g["pos_in"], g["vel_in"], prm, steps=1, threads=1)
