@@ -72,13 +72,14 @@ RAMP = np.array([[0.05, 0.25, 0.0, 0.95, 0.05, 0.0, 0.95, 0.05, 1.0],
 
 
 def ramp_scene():
-    """8^3 block (s = 0.05, h = 0.1) just above the ramp, moving down and along x."""
+    """8^3 block (s = 0.05, h = 0.1) just above the ramp, moving down and along x: its
+    lowest layer reaches the ramp in the first step."""
     s = 0.05
-    p = scenes.lattice(8, 8, 8, s, corner=(0.3, 0.22, 0.3))
+    p = scenes.lattice(8, 8, 8, s, corner=(0.3, 0.20, 0.3))
     p += scenes.uniform(5, p.size, -0.001, 0.001).reshape(p.shape)
     v = np.zeros_like(p)
     v[:, 0] = 0.3
-    v[:, 1] = -2.0
+    v[:, 1] = -3.0
     return p, v, scenes.physical_params(0.1, s)
 
 
