@@ -15,11 +15,13 @@
 //   p.ps[i]->getPosition() / getNewPosition() / getLatestDensityEstimate()
 //   p.ps[i]->velocity, getDensityBasedColor(), p.estimateDensityAt(pos)
 //   p.updateSurface(); p.surface; p.getSurfacePrims(iso, step)   // marching cubes
+//   p.setColliderMesh(vertices)                                   // the BVH's triangles
 //
-// Differences, by design: the collider is the axis-aligned box of the pbf_params
-// (the reference casts rays against a BVH of scene triangles; `bvh` is kept as an
-// opaque, unused pointer); the XSPH pass is order-independent; positions,
-// velocities and densities are FP32 on the device and mirrored into V after
+// Differences, by design: the collider is the axis-aligned box of the pbf_params plus the
+// triangles given to setColliderMesh (the reference casts rays against a BVH of the
+// scene's primitives; `bvh` is kept as an opaque, unused pointer); the XSPH pass is
+// order-independent; positions, velocities and densities are FP32 on the device and
+// mirrored into V after
 // every step; Particle::neighbors stays empty (neighbour sets live on the device,
 // see pbf_get_neighbors). Errors throw std::runtime_error with pbf_last_error().
 #pragma once
@@ -176,6 +178,18 @@ class Particles {
     surfaceUpToTimestep = true;
   }
 
+  // The collider's triangles besides the box walls (the reference ray-casts the triangles
+  // of its scene's BVH, `bvh`): three vertices per triangle, in the order p1 p2 p3.
+  void setColliderMesh(const std::vector<V>& vertices) {
+    mesh_.assign(vertices.size() * 3, 0.f);
+    for (size_t k = 0; k < vertices.size(); ++k) {
+      mesh_[3 * k] = static_cast<float>(vertices[k].x);
+      mesh_[3 * k + 1] = static_cast<float>(vertices[k].y);
+      mesh_[3 * k + 2] = static_cast<float>(vertices[k].z);
+    }
+    if (h_ && !dirty_) check(pbf_set_collider_mesh(h_, mesh_.size() / 9, mesh_.data()));
+  }
+
   const pbf_params& params() const { return prm_; }
   pbf_stats stats() {
     pbf_stats s{};
@@ -192,6 +206,7 @@ class Particles {
   bool dirty_ = true;
   bool verbose_ = false;
   int device_ = 0;
+  std::vector<float> mesh_;  // collider triangles, 9 floats each
 
   void check(pbf_status st) const {
     if (st != PBF_OK) throw std::runtime_error(std::string("pbf: ") + pbf_last_error(h_));
@@ -220,6 +235,7 @@ class Particles {
     if (st != PBF_OK) throw std::runtime_error(std::string("pbf_create: ") + pbf_last_error(nullptr));
     h_ = h;
     dirty_ = false;
+    if (!mesh_.empty()) check(pbf_set_collider_mesh(h_, mesh_.size() / 9, mesh_.data()));
   }
 
   // Mirror device state into the Particle objects (original order).
