@@ -208,38 +208,41 @@ def dist_setup():
 
 
 def reduce_max(x: float, world: int) -> float:
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
+    from fluid_gb300.shard import max_over_ranks
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return max_over_ranks(x, world)
 
 
 def barrier(world):
-    if world > 1:
-        import torch.distributed as dist
+    from fluid_gb300.shard import barrier as _barrier
 
-        dist.barrier()
+    _barrier(world)
 
 
-def bench_batched(args, local, steps: int = 10, warmup: int = 3) -> dict:
+def bench_batched(args, world, rank, local, steps: int = 10, warmup: int = 3) -> dict:
     """256 independent scenes of 2k-32k particles: one batched handle (one launch per
     phase over every scene, the step replayed as a CUDA graph, launch shapes from the
     autotuner) against the same scenes stepped one at a time, each with its own graph.
     Both time device work with CUDA events per step; every step starts from the scenes'
-    configured state (snapshot restored between steps, untimed)."""
+    configured state (snapshot restored between steps, untimed). With several ranks the
+    scenes are partitioned by scene (fluid_gb300.shard, balanced by particle count) and
+    each rank steps its share; the job's time is the slowest rank's."""
     import torch
 
     from fluid_gb300 import pbf, scenes
     from fluid_gb300.params import PBF_FLAG_GRAPH
+    from fluid_gb300.shard import max_over_ranks, shard_scenes
 
     b = scenes.batched_256()
+    mine = shard_scenes(b.counts, world)[rank]
+    first = np.concatenate([[0], np.cumsum(b.counts)])
+    pos = np.concatenate([b.pos[first[k]:first[k + 1]] for k in mine])
+    vel = np.concatenate([b.vel[first[k]:first[k + 1]] for k in mine])
+    counts = [b.counts[k] for k in mine]
+    boxes = [b.boxes[k] for k in mine]
     prm = b.params.with_(flags=PBF_FLAG_GRAPH)
     dt = prm.dt
-    sim = pbf.Simulator(b.pos, b.vel, prm, device=local, counts=b.counts, boxes=b.boxes)
+    sim = pbf.Simulator(pos, vel, prm, device=local, counts=counts, boxes=boxes)
     sim.sort()
     sim.snapshot()
     tuning = sim.autotune(dt, reps=2)
@@ -255,19 +258,16 @@ def bench_batched(args, local, steps: int = 10, warmup: int = 3) -> dict:
         sim.step_async(dt, 1)
         ev[k][1].record(stream)
     sim.sync()
-    batched_s = sum(a.elapsed_time(z) for a, z in ev) / 1e3
-    n_total = sim.n
+    batched_s = max_over_ranks(sum(a.elapsed_time(z) for a, z in ev) / 1e3, world)
     sim.close()
 
     singles = []
-    off = 0
-    for c in b.counts:
-        s1 = pbf.Simulator(b.pos[off:off + c], b.vel[off:off + c], prm, device=local)
+    for k in mine:
+        s1 = pbf.Simulator(b.pos[first[k]:first[k + 1]], b.vel[first[k]:first[k + 1]], prm, device=local)
         s1.set_tuning(**tuning)
         s1.sort()
         s1.snapshot()
         singles.append(s1)
-        off += c
     for s1 in singles:  # warm each graph
         for _ in range(2):
             s1.restore()
@@ -286,13 +286,16 @@ def bench_batched(args, local, steps: int = 10, warmup: int = 3) -> dict:
             single_s += a.elapsed_time(z) / 1e3
     for s1 in singles:
         s1.close()
+    single_s = max_over_ranks(single_s, world)
+    n_total = int(sum(b.counts))
     v_b = n_total * steps / batched_s
     v_1 = n_total * steps / single_s
-    return {"workload": "batched_256", "scenes": len(b.counts), "particles": int(n_total),
+    return {"workload": "batched_256", "scenes": len(b.counts), "particles": n_total,
             "counts_min_max": [min(b.counts), max(b.counts)], "steps": steps,
             "value": v_b, "one_at_a_time": v_1, "speedup": v_b / v_1, "unit": UNIT,
             "ms_per_step": batched_s / steps * 1e3, "one_at_a_time_ms_per_step": single_s / steps * 1e3,
-            "graph": True, "tuning": tuning}
+            "graph": True, "tuning": tuning, "ranks": world,
+            "sharding": "scenes partitioned over ranks by particle count" if world > 1 else "one rank"}
 
 
 def bench_reference(args, scene, world, rank):
@@ -592,6 +595,7 @@ def bench_ours(args, scene, world, rank, local):
                "path": "pbf_set_state + pbf_step + pbf_get_positions + pbf_get_velocities, pinned host buffers"}
     sim.close()
 
+    batched = bench_batched(args, world, rank, local) if not args.no_batched else None
     if rank != 0:
         return 0
     line = {
@@ -623,8 +627,8 @@ def bench_ours(args, scene, world, rank, local):
         line["e2e"] = e2e
     if surface:
         line["surface"] = surface
-    if not args.no_batched:
-        line["batched"] = bench_batched(args, local)
+    if batched:
+        line["batched"] = batched
     if not args.no_adjoint:
         line["adjoint"] = bench_adjoint(args, local)
     if not args.no_cpu_baseline and world == 1:

@@ -176,12 +176,17 @@ def _block_of(count: int, s: float, corner_sel: int, box=(0.0, 1.0)) -> np.ndarr
     return p + np.asarray(corner)
 
 
+def batched_counts(seed: int = 4, n_scenes: int = 256, lo: int = 2048, hi: int = 32768) -> list:
+    """Particle counts of the batched workload's scenes: log-uniform in [lo, hi]."""
+    u = uniform(seed, n_scenes, math.log(lo), math.log(hi))
+    return [int(round(math.exp(x))) for x in u]
+
+
 def batched_256(seed: int = 4, n_scenes: int = 256, lo: int = 2048, hi: int = 32768) -> Scene:
     """256 independent [0,1]^3 scenes, counts log-uniform in [2k, 32k], h = 0.05, s = 0.025."""
     h = 0.05
     s = h / 2
-    u = uniform(seed, n_scenes, math.log(lo), math.log(hi))
-    counts = [int(round(math.exp(x))) for x in u]
+    counts = batched_counts(seed, n_scenes, lo, hi)
     corners = (splitmix64(seed, n_scenes, stream=2) >> np.uint64(61)).astype(int)
     vels = uniform(seed, 3 * n_scenes, -0.5, 0.5, stream=3).reshape(n_scenes, 3)
     jit_total = sum(counts) * 3
