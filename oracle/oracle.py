@@ -22,6 +22,8 @@ LIB = HERE / "_build" / "libpbf_oracle.so"
 LIB32 = HERE / "_build" / "libpbf_oracle_fp32.so"
 SRC_ADJ = HERE / "pbf_oracle_adj.c"
 LIB_ADJ = HERE / "_build" / "libpbf_oracle_adj.so"
+SRC_PT = HERE / "pbf_oracle_pt.c"
+LIB_PT = HERE / "_build" / "libpbf_oracle_pt.so"
 
 if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
@@ -31,10 +33,12 @@ from fluid_gb300.params import PbfParams  # noqa: E402
 
 def build(force: bool = False) -> Path:
     """Build the FP64 restatement, its FP32 twin (same source, -DORC_FLOAT) and the
-    FP64 reference gradient (pbf_oracle_adj.c, which includes the restatement)."""
+    FP64 reference gradient (pbf_oracle_adj.c, which includes the restatement) and the
+    path tracer's restatement (pbf_oracle_pt.c)."""
     LIB.parent.mkdir(parents=True, exist_ok=True)
-    for out, src, extra in ((LIB, SRC, []), (LIB32, SRC, ["-DORC_FLOAT"]), (LIB_ADJ, SRC_ADJ, [])):
-        newest = max(SRC.stat().st_mtime, src.stat().st_mtime)
+    for out, src, extra in ((LIB, SRC, []), (LIB32, SRC, ["-DORC_FLOAT"]), (LIB_ADJ, SRC_ADJ, []),
+                            (LIB_PT, SRC_PT, [])):
+        newest = src.stat().st_mtime if src == SRC_PT else max(SRC.stat().st_mtime, src.stat().st_mtime)
         if not force and out.exists() and out.stat().st_mtime >= newest:
             continue
         cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
@@ -247,6 +251,83 @@ def surface(pos, params: PbfParams, ntri, tri, iso: float | None = None, step: f
     total, *_ = run(0)
     total, xyz, nrm, cube = run(int(total))
     return {"xyz": xyz[:total], "nrm": nrm[:total], "cube": cube[:total]}
+
+
+class OrcMat(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int64), ("c1", ctypes.c_double * 3), ("c2", ctypes.c_double * 3),
+                ("ior", ctypes.c_double)]
+
+
+class OrcLight(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int64)] + [(k, ctypes.c_double * 3) for k in
+                                             ("radiance", "position", "direction", "dim_x", "dim_y")]
+
+
+class OrcCam(ctypes.Structure):
+    _fields_ = [("pos", ctypes.c_double * 3), ("c2w", ctypes.c_double * 9), ("hfov", ctypes.c_double),
+                ("vfov", ctypes.c_double), ("nclip", ctypes.c_double), ("fclip", ctypes.c_double)]
+
+
+RNG_STD, RNG_COUNTER = 0, 1
+
+
+def _pt_lib():
+    if LIB_PT not in _libs:
+        if not LIB_PT.exists():
+            build()
+        L = ctypes.CDLL(str(LIB_PT))
+        P = ctypes.c_void_p
+        L.orc_camera_frame.argtypes = [ctypes.c_double] * 4 + [P] + [ctypes.c_double] * 5 + [ctypes.c_int64] * 2 + [P]
+        L.orc_camera_frame.restype = None
+        L.orc_render.argtypes = [P, P, P, ctypes.c_int64, P, P, ctypes.c_int64, P, ctypes.c_int64, ctypes.c_int64,
+                                 ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_uint64, P, P,
+                                 ctypes.c_int]
+        L.orc_render.restype = ctypes.c_int
+        _libs[LIB_PT] = L
+    return _libs[LIB_PT]
+
+
+def camera_frame(cam, width: int, height: int) -> dict:
+    """Camera::configure + Camera::place (camera.cpp:15-46, 92-111): position, c2w
+    columns (3, 3), the adjusted fields of view and the clip distances."""
+    L = _pt_lib()
+    out = OrcCam()
+    tgt = np.ascontiguousarray(cam.target, dtype=np.float64)
+    L.orc_camera_frame(cam.hfov, cam.vfov, cam.nclip, cam.fclip, _ptr(tgt), cam.phi, cam.theta, cam.r, cam.min_r,
+                       cam.max_r, width, height, ctypes.byref(out))
+    return {"pos": np.array(out.pos[:]), "c2w": np.array(out.c2w[:]).reshape(3, 3), "hfov": out.hfov,
+            "vfov": out.vfov, "nclip": out.nclip, "fclip": out.fclip, "_c": out}
+
+
+def render(scene, cam, surface_xyz, surface_nrm, width: int, height: int, ns_aa: int = 1, max_depth: int = 1,
+           ns_area_light: int = 1, rng: int = RNG_STD, seed: int = 1, threads: int = 0) -> dict:
+    """One frame of the restated path tracer over the scene's triangles plus the fluid
+    surface triangles (DiffuseBSDF(0.1, 0.1, 0.8)). Returns ``hdr`` (H, W, 3) float32 with
+    row 0 at y = 0 (the bottom, as the reference's sample buffer) and ``rgba`` (H, W, 4)
+    uint8 in PNG row order (top first)."""
+    from fluid_gb300 import render as R
+
+    L = _pt_lib()
+    sx = np.asarray(surface_xyz, dtype=np.float64).reshape(-1, 3, 3)
+    sn = np.asarray(surface_nrm, dtype=np.float64).reshape(-1, 3, 3)
+    mats = list(scene.materials) + [R.Material(R.DIFFUSE, R.FLUID_ALBEDO)]
+    tri = np.ascontiguousarray(np.concatenate([scene.tri, sx]))
+    nrm = np.ascontiguousarray(np.concatenate([scene.nrm, sn]))
+    tri_mat = np.ascontiguousarray(np.concatenate([scene.tri_mat, np.full(len(sx), len(mats) - 1, np.int64)]))
+    cm = (OrcMat * len(mats))(*[OrcMat(m.kind, (ctypes.c_double * 3)(*m.c1), (ctypes.c_double * 3)(*m.c2), m.ior)
+                                for m in mats])
+    cl = (OrcLight * max(len(scene.lights), 1))(*[OrcLight(l.kind, *[(ctypes.c_double * 3)(*getattr(l, k)) for k in
+                                                                     ("radiance", "position", "direction", "dim_x",
+                                                                      "dim_y")]) for l in scene.lights])
+    fr = camera_frame(cam, width, height)
+    hdr = np.zeros((height, width, 3), dtype=np.float32)
+    rgba = np.zeros((height, width, 4), dtype=np.uint8)
+    rc = L.orc_render(_ptr(tri), _ptr(nrm), _ptr(tri_mat), len(tri), ctypes.cast(cm, ctypes.c_void_p),
+                      ctypes.cast(cl, ctypes.c_void_p), len(scene.lights), ctypes.byref(fr["_c"]), width, height,
+                      ns_aa, max_depth, ns_area_light, rng, seed, _ptr(hdr), _ptr(rgba), threads)
+    if rc != 0:
+        raise ValueError("orc_render: bad arguments")
+    return {"hdr": hdr, "rgba": rgba, "frame": fr}
 
 
 def max_threads() -> int:

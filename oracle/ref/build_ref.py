@@ -13,8 +13,10 @@ Two stages, both writing only under ``oracle/_ref/`` (git-ignored):
 2. ``compile()`` — needs only the staged tree, so it also runs on a machine without
    the reference checkout. Compiles the staged translation units with the driver
    ``oracle/ref/ref_driver.cpp`` and ``oracle/ref/gl_link_stubs.cpp`` into
-   ``oracle/_ref/pbf_ref_driver`` with ``g++ -O3 -std=gnu++11 -ffp-contract=off``
-   (contraction off so x86-64 and aarch64 round identically).
+   ``oracle/_ref/pbf_ref_driver``, and with the path tracer's units and
+   ``oracle/ref/ref_render.cpp`` into ``oracle/_ref/pbf_ref_render``, with
+   ``g++ -O3 -std=gnu++11 -ffp-contract=off`` (contraction off so x86-64 and aarch64
+   round identically).
 
 Usage: ``python oracle/ref/build_ref.py [--stage-only|--compile-only]``.
 """
@@ -33,6 +35,7 @@ ORACLE = HERE.parent
 OUT = ORACLE / "_ref"
 STAGE = OUT / "src"
 DRIVER = OUT / "pbf_ref_driver"
+RENDER = OUT / "pbf_ref_render"
 
 REFERENCE = Path(os.environ.get("PBF_REFERENCE_DIR", "/root/reference"))
 
@@ -48,6 +51,14 @@ REF_TUS = [
     "CGL/src/color.cpp",
     "CGL/src/spectrum.cpp",
     "CGL/src/matrix3x3.cpp",
+]
+# Further translation units of the renderer driver (the path tracer and what it links).
+RENDER_TUS = [
+    "src/pathtracer.cpp",
+    "src/static_scene/light.cpp",
+    "src/static_scene/environment_light.cpp",
+    "src/camera.cpp",
+    "CGL/src/lodepng.cpp",
 ]
 # Header trees the step's includes reach.
 REF_HEADER_DIRS = ["src", "CGL/include"]
@@ -107,7 +118,7 @@ def stage(reference: Path = REFERENCE) -> None:
             dst = STAGE / src.relative_to(reference)
             dst.parent.mkdir(parents=True, exist_ok=True)
             shutil.copy2(src, dst)
-    for tu in REF_TUS:
+    for tu in REF_TUS + RENDER_TUS:
         dst = STAGE / tu
         dst.parent.mkdir(parents=True, exist_ok=True)
         shutil.copy2(reference / tu, dst)
@@ -131,11 +142,12 @@ def compile(jobs: int = 8, cxx: str = "g++") -> Path:
         "-I", str(STAGE / "CGL" / "include"), "-I", str(STAGE / "CGL" / "include" / "CGL"),
         "-I", str(STAGE / "src"),
     ]
-    sources = [STAGE / tu for tu in REF_TUS] + [
+    common = [STAGE / tu for tu in REF_TUS] + [
         STAGE / "src" / "particles_param.cpp",
-        HERE / "ref_driver.cpp",
         HERE / "gl_link_stubs.cpp",
     ]
+    render = [STAGE / tu for tu in RENDER_TUS] + [HERE / "ref_render.cpp"]
+    sources = common + [HERE / "ref_driver.cpp"] + render
 
     def cc(src: Path) -> Path:
         obj = obj_dir / (src.name.replace(".cpp", ".o"))
@@ -145,8 +157,10 @@ def compile(jobs: int = 8, cxx: str = "g++") -> Path:
         return obj
 
     with ThreadPoolExecutor(max_workers=jobs) as ex:
-        objs = list(ex.map(cc, sources))
-    subprocess.run([cxx, "-o", str(DRIVER), *map(str, objs)], check=True)
+        objs = dict(zip(sources, ex.map(cc, sources)))
+    base = [str(objs[s]) for s in common]
+    subprocess.run([cxx, "-o", str(DRIVER), *base, str(objs[HERE / "ref_driver.cpp"])], check=True)
+    subprocess.run([cxx, "-o", str(RENDER), *base, *(str(objs[s]) for s in render), "-pthread"], check=True)
     return DRIVER
 
 

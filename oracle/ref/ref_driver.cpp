@@ -45,6 +45,7 @@
 
 #include "particles.h"  // includes marching.h (polygonise), which has no include guard
 #include "ref_params.h"
+#include "ref_surface.h"
 #include "static_scene/marching_triangle.h"
 
 double pbf_ref_dt = 0.016;
@@ -279,32 +280,7 @@ int main(int argc, char** argv) {
   std::vector<int64_t> scube;
   if (flags & 16) {
     std::cout.rdbuf(sink.rdbuf());
-    const double iso = 0.95 * rest_density, fstep = pbf_ref_h * 0.5;
-    const double xmin = P.getParticlesAxisMin(0), ymin = P.getParticlesAxisMin(1), zmin = P.getParticlesAxisMin(2);
-    const double xmax = P.getParticlesAxisMax(0), ymax = P.getParticlesAxisMax(1), zmax = P.getParticlesAxisMax(2);
-    const int xsteps = (int)((xmax - xmin) / fstep), ysteps = (int)((ymax - ymin) / fstep),
-              zsteps = (int)((zmax - zmin) / fstep);
-    for (int ix = 0; ix <= xsteps; ix++)
-      for (int iy = 0; iy <= ysteps; iy++)
-        for (int iz = 0; iz <= zsteps; iz++) {
-          const double x1 = xmin + ix * fstep, x2 = std::min(xmax, x1 + fstep);
-          const double y1 = ymin + iy * fstep, y2 = std::min(ymax, y1 + fstep);
-          const double z1 = zmin + iz * fstep, z2 = std::min(zmax, z1 + fstep);
-          GridCell grid = P.generateGridCell(x1, x2, y1, y2, z1, z2);
-          std::vector<TriangleVertices*> tris = polygonise(grid, iso);
-          for (TriangleVertices* t : tris) {
-            for (int v = 0; v < 3; v++) {
-              Vector3D q = t->p[v];
-              Vector3D nq = P.getVertexNormal(q);
-              for (int k = 0; k < 3; k++) {
-                sxyz.push_back(q[k]);
-                snrm.push_back(nq[k]);
-              }
-            }
-            scube.push_back((static_cast<int64_t>(ix) * (ysteps + 1) + iy) * (zsteps + 1) + iz);
-            delete t;
-          }
-        }
+    pbf_ref::surface_triangles(P, 0.95 * rest_density, pbf_ref_h * 0.5, &sxyz, &snrm, &scube);
     std::cout.rdbuf(old_out);
   }
   std::ofstream out(argv[2], std::ios::binary);

@@ -105,3 +105,131 @@ def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool 
         out["surf_nrm"] = take(np.float64, 9 * nt).reshape(nt, 3, 3)
         out["surf_cube"] = take(np.int64, nt)
     return out
+
+
+RENDER = Path(__file__).resolve().parent / "_ref" / "pbf_ref_render"
+
+
+def read_png(path) -> np.ndarray:
+    """A non-interlaced PNG as lodepng::encode writes it (it picks the smallest colour
+    type: grey, RGB, palette or RGBA) -> (H, W, 4) uint8 RGBA."""
+    import zlib
+
+    data = Path(path).read_bytes()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n", "not a PNG"
+    off, idat, w, h, depth, ctype, plte, trns = 8, b"", 0, 0, 8, 6, None, None
+    while off < len(data):
+        (ln,) = struct.unpack_from(">I", data, off)
+        kind = data[off + 4:off + 8]
+        body = data[off + 8:off + 8 + ln]
+        off += 12 + ln
+        if kind == b"IHDR":
+            w, h, depth, ctype, _, _, interlace = struct.unpack(">IIBBBBB", body)
+            assert interlace == 0 and (depth == 8 or ctype in (0, 3)), "unsupported PNG"
+        elif kind == b"PLTE":
+            plte = np.frombuffer(body, dtype=np.uint8).reshape(-1, 3)
+        elif kind == b"tRNS":
+            trns = np.frombuffer(body, dtype=np.uint8)
+        elif kind == b"IDAT":
+            idat += body
+        elif kind == b"IEND":
+            break
+    chans = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    stride = (w * chans * depth + 7) // 8
+    bpp = max(1, chans * depth // 8)
+    raw = np.frombuffer(zlib.decompress(idat), dtype=np.uint8).reshape(h, 1 + stride)
+    rows = np.zeros((h, stride), dtype=np.int32)
+    for y in range(h):
+        ft, line = raw[y, 0], raw[y, 1:].astype(np.int32)
+        prev = rows[y - 1] if y else np.zeros(stride, dtype=np.int32)
+        cur = np.zeros(stride, dtype=np.int32)
+        for x in range(stride):
+            a = cur[x - bpp] if x >= bpp else 0
+            b = prev[x]
+            c = prev[x - bpp] if x >= bpp else 0
+            if ft == 0:
+                p = 0
+            elif ft == 1:
+                p = a
+            elif ft == 2:
+                p = b
+            elif ft == 3:
+                p = (a + b) // 2
+            else:
+                pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
+                p = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+            cur[x] = (line[x] + p) & 255
+        rows[y] = cur
+    rows = rows.astype(np.uint8)
+    if depth < 8:
+        bits = np.unpackbits(rows, axis=1).reshape(h, -1, depth)
+        vals = np.zeros(bits.shape[:2], dtype=np.int32)
+        for k in range(depth):
+            vals = vals * 2 + bits[:, :, k]
+        samples = vals[:, :w * chans].astype(np.uint8)
+    else:
+        samples = rows[:, :w * chans]
+    px = samples.reshape(h, w, chans)
+    out = np.full((h, w, 4), 255, dtype=np.uint8)
+    if ctype == 3:
+        out[..., :3] = plte[px[..., 0]]
+        if trns is not None:
+            alpha = np.full(len(plte), 255, dtype=np.uint8)
+            alpha[:len(trns)] = trns
+            out[..., 3] = alpha[px[..., 0]]
+    elif ctype in (0, 4):
+        g = px[..., 0] * (255 // ((1 << depth) - 1)) if depth < 8 else px[..., 0]
+        out[..., 0] = out[..., 1] = out[..., 2] = g
+        if ctype == 4:
+            out[..., 3] = px[..., 1]
+    else:
+        out[..., :chans] = px
+    return out
+
+
+def render_available() -> bool:
+    return RENDER.is_file() and os.access(RENDER, os.X_OK)
+
+
+def render(scene, cam, pos, params, width: int, height: int, ns_aa: int = 1, max_depth: int = 1,
+           ns_area_light: int = 1, seed: int = 1, timeout: float | None = None) -> dict:
+    """One frame of the reference's PathTracer::render_to_file over ``scene`` (a
+    fluid_gb300.render.RenderScene) plus the surface of particles ``pos``, camera ``cam``
+    (CameraDesc), random numbers from srand(seed). Returns ``rgba`` (H, W, 4) from the
+    PNG, the camera's ``position`` / ``up`` / ``vfov`` after configure + place, the fluid
+    surface triangles ``surf_xyz`` / ``surf_nrm`` (T, 3, 3) and ``seconds``."""
+    if not render_available():
+        raise FileNotFoundError(f"reference renderer not built: {RENDER}")
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    with tempfile.TemporaryDirectory() as td:
+        fin, fpng, fout = Path(td) / "in.bin", Path(td) / "out.png", Path(td) / "out.bin"
+        with open(fin, "wb") as f:
+            f.write(b"PBFRNDI1")
+            f.write(struct.pack("<10q", len(pos), width, height, ns_aa, max_depth, ns_area_light, seed,
+                                len(scene.tri), len(scene.materials), len(scene.lights)))
+            f.write(struct.pack("<3d", params.h, params.h2, params.rest_density))
+            f.write(pos.tobytes())
+            f.write(np.ascontiguousarray(scene.tri, dtype=np.float64).tobytes())
+            f.write(np.ascontiguousarray(scene.nrm, dtype=np.float64).tobytes())
+            f.write(np.ascontiguousarray(scene.tri_mat, dtype=np.int64).tobytes())
+            for m in scene.materials:
+                f.write(struct.pack("<q7d", m.kind, *m.c1, *m.c2, m.ior))
+            for l in scene.lights:
+                f.write(struct.pack("<q15d", l.kind, *l.radiance, *l.position, *l.direction, *l.dim_x, *l.dim_y))
+            f.write(struct.pack("<12d", cam.hfov, cam.vfov, cam.nclip, cam.fclip, *cam.target, cam.phi, cam.theta,
+                                cam.r, cam.min_r, cam.max_r))
+        subprocess.run([str(RENDER), str(fin), str(fpng), str(fout)], check=True, timeout=timeout,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        rgba = read_png(fpng)
+        buf = fout.read_bytes()
+    assert buf[:8] == b"PBFRNDO1"
+    off = 8
+    position = np.frombuffer(buf, np.float64, 3, off); off += 24
+    up = np.frombuffer(buf, np.float64, 3, off); off += 24
+    (vfov,) = struct.unpack_from("<d", buf, off); off += 8
+    (nt,) = struct.unpack_from("<q", buf, off); off += 8
+    sxyz = np.frombuffer(buf, np.float64, 9 * nt, off).reshape(nt, 3, 3); off += 72 * nt
+    snrm = np.frombuffer(buf, np.float64, 9 * nt, off).reshape(nt, 3, 3); off += 72 * nt
+    (seconds,) = struct.unpack_from("<d", buf, off)
+    return {"rgba": rgba, "position": position.copy(), "up": up.copy(), "vfov": vfov, "surf_xyz": sxyz.copy(),
+            "surf_nrm": snrm.copy(), "seconds": seconds}
