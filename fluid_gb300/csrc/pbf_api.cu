@@ -164,6 +164,7 @@ void Handle::free_all() {
   surf_table_dev = nullptr;
   if (mesh_dev) cudaFree(mesh_dev);
   mesh_dev = nullptr;
+  render.release();
   snap_pos = snap_vel = nullptr;
   snap_id = nullptr;
   snap_valid = false;
@@ -782,62 +783,85 @@ void pbf_mc_table(uint16_t* edges, uint8_t* ntri, int8_t* tri) {
   if (tri) std::memcpy(tri, t.tri, sizeof(t.tri));
 }
 
+namespace pbf {
+
+// The cube grid of Particles::getSurfacePrims over [lo, hi] (NULL: the reference's fixed
+// bounds, particles.cpp:330-349), the per-cube triangle counts of the current state and
+// their total; the counts stay in the handle's scratch for surface_emit.
+pbf_status Handle::surface_count(double isolevel, double step, const double* lo, const double* hi, SurfGrid* g,
+                                 uint32_t* total) {
+  if (!(step > 0) || !std::isfinite(step) || !std::isfinite(isolevel))
+    return fail(PBF_ERR_INVALID, "step must be positive and isolevel finite");
+  static const double kLo[3] = {-1.0, 0.0, -1.0}, kHi[3] = {1.0, 1.5, 1.0};  // particles.cpp:330-349
+  g->step = step;
+  double cubes = 1.0;
+  for (int a = 0; a < 3; ++a) {
+    g->lo[a] = lo ? lo[a] : kLo[a];
+    g->hi[a] = hi ? hi[a] : kHi[a];
+    if (!std::isfinite(g->lo[a]) || !std::isfinite(g->hi[a]) || g->hi[a] < g->lo[a])
+      return fail(PBF_ERR_INVALID, "surface bounds must be finite with hi >= lo");
+    const double steps = std::floor((g->hi[a] - g->lo[a]) / step);
+    if (steps > 4095) return fail(PBF_ERR_INVALID, "surface grid too fine: at most 4096 cubes per axis");
+    g->nc[a] = static_cast<int>(steps) + 1;
+    cubes *= g->nc[a];
+  }
+  if (cubes > 2.0e9) return fail(PBF_ERR_INVALID, "surface grid too large");
+  *total = 0;
+  if (b.n == 0) return PBF_OK;
+  pbf_status st = cuda(launch_resort(b, dp, tune, cur, stream), "resort");
+  if (st != PBF_OK) return st;
+  cur ^= 1;
+  nbr_valid = false;
+  drop_graphs();
+  if (!surf_table_dev) {
+    st = cuda(cudaMalloc(&surf_table_dev, sizeof(SurfTable)), "cudaMalloc(table)");
+    if (st != PBF_OK) return st;
+    st = cuda(cudaMemcpy(surf_table_dev, &surf_table(), sizeof(SurfTable), cudaMemcpyHostToDevice), "H2D table");
+    if (st != PBF_OK) return st;
+  }
+  const size_t nc = static_cast<size_t>(cubes);
+  const size_t corners = static_cast<size_t>(g->nc[0] + 1) * (g->nc[1] + 1) * (g->nc[2] + 1);
+  const size_t tiles = exclusive_scan_tiles(static_cast<uint32_t>(nc));
+  st = ensure_scratch(4 * (corners + nc + (nc + 1) + tiles) + 256);
+  if (st != PBF_OK) return st;
+  float* field = static_cast<float*>(scratch);
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(field + corners);
+  uint32_t* first = cnt + nc;
+  uint32_t* tile = first + nc + 1;
+  st = cuda(launch_surface_count(b, dp, cur, *g, static_cast<float>(isolevel), surf_table_dev, field, cnt, first,
+                                 tile, stream),
+            "surface count");
+  if (st != PBF_OK) return st;
+  st = cuda(cudaMemcpyAsync(total, first + nc, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "D2H");
+  if (st == PBF_OK) st = cuda(cudaStreamSynchronize(stream), "sync");
+  return st;
+}
+
+// The first min(cap, total) triangles of the last surface_count into DEVICE arrays.
+pbf_status Handle::surface_emit(const SurfGrid& g, double isolevel, float* xyz, float* nrm, uint32_t cap) {
+  if (cap == 0 || b.n == 0) return PBF_OK;
+  const size_t nc = static_cast<size_t>(g.nc[0]) * g.nc[1] * g.nc[2];
+  const size_t corners = static_cast<size_t>(g.nc[0] + 1) * (g.nc[1] + 1) * (g.nc[2] + 1);
+  const float* field = static_cast<const float*>(scratch);
+  const uint32_t* first = reinterpret_cast<const uint32_t*>(field + corners) + nc;
+  return cuda(launch_surface_emit(b, dp, cur, g, static_cast<float>(isolevel), surf_table_dev, field, first, xyz, nrm,
+                                  cap, stream),
+              "surface emit");
+}
+
+}  // namespace pbf
+
 pbf_status pbf_surface(pbf_handle* hh, double isolevel, double step, const double* lo, const double* hi,
                        float* xyz, float* nrm, size_t cap, size_t* count) {
   if (!hh) return PBF_ERR_INVALID;
   Handle* h = reinterpret_cast<Handle*>(hh);
   if (!count) return h->fail(PBF_ERR_INVALID, "count is NULL");
   if (cap && (!xyz || !nrm)) return h->fail(PBF_ERR_INVALID, "xyz / nrm is NULL");
-  if (!(step > 0) || !std::isfinite(step) || !std::isfinite(isolevel))
-    return h->fail(PBF_ERR_INVALID, "step must be positive and isolevel finite");
-  static const double kLo[3] = {-1.0, 0.0, -1.0}, kHi[3] = {1.0, 1.5, 1.0};  // particles.cpp:330-349
-  pbf::SurfGrid g;
-  g.step = step;
-  double cubes = 1.0;
-  for (int a = 0; a < 3; ++a) {
-    g.lo[a] = lo ? lo[a] : kLo[a];
-    g.hi[a] = hi ? hi[a] : kHi[a];
-    if (!std::isfinite(g.lo[a]) || !std::isfinite(g.hi[a]) || g.hi[a] < g.lo[a])
-      return h->fail(PBF_ERR_INVALID, "surface bounds must be finite with hi >= lo");
-    const double steps = std::floor((g.hi[a] - g.lo[a]) / step);
-    if (steps > 4095) return h->fail(PBF_ERR_INVALID, "surface grid too fine: at most 4096 cubes per axis");
-    g.nc[a] = static_cast<int>(steps) + 1;
-    cubes *= g.nc[a];
-  }
-  if (cubes > 2.0e9) return h->fail(PBF_ERR_INVALID, "surface grid too large");
   *count = 0;
   pbf::DeviceGuard dg(h->device);
-  if (h->b.n == 0) return PBF_OK;
-  pbf_status st = h->cuda(pbf::launch_resort(h->b, h->dp, h->tune, h->cur, h->stream), "resort");
-  if (st != PBF_OK) return st;
-  h->cur ^= 1;
-  h->nbr_valid = false;
-  h->drop_graphs();
-  if (!h->surf_table_dev) {
-    st = h->cuda(cudaMalloc(&h->surf_table_dev, sizeof(pbf::SurfTable)), "cudaMalloc(table)");
-    if (st != PBF_OK) return st;
-    st = h->cuda(cudaMemcpy(h->surf_table_dev, &pbf::surf_table(), sizeof(pbf::SurfTable), cudaMemcpyHostToDevice),
-                 "H2D table");
-    if (st != PBF_OK) return st;
-  }
-  const size_t nc = static_cast<size_t>(cubes);
-  const size_t corners = static_cast<size_t>(g.nc[0] + 1) * (g.nc[1] + 1) * (g.nc[2] + 1);
-  const size_t tiles = pbf::exclusive_scan_tiles(static_cast<uint32_t>(nc));
-  const size_t need = 4 * (corners + nc + (nc + 1) + tiles) + 256;
-  st = h->ensure_scratch(need);
-  if (st != PBF_OK) return st;
-  float* field = static_cast<float*>(h->scratch);
-  uint32_t* cnt = reinterpret_cast<uint32_t*>(field + corners);
-  uint32_t* first = cnt + nc;
-  uint32_t* tile = first + nc + 1;
-  const float iso = static_cast<float>(isolevel);
-  st = h->cuda(pbf::launch_surface_count(h->b, h->dp, h->cur, g, iso, h->surf_table_dev, field, cnt, first, tile,
-                                         h->stream),
-               "surface count");
-  if (st != PBF_OK) return st;
+  pbf::SurfGrid g;
   uint32_t total = 0;
-  st = h->cuda(cudaMemcpyAsync(&total, first + nc, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream), "D2H");
-  if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "sync");
+  pbf_status st = h->surface_count(isolevel, step, lo, hi, &g, &total);
   if (st != PBF_OK) return st;
   *count = total;
   const size_t m = std::min(static_cast<size_t>(total), cap);
@@ -845,9 +869,7 @@ pbf_status pbf_surface(pbf_handle* hh, double isolevel, double step, const doubl
   float* dev = nullptr;
   st = h->cuda(cudaMalloc(&dev, sizeof(float) * 18 * m), "cudaMalloc(surface)");
   if (st != PBF_OK) return st;
-  st = h->cuda(pbf::launch_surface_emit(h->b, h->dp, h->cur, g, iso, h->surf_table_dev, field, first, dev,
-                                        dev + 9 * m, static_cast<uint32_t>(m), h->stream),
-               "surface emit");
+  st = h->surface_emit(g, isolevel, dev, dev + 9 * m, static_cast<uint32_t>(m));
   if (st == PBF_OK)
     st = h->cuda(cudaMemcpyAsync(xyz, dev, sizeof(float) * 9 * m, cudaMemcpyDeviceToHost, h->stream), "D2H");
   if (st == PBF_OK)

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "pbf_internal.h"
+#include "pbf_render.h"
 
 namespace pbf {
 
@@ -59,6 +60,7 @@ struct Handle {
   Tape tape;                 // recording + work arrays of the adjoint (first use)
   SurfTable* surf_table_dev = nullptr;  // marching-cubes table (first pbf_surface)
   float4* mesh_dev = nullptr;           // collider triangles (pbf_set_collider_mesh)
+  RenderState render;                   // path tracer (pbf_render_set_scene, pbf_render)
   double phase_ms[kNumPhases] = {};
   uint64_t phase_launches[kNumPhases] = {};
 
@@ -69,6 +71,9 @@ struct Handle {
   pbf_status ensure_scratch(size_t bytes);
   pbf_status ensure_tape();
   void free_tape();
+  pbf_status surface_count(double isolevel, double step, const double* lo, const double* hi, SurfGrid* g,
+                           uint32_t* total);
+  pbf_status surface_emit(const SurfGrid& g, double isolevel, float* xyz, float* nrm, uint32_t cap);
   pbf_status enqueue_steps(float dt, int nsteps);
   pbf_status sync_and_check();
   void drop_graphs();

@@ -1,0 +1,693 @@
+// Path tracer of the fluid surface and its scene for sm_103a: the reference's
+// PathTracer (src/pathtracer.cpp:483-632) on the GPU, one thread per pixel.
+//
+//   k_surf_tris        marching-cubes output -> ray-test triangles (fluid material)
+//   k_bounds_*         bounds of the triangle centroids
+//   k_morton           30-bit Morton code of each centroid
+//   k_sort_*           stable LSD radix sort of the codes (4 passes of 8 bits)
+//   k_tree             binary radix tree over the sorted codes (Karras 2012,
+//                      "Maximizing parallelism in the construction of BVHs, octrees
+//                      and k-d trees"), ties broken by sorted position
+//   k_refit            bottom-up boxes: the second child to finish fills its parent
+//   k_render           camera rays, closest hits, direct light from every light,
+//                      one BSDF-sampled bounce per level with Russian roulette
+//   k_tonemap          HDRImageBuffer::toColor + ImageBuffer::update_pixel
+//
+// Every random number is a pure function of (seed, pixel, sample, draw index), so a
+// frame does not depend on scheduling: draw k of sample s of pixel p is the top 24 bits
+// of splitmix64(key(p, s) + k * 0x9E3779B97F4A7C15) times 2^-24 (splitmix64: Steele,
+// Lea and Flood, "Fast splittable pseudorandom number generators", 2014). The draws
+// are consumed in the reference's order: camera jitter (x, y) when ns_aa > 1; at each
+// hit, per light and sample the light's draws, then the BSDF's, then the roulette coin.
+#include <cfloat>
+#include <cstdint>
+
+#include "pbf_internal.h"
+#include "pbf_render.h"
+
+namespace pbf {
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr uint32_t kSortTile = kSortThreads * kSortItems;
+constexpr float kPi = 3.14159265358979323846f;
+
+// ---- small vector helpers --------------------------------------------------------------
+struct V3 {
+  float x, y, z;
+};
+__device__ __forceinline__ V3 mk(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 v3(const float4& a) { return V3{a.x, a.y, a.z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(V3 a, float c) { return mk(a.x * c, a.y * c, a.z * c); }
+__device__ __forceinline__ V3 operator*(float c, V3 a) { return mk(a.x * c, a.y * c, a.z * c); }
+__device__ __forceinline__ V3 mulv(V3 a, V3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 cross(V3 u, V3 v) {
+  return mk(u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x);
+}
+__device__ __forceinline__ V3 unit(V3 a) { return a * rsqrtf(dot(a, a)); }
+__device__ __forceinline__ V3 ld3(const float* p) { return mk(p[0], p[1], p[2]); }
+__device__ __forceinline__ float illum(V3 s) { return 0.2126f * s.x + 0.7152f * s.y + 0.0722f * s.z; }
+
+// ---- random numbers --------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+  unsigned long long z = x + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+struct Rng {
+  unsigned long long key;
+  unsigned long long k;
+  __device__ __forceinline__ float next() {
+    const unsigned long long z = splitmix64(key + (k++) * 0x9E3779B97F4A7C15ull);
+    return static_cast<float>(z >> 40) * (1.0f / 16777216.0f);
+  }
+};
+__device__ __forceinline__ unsigned long long path_key(unsigned long long seed, unsigned long long pixel,
+                                                       unsigned long long sample) {
+  return splitmix64(seed ^ splitmix64((pixel << 20) ^ sample));
+}
+
+// ---- surface triangles -----------------------------------------------------------------------
+__global__ void k_surf_tris(const float* __restrict__ xyz, const float* __restrict__ nrm, uint32_t m, int material,
+                            RTri* __restrict__ tri, RNrm* __restrict__ nn) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const float* p = xyz + 9 * static_cast<size_t>(i);
+  const float* q = nrm + 9 * static_cast<size_t>(i);
+  tri[i] = RTri{make_float4(p[0], p[1], p[2], __int_as_float(material)), make_float4(p[3], p[4], p[5], 0.f),
+                make_float4(p[6], p[7], p[8], 0.f)};
+  nn[i] = RNrm{make_float4(q[0], q[1], q[2], 0.f), make_float4(q[3], q[4], q[5], 0.f),
+               make_float4(q[6], q[7], q[8], 0.f)};
+}
+
+// ---- BVH build -------------------------------------------------------------------------------
+__device__ __forceinline__ V3 centroid(const RTri& t) {
+  return mk((t.p1.x + t.p2.x + t.p3.x) * (1.f / 3.f), (t.p1.y + t.p2.y + t.p3.y) * (1.f / 3.f),
+            (t.p1.z + t.p2.z + t.p3.z) * (1.f / 3.f));
+}
+
+__device__ __forceinline__ void block_minmax(V3& lo, V3& hi) {
+  __shared__ float s[6][32];
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  float v[6] = {lo.x, lo.y, lo.z, hi.x, hi.y, hi.z};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const float u = __shfl_xor_sync(0xffffffffu, v[c], o);
+      v[c] = c < 3 ? fminf(v[c], u) : fmaxf(v[c], u);
+    }
+  if (lane == 0)
+    for (int c = 0; c < 6; ++c) s[c][warp] = v[c];
+  __syncthreads();
+  if (warp == 0) {
+    const unsigned nw = blockDim.x >> 5;
+    for (int c = 0; c < 6; ++c) v[c] = lane < nw ? s[c][lane] : (c < 3 ? FLT_MAX : -FLT_MAX);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const float u = __shfl_xor_sync(0xffffffffu, v[c], o);
+        v[c] = c < 3 ? fminf(v[c], u) : fmaxf(v[c], u);
+      }
+  }
+  lo = mk(v[0], v[1], v[2]);
+  hi = mk(v[3], v[4], v[5]);
+}
+
+// bounds[2 + 2 b], bounds[3 + 2 b]: the centroid box of block b's share
+__global__ void __launch_bounds__(256) k_bounds_part(const RTri* __restrict__ tri, uint32_t n, float4* bounds) {
+  V3 lo = mk(FLT_MAX, FLT_MAX, FLT_MAX), hi = mk(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const V3 c = centroid(tri[i]);
+    lo = mk(fminf(lo.x, c.x), fminf(lo.y, c.y), fminf(lo.z, c.z));
+    hi = mk(fmaxf(hi.x, c.x), fmaxf(hi.y, c.y), fmaxf(hi.z, c.z));
+  }
+  block_minmax(lo, hi);
+  if (threadIdx.x == 0) {
+    bounds[2 + 2 * blockIdx.x] = make_float4(lo.x, lo.y, lo.z, 0.f);
+    bounds[3 + 2 * blockIdx.x] = make_float4(hi.x, hi.y, hi.z, 0.f);
+  }
+}
+
+__global__ void __launch_bounds__(kBoundsBlocks) k_bounds_final(float4* bounds) {
+  const float4 a = bounds[2 + 2 * threadIdx.x], b = bounds[3 + 2 * threadIdx.x];
+  V3 lo = v3(a), hi = v3(b);
+  block_minmax(lo, hi);
+  if (threadIdx.x == 0) {
+    bounds[0] = make_float4(lo.x, lo.y, lo.z, 0.f);
+    bounds[1] = make_float4(hi.x, hi.y, hi.z, 0.f);
+  }
+}
+
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {  // 10 bits -> every third bit
+  v = (v * 0x00010001u) & 0xFF0000FFu;
+  v = (v * 0x00000101u) & 0x0F00F00Fu;
+  v = (v * 0x00000011u) & 0xC30C30C3u;
+  v = (v * 0x00000005u) & 0x49249249u;
+  return v;
+}
+
+__global__ void k_morton(const RTri* __restrict__ tri, uint32_t n, const float4* __restrict__ bounds,
+                         uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const V3 lo = v3(bounds[0]), hi = v3(bounds[1]);
+  const V3 c = centroid(tri[i]);
+  const float e[3] = {hi.x - lo.x, hi.y - lo.y, hi.z - lo.z};
+  const float r[3] = {c.x - lo.x, c.y - lo.y, c.z - lo.z};
+  uint32_t q[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float f = e[a] > 0.f ? r[a] / e[a] : 0.f;
+    q[a] = static_cast<uint32_t>(fminf(fmaxf(f * 1024.f, 0.f), 1023.f));
+  }
+  keys[i] = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+  vals[i] = i;
+}
+
+// hist[d * nb + b]: count of digit d in tile b
+__global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
+                                                             uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t base = blockIdx.x * kSortTile;
+  for (int k = 0; k < kSortItems; ++k) {
+    const uint32_t i = base + k * kSortThreads + threadIdx.x;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter: the tile's items go in order, 256 at a time; an item's place is its
+// digit's running start + the same-digit items before it in earlier warps of the chunk
+// + those before it in its own warp.
+__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* __restrict__ keys,
+                                                                const uint32_t* __restrict__ vals, uint32_t n,
+                                                                int shift, const uint32_t* __restrict__ start,
+                                                                uint32_t* __restrict__ keys_out,
+                                                                uint32_t* __restrict__ vals_out) {
+  constexpr int W = kSortThreads / 32;
+  __shared__ uint32_t run[256];
+  __shared__ uint32_t cnt[W][256];
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  run[threadIdx.x] = start[threadIdx.x * gridDim.x + blockIdx.x];
+  const uint32_t base = blockIdx.x * kSortTile;
+  for (int k = 0; k < kSortItems; ++k) {
+    for (int w = 0; w < W; ++w) cnt[w][threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t i = base + k * kSortThreads + threadIdx.x;
+    const bool live = i < n;
+    const uint32_t key = live ? keys[i] : 0u;
+    const uint32_t d = live ? ((key >> shift) & 255u) : 256u;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    if (live && lane == static_cast<unsigned>(__ffs(peers) - 1)) cnt[warp][d] = __popc(peers);
+    __syncthreads();
+    if (live) {
+      uint32_t pre = 0;
+      for (unsigned w = 0; w < warp; ++w) pre += cnt[w][d];
+      const uint32_t pos = run[d] + pre + __popc(peers & lt);
+      keys_out[pos] = key;
+      vals_out[pos] = vals[i];
+    }
+    __syncthreads();
+    uint32_t add = 0;
+    for (int w = 0; w < W; ++w) add += cnt[w][threadIdx.x];
+    run[threadIdx.x] += add;
+    __syncthreads();
+  }
+}
+
+// Common-prefix length of the augmented keys (code, sorted position) of a and b.
+__device__ __forceinline__ int prefix(const uint32_t* __restrict__ keys, int n, int a, int b) {
+  if (b < 0 || b >= n) return -1;
+  const unsigned long long ka = (static_cast<unsigned long long>(keys[a]) << 32) | static_cast<uint32_t>(a);
+  const unsigned long long kb = (static_cast<unsigned long long>(keys[b]) << 32) | static_cast<uint32_t>(b);
+  return __clzll(ka ^ kb);
+}
+
+// Internal node i of n - 1 (node 0 is the root); children: internal index, or kLeafBit |
+// sorted position. parent[] over internal nodes [0, n-1) then leaves [n-1, 2n-1).
+__global__ void k_tree(const uint32_t* __restrict__ keys, int n, BvhNode* __restrict__ nodes,
+                       uint32_t* __restrict__ parent) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int d = (prefix(keys, n, i, i + 1) - prefix(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = prefix(keys, n, i, i - d);
+  int lmax = 2;
+  while (prefix(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
+  int l = 0;
+  for (int t = lmax / 2; t >= 1; t /= 2)
+    if (prefix(keys, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = i + l * d;
+  const int dnode = prefix(keys, n, i, j);
+  int s = 0;
+  for (int t = (l + 1) / 2;; t = (t + 1) / 2) {
+    if (prefix(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    if (t == 1) break;
+  }
+  const int gamma = i + s * d + min(d, 0);
+  const uint32_t left = (min(i, j) == gamma) ? (kLeafBit | static_cast<uint32_t>(gamma)) : static_cast<uint32_t>(gamma);
+  const uint32_t right = (max(i, j) == gamma + 1) ? (kLeafBit | static_cast<uint32_t>(gamma + 1))
+                                                  : static_cast<uint32_t>(gamma + 1);
+  nodes[i].lo_l.w = __uint_as_float(left);
+  nodes[i].lo_r.w = __uint_as_float(right);
+  parent[(left & kLeafBit) ? (n - 1 + (left & ~kLeafBit)) : left] = static_cast<uint32_t>(i);
+  parent[(right & kLeafBit) ? (n - 1 + (right & ~kLeafBit)) : right] = static_cast<uint32_t>(i);
+  if (i == 0) parent[0] = 0xffffffffu;
+}
+
+__device__ __forceinline__ float pad(float v, float s) { return v + s * (1e-6f * fabsf(v) + 1e-7f); }
+
+// One thread per leaf: its triangle's box (padded by a few ulps), then up the tree; the
+// second thread to reach a node writes its children's boxes and its own.
+__global__ void k_refit(const RTri* __restrict__ tri, const uint32_t* __restrict__ vals, int n,
+                        BvhNode* __restrict__ nodes, const uint32_t* __restrict__ parent, uint32_t* flags,
+                        float4* box_lo, float4* box_hi) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const RTri t = tri[vals[k]];
+  const uint32_t self = static_cast<uint32_t>(n - 1 + k);
+  box_lo[self] = make_float4(pad(fminf(fminf(t.p1.x, t.p2.x), t.p3.x), -1.f),
+                             pad(fminf(fminf(t.p1.y, t.p2.y), t.p3.y), -1.f),
+                             pad(fminf(fminf(t.p1.z, t.p2.z), t.p3.z), -1.f), 0.f);
+  box_hi[self] = make_float4(pad(fmaxf(fmaxf(t.p1.x, t.p2.x), t.p3.x), 1.f),
+                             pad(fmaxf(fmaxf(t.p1.y, t.p2.y), t.p3.y), 1.f),
+                             pad(fmaxf(fmaxf(t.p1.z, t.p2.z), t.p3.z), 1.f), 0.f);
+  uint32_t p = parent[self];
+  while (p != 0xffffffffu) {
+    __threadfence();
+    if (atomicAdd(&flags[p], 1u) == 0u) return;  // the sibling finishes this node
+    __threadfence();
+    const uint32_t cl = __float_as_uint(__ldcg(&nodes[p].lo_l.w)), cr = __float_as_uint(__ldcg(&nodes[p].lo_r.w));
+    const uint32_t bl = (cl & kLeafBit) ? static_cast<uint32_t>(n - 1) + (cl & ~kLeafBit) : cl;
+    const uint32_t br = (cr & kLeafBit) ? static_cast<uint32_t>(n - 1) + (cr & ~kLeafBit) : cr;
+    const float4 ll = __ldcg(&box_lo[bl]), lh = __ldcg(&box_hi[bl]);
+    const float4 rl = __ldcg(&box_lo[br]), rh = __ldcg(&box_hi[br]);
+    nodes[p].lo_l = make_float4(ll.x, ll.y, ll.z, __uint_as_float(cl));
+    nodes[p].hi_l = lh;
+    nodes[p].lo_r = make_float4(rl.x, rl.y, rl.z, __uint_as_float(cr));
+    nodes[p].hi_r = rh;
+    box_lo[p] = make_float4(fminf(ll.x, rl.x), fminf(ll.y, rl.y), fminf(ll.z, rl.z), 0.f);
+    box_hi[p] = make_float4(fmaxf(lh.x, rh.x), fmaxf(lh.y, rh.y), fmaxf(lh.z, rh.z), 0.f);
+    p = parent[p];
+  }
+}
+
+// ---- ray queries -------------------------------------------------------------------------------
+struct Ray {
+  V3 o, d, inv;
+  float tmin, tmax;
+};
+__device__ __forceinline__ Ray make_ray(V3 o, V3 d, float tmin, float tmax) {
+  return Ray{o, d, mk(1.f / d.x, 1.f / d.y, 1.f / d.z), tmin, tmax};
+}
+
+// MarchingTriangle::intersect (marching_triangle.cpp:46-73) in FP32
+__device__ __forceinline__ bool tri_test(const RTri& t, const Ray& r, float tmax, float* tt, float* uu, float* vv) {
+  const V3 p1 = v3(t.p1);
+  const V3 e1 = v3(t.p2) - p1, e2 = v3(t.p3) - p1, s = r.o - p1;
+  const V3 s1 = cross(r.d, e2), s2 = cross(s, e1);
+  const float d = dot(s1, e1);
+  if (d == 0.f) return false;
+  const float tv = dot(s2, e2) / d;
+  if (tv < r.tmin || tv > tmax) return false;
+  const float u = dot(s1, s) / d, v = dot(s2, r.d) / d, w = 1.f - u - v;
+  if (u < 0.f || u > 1.f || v < 0.f || v > 1.f || w < 0.f || w > 1.f) return false;
+  *tt = tv;
+  *uu = u;
+  *vv = v;
+  return true;
+}
+
+__device__ __forceinline__ bool box_test(const float4& lo, const float4& hi, const Ray& r, float tmax, float* tn) {
+  const float tx0 = (lo.x - r.o.x) * r.inv.x, tx1 = (hi.x - r.o.x) * r.inv.x;
+  const float ty0 = (lo.y - r.o.y) * r.inv.y, ty1 = (hi.y - r.o.y) * r.inv.y;
+  const float tz0 = (lo.z - r.o.z) * r.inv.z, tz1 = (hi.z - r.o.z) * r.inv.z;
+  const float t0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), r.tmin));
+  const float t1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+  *tn = t0;
+  return t0 <= t1;
+}
+
+// Closest hit (ANY = false) or any hit (ANY = true) below r.tmax; *tri = -1 for none.
+template <bool ANY>
+__device__ bool trace(const BvhNode* __restrict__ nodes, const RTri* __restrict__ tris,
+                      const uint32_t* __restrict__ leaf_tri, uint32_t n, const Ray& r, int* hit_tri, float* ht,
+                      float* hu, float* hv, unsigned* err) {
+  float tmax = r.tmax;
+  int best = -1;
+  float bu = 0.f, bv = 0.f;
+  if (n == 0) return false;
+  if (n == 1) {
+    float t, u, v;
+    if (tri_test(tris[0], r, tmax, &t, &u, &v)) {
+      best = 0;
+      tmax = t;
+      bu = u;
+      bv = v;
+    }
+  } else {
+    uint32_t stack[kBvhStack];
+    int sp = 0;
+    uint32_t node = 0;
+    while (true) {
+      const BvhNode nd = nodes[node];
+      float tl, tr;
+      bool hl = box_test(nd.lo_l, nd.hi_l, r, tmax, &tl);
+      bool hr = box_test(nd.lo_r, nd.hi_r, r, tmax, &tr);
+      const uint32_t cl = __float_as_uint(nd.lo_l.w), cr = __float_as_uint(nd.lo_r.w);
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {
+        const uint32_t c = side ? cr : cl;
+        bool& h = side ? hr : hl;
+        if (h && (c & kLeafBit)) {
+          h = false;
+          const uint32_t ti = leaf_tri[c & ~kLeafBit];
+          float t, u, v;
+          if (tri_test(tris[ti], r, tmax, &t, &u, &v)) {
+            best = static_cast<int>(ti);
+            tmax = t;
+            bu = u;
+            bv = v;
+            if (ANY) {
+              *hit_tri = best;
+              return true;
+            }
+          }
+        }
+      }
+      if (hl && hr) {
+        const bool lfirst = tl <= tr;
+        if (sp < kBvhStack) {
+          stack[sp++] = lfirst ? cr : cl;
+        } else {
+          atomicOr(err, 1u);
+        }
+        node = lfirst ? cl : cr;
+      } else if (hl) {
+        node = cl;
+      } else if (hr) {
+        node = cr;
+      } else {
+        if (sp == 0) break;
+        node = stack[--sp];
+      }
+    }
+  }
+  *hit_tri = best;
+  *ht = tmax;
+  *hu = bu;
+  *hv = bv;
+  return best >= 0;
+}
+
+// ---- BSDFs and lights (bsdf.cpp, light.cpp) --------------------------------------------------------
+struct Frame {
+  V3 x, y, z;
+  __device__ __forceinline__ V3 to_local(V3 w) const { return mk(dot(x, w), dot(y, w), dot(z, w)); }
+  __device__ __forceinline__ V3 to_world(V3 w) const { return x * w.x + y * w.y + z * w.z; }
+};
+
+// make_coord_space (bsdf.cpp:13-32)
+__device__ __forceinline__ Frame coord_space(V3 n) {
+  V3 h = n;
+  if (fabsf(h.x) <= fabsf(h.y) && fabsf(h.x) <= fabsf(h.z)) h.x = 1.f;
+  else if (fabsf(h.y) <= fabsf(h.x) && fabsf(h.y) <= fabsf(h.z)) h.y = 1.f;
+  else h.z = 1.f;
+  const V3 z = unit(n);
+  const V3 y = unit(cross(h, z));
+  const V3 x = unit(cross(z, y));
+  return Frame{x, y, z};
+}
+
+__device__ __forceinline__ bool mat_delta(int kind) {
+  return kind == kMatMirror || kind == kMatGlass || kind == kMatRefraction;
+}
+
+__device__ __forceinline__ V3 cosine_sample(Rng& g, float* pdf) {
+  const float xi1 = g.next(), xi2 = g.next();
+  const float r = sqrtf(xi1), th = 2.f * kPi * xi2;
+  const float c = sqrtf(1.f - xi1);
+  *pdf = c / kPi;
+  float sn, cs;
+  sincosf(th, &sn, &cs);
+  return mk(r * cs, r * sn, c);
+}
+
+// sample_f of each BSDF (bsdf.cpp); wo, wi in the local frame
+__device__ V3 sample_f(const RMat& m, V3 wo, V3* wi, float* pdf, Rng& g) {
+  const V3 c1 = ld3(m.c1), c2 = ld3(m.c2);
+  switch (m.kind) {
+    case kMatDiffuse:
+      *wi = cosine_sample(g, pdf);
+      return c1 * (1.f / kPi);
+    case kMatMirror:
+      *wi = mk(-wo.x, -wo.y, wo.z);
+      *pdf = 1.f;
+      return c1 * (1.f / fabsf(wi->z));
+    case kMatGlass: {
+      const float ior = m.ior;
+      const float no = wo.z > 0.f ? 1.f : ior, ni = wo.z > 0.f ? ior : 1.f;
+      const float sint2 = (1.f - wo.z * wo.z) * no * no / ni / ni;
+      if (sint2 >= 1.f) {  // total internal reflection
+        *wi = mk(-wo.x, -wo.y, wo.z);
+        *pdf = 1.f;
+        return c2 * (1.f / fabsf(wi->z));
+      }
+      const float cost = wo.z > 0.f ? -sqrtf(1.f - sint2) : sqrtf(1.f - sint2);
+      *wi = unit(mk(-wo.x * no / ni, -wo.y * no / ni, cost));
+      float R = (ior - 1.f) * (ior - 1.f) / (ior + 1.f) / (ior + 1.f);
+      const float c = 1.f - fabsf(wi->z);
+      R = R + (1.f - R) * c * c * c * c * c;
+      if (g.next() < R) {
+        *wi = mk(-wo.x, -wo.y, wo.z);
+        *pdf = R;
+        return c2 * (R / fabsf(wi->z));
+      }
+      *pdf = 1.f - R;
+      const float nr = wi->z > 0.f ? ior : 1.f / ior;
+      return c1 * ((1.f - R) * nr * nr / fabsf(wi->z));
+    }
+    case kMatEmission:
+      *wi = cosine_sample(g, pdf);
+      return mk(0.f, 0.f, 0.f);
+    default:  // the reference's RefractionBSDF returns black
+      *wi = mk(0.f, 0.f, 1.f);
+      *pdf = 1.f;
+      return mk(0.f, 0.f, 0.f);
+  }
+}
+
+__device__ V3 sample_L(const RLight& l, V3 p, V3* wi, float* dist, float* pdf, Rng& g) {
+  switch (l.kind) {
+    case kLightDirectional:
+      *wi = ld3(l.dir);
+      *dist = FLT_MAX;
+      *pdf = 1.f;
+      return ld3(l.rad);
+    case kLightHemisphere: {
+      const float xi1 = g.next(), xi2 = g.next();
+      const float th = acosf(xi1), ph = 2.f * kPi * xi2;
+      const float xs = sinf(th) * cosf(ph), ys = sinf(th) * sinf(ph), zs = cosf(th);
+      *wi = mk(xs, zs, -ys);  // sampleToWorld columns (1,0,0), (0,0,-1), (0,1,0)
+      *dist = FLT_MAX;
+      *pdf = 1.f / (2.f * kPi);
+      return ld3(l.rad);
+    }
+    case kLightPoint: {
+      const V3 d = ld3(l.pos) - p;
+      const float len = sqrtf(dot(d, d));
+      *wi = d * (1.f / len);
+      *dist = len;
+      *pdf = 1.f;
+      return ld3(l.rad);
+    }
+    default: {  // area (light.cpp:79-93)
+      const float sx = g.next() - 0.5f, sy = g.next() - 0.5f;
+      const V3 d = ld3(l.pos) + sx * ld3(l.dx) + sy * ld3(l.dy) - p;
+      const float cosTheta = dot(d, ld3(l.dir));
+      const float sq = dot(d, d);
+      const float dd = sqrtf(sq);
+      *wi = d * (1.f / dd);
+      *dist = dd;
+      *pdf = sq / (l.area * fabsf(cosTheta));
+      return cosTheta < 0.f ? ld3(l.rad) : mk(0.f, 0.f, 0.f);
+    }
+  }
+}
+
+// ---- the path tracer ---------------------------------------------------------------------------
+struct Scene {
+  const BvhNode* nodes;
+  const RTri* tri;
+  const RNrm* nrm;
+  const uint32_t* leaf_tri;
+  uint32_t n;
+  const RMat* mats;
+  const RLight* lights;
+};
+
+__global__ void __launch_bounds__(128) k_render(Scene sc, RCam cam, RArgs a, float* __restrict__ hdr, unsigned* err) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= a.width * a.height) return;
+  const int px = pix % a.width, py = pix / a.width;
+  const V3 cpos = ld3(cam.pos), cx = ld3(cam.c2w), cy = ld3(cam.c2w + 3), cz = ld3(cam.c2w + 6);
+  V3 sum = mk(0.f, 0.f, 0.f);
+  for (int s = 0; s < a.ns_aa; ++s) {
+    Rng g{path_key(a.seed, static_cast<unsigned long long>(pix), static_cast<unsigned long long>(s)), 0ull};
+    float jx = 0.5f, jy = 0.5f;
+    if (a.ns_aa > 1) {
+      jx = g.next();
+      jy = g.next();
+    }
+    const float xn = (px + jx) / a.width, yn = (py + jy) / a.height;
+    const V3 dir = unit(cx * ((xn - 0.5f) * cam.htan) + cy * ((yn - 0.5f) * cam.vtan) - cz);
+    Ray r = make_ray(cpos, dir, cam.nclip, cam.fclip);
+    V3 L = mk(0.f, 0.f, 0.f), beta = mk(1.f, 1.f, 1.f);
+    bool includeLe = true;
+    for (int depth = a.max_depth;; --depth) {
+      int ti;
+      float t, u, v;
+      if (!trace<false>(sc.nodes, sc.tri, sc.leaf_tri, sc.n, r, &ti, &t, &u, &v, err)) break;
+      const RTri tr = sc.tri[ti];
+      const RMat m = sc.mats[__float_as_int(tr.p1.w)];
+      const RNrm nn = sc.nrm[ti];
+      const float w = 1.f - u - v;
+      const V3 n = w * v3(nn.n1) + u * v3(nn.n2) + v * v3(nn.n3);
+      const V3 hit = r.o + r.d * t;
+      if (includeLe && m.kind == kMatEmission) L = L + mulv(beta, ld3(m.c1));
+      const Frame f = coord_space(n);
+      if (!mat_delta(m.kind)) {
+        // estimate_direct_lighting (pathtracer.cpp:483-524); only the diffuse BSDF has f != 0
+        const V3 fval = m.kind == kMatDiffuse ? ld3(m.c1) * (1.f / kPi) : mk(0.f, 0.f, 0.f);
+        V3 Ld = mk(0.f, 0.f, 0.f);
+        for (int li = 0; li < a.n_light; ++li) {
+          const RLight& l = sc.lights[li];
+          const int ns = (l.kind == kLightDirectional || l.kind == kLightPoint) ? 1 : a.ns_area;
+          V3 Ll = mk(0.f, 0.f, 0.f);
+          for (int i = 0; i < ns; ++i) {
+            V3 wi;
+            float dist, pdf;
+            const V3 Ls = sample_L(l, hit, &wi, &dist, &pdf, g);
+            const float cz_in = dot(f.z, wi);
+            if (cz_in < 0.f) continue;
+            const Ray sh = make_ray(hit, wi, a.ray_eps, dist);
+            int st;
+            float s0, s1, s2;
+            if (trace<true>(sc.nodes, sc.tri, sc.leaf_tri, sc.n, sh, &st, &s0, &s1, &s2, err)) continue;
+            Ll = Ll + mulv(Ls, fval) * (fabsf(cz_in) / pdf);
+          }
+          Ld = Ld + mk(Ll.x / ns, Ll.y / ns, Ll.z / ns);
+        }
+        L = L + mulv(beta, Ld);
+      }
+      if (depth <= 0) break;
+      // estimate_indirect_lighting (pathtracer.cpp:526-551)
+      const V3 wo = f.to_local(mk(-r.d.x, -r.d.y, -r.d.z));
+      V3 wi;
+      float pdf;
+      const V3 fs = sample_f(m, wo, &wi, &pdf, g);
+      const float p_cont = fminf(illum(fs) * 15.f, 1.f);
+      if (!(g.next() < p_cont)) break;
+      beta = mulv(beta, fs) * (fabsf(wi.z) / p_cont / pdf);
+      includeLe = mat_delta(m.kind);
+      r = make_ray(hit, f.to_world(wi), a.ray_eps, FLT_MAX);
+    }
+    sum = sum + L;
+  }
+  const float ns = static_cast<float>(a.ns_aa);
+  float* o = hdr + 3 * static_cast<size_t>(pix);
+  o[0] = sum.x / ns;
+  o[1] = sum.y / ns;
+  o[2] = sum.z / ns;
+}
+
+// HDRImageBuffer::toColor (image.h:174-189) with ImageBuffer::update_pixel (image.h:49-58):
+// gamma 2.2, exposure sqrt(2), min(1, c) * 255 truncated (the reference's clamp call
+// reduces to min(1, c)), rows flipped as PathTracer::save_image writes the PNG.
+__device__ __forceinline__ uint8_t to_byte(float c) {
+  const float v = c < 1.f ? c : 1.f;
+  return static_cast<uint8_t>(static_cast<uint32_t>(v * 255.f));
+}
+__global__ void k_tonemap(const float* __restrict__ hdr, int W, int H, uint8_t* __restrict__ rgba) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= W * H) return;
+  const int x = pix % W, y = pix / W;
+  const float exposure = 1.41421356237309515f, g = 1.f / 2.2f;
+  const float* s = hdr + 3 * static_cast<size_t>(pix);
+  uint8_t* o = rgba + 4 * (static_cast<size_t>(H - 1 - y) * W + x);
+  o[0] = to_byte(powf(s[0] * exposure, g));
+  o[1] = to_byte(powf(s[1] * exposure, g));
+  o[2] = to_byte(powf(s[2] * exposure, g));
+  o[3] = 255;
+}
+
+inline unsigned blocks(size_t n, int b) { return static_cast<unsigned>((n + b - 1) / b); }
+
+}  // namespace
+
+uint32_t sort_blocks(uint32_t n) { return (n + kSortTile - 1) / kSortTile; }
+
+cudaError_t launch_surface_to_tris(const float* xyz, const float* nrm, uint32_t m, int material, RTri* tri,
+                                   RNrm* nn, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  k_surf_tris<<<blocks(m, 256), 256, 0, s>>>(xyz, nrm, m, material, tri, nn);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bvh_build(const RTri* tri, uint32_t n, const BvhScratch& w, BvhNode* nodes, cudaStream_t s) {
+  if (n < 2) return cudaSuccess;
+  k_bounds_part<<<kBoundsBlocks, 256, 0, s>>>(tri, n, w.bounds);
+  k_bounds_final<<<1, kBoundsBlocks, 0, s>>>(w.bounds);
+  k_morton<<<blocks(n, 256), 256, 0, s>>>(tri, n, w.bounds, w.keys, w.vals);
+  const uint32_t nb = sort_blocks(n);
+  uint32_t *ka = w.keys, *va = w.vals, *kb = w.keys2, *vb = w.vals2;
+  for (int shift = 0; shift < 32; shift += 8) {
+    k_sort_hist<<<nb, kSortThreads, 0, s>>>(ka, n, shift, w.hist);
+    cudaError_t e = launch_exclusive_scan(w.hist, w.start, w.tile_sums, 256u * nb, s);
+    if (e != cudaSuccess) return e;
+    k_sort_scatter<<<nb, kSortThreads, 0, s>>>(ka, va, n, shift, w.start, kb, vb);
+    uint32_t* t = ka;
+    ka = kb;
+    kb = t;
+    t = va;
+    va = vb;
+    vb = t;
+  }
+  // four passes: the sorted codes and triangle indices are back in keys / vals
+  k_tree<<<blocks(n - 1, 256), 256, 0, s>>>(w.keys, static_cast<int>(n), nodes, w.parent);
+  cudaError_t e = cudaMemsetAsync(w.flags, 0, sizeof(uint32_t) * (n - 1), s);
+  if (e != cudaSuccess) return e;
+  k_refit<<<blocks(n, 256), 256, 0, s>>>(tri, w.vals, static_cast<int>(n), nodes, w.parent, w.flags, w.box_lo,
+                                         w.box_hi);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_render(const BvhNode* nodes, const RTri* tri, const RNrm* nrm, const uint32_t* leaf_tri,
+                          uint32_t n_tri, const RMat* mats, const RLight* lights, const RCam& cam, const RArgs& a,
+                          float* hdr, unsigned* err, cudaStream_t s) {
+  const size_t px = static_cast<size_t>(a.width) * a.height;
+  if (px == 0) return cudaSuccess;
+  const Scene sc{nodes, tri, nrm, leaf_tri, n_tri, mats, lights};
+  k_render<<<blocks(px, 128), 128, 0, s>>>(sc, cam, a, hdr, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tonemap(const float* hdr, int width, int height, uint8_t* rgba, cudaStream_t s) {
+  const size_t px = static_cast<size_t>(width) * height;
+  if (px == 0) return cudaSuccess;
+  k_tonemap<<<blocks(px, 256), 256, 0, s>>>(hdr, width, height, rgba);
+  return cudaGetLastError();
+}
+
+}  // namespace pbf

@@ -20,7 +20,7 @@ from .params import CParams, PbfParams
 LIB_PATH = Path(os.environ.get("PBF_LIB") or Path(__file__).resolve().parent / "_lib" / "libpbf.so")
 
 PBF_OK = 0
-ABI_VERSION = 4  # PBF_ABI_VERSION of include/pbf.h that these declarations follow
+ABI_VERSION = 5  # PBF_ABI_VERSION of include/pbf.h that these declarations follow
 STATUS = {0: "PBF_OK", 1: "PBF_ERR_INVALID", 2: "PBF_ERR_CUDA", 3: "PBF_ERR_TIMEOUT",
           4: "PBF_ERR_NONFINITE", 5: "PBF_ERR_CAPACITY", 6: "PBF_ERR_NOMEM"}
 
@@ -49,6 +49,43 @@ class CStats(ctypes.Structure):
         ("low_neighbor_count", ctypes.c_uint64),
         ("error_flags", ctypes.c_uint32),
     ]
+
+
+class CMaterial(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("c1", ctypes.c_float * 3), ("c2", ctypes.c_float * 3),
+                ("ior", ctypes.c_float)]
+
+
+class CLight(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32)] + [(k, ctypes.c_float * 3) for k in
+                                              ("radiance", "position", "direction", "dim_x", "dim_y")]
+
+
+class CCameraDesc(ctypes.Structure):
+    _fields_ = [("hfov", ctypes.c_double), ("vfov", ctypes.c_double), ("nclip", ctypes.c_double),
+                ("fclip", ctypes.c_double), ("target", ctypes.c_double * 3), ("phi", ctypes.c_double),
+                ("theta", ctypes.c_double), ("r", ctypes.c_double), ("min_r", ctypes.c_double),
+                ("max_r", ctypes.c_double)]
+
+
+class CCamera(ctypes.Structure):
+    _fields_ = [("position", ctypes.c_double * 3), ("c2w", ctypes.c_double * 9), ("hfov", ctypes.c_double),
+                ("vfov", ctypes.c_double), ("nclip", ctypes.c_double), ("fclip", ctypes.c_double)]
+
+
+class CRenderParams(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("ns_aa", ctypes.c_uint32),
+                ("max_ray_depth", ctypes.c_uint32), ("ns_area_light", ctypes.c_uint32),
+                ("fluid_surface", ctypes.c_uint32), ("surface_bounds", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("seed", ctypes.c_uint64), ("isolevel", ctypes.c_double), ("step", ctypes.c_double),
+                ("surface_lo", ctypes.c_double * 3), ("surface_hi", ctypes.c_double * 3),
+                ("fluid_albedo", ctypes.c_float * 3), ("ray_eps", ctypes.c_float)]
+
+
+class CRenderStats(ctypes.Structure):
+    _fields_ = [("triangles", ctypes.c_uint64), ("surface_triangles", ctypes.c_uint64),
+                ("ms_surface", ctypes.c_double), ("ms_bvh", ctypes.c_double), ("ms_trace", ctypes.c_double),
+                ("ms_total", ctypes.c_double)]
 
 
 _lib = None
@@ -96,6 +133,10 @@ def _declare(L):
         "pbf_surface": (st, [P, ctypes.c_double, ctypes.c_double, P, P, P, P, sz, P]),
         "pbf_mc_table": (None, [P, P, P]),
         "pbf_set_collider_mesh": (st, [P, sz, P]),
+        "pbf_render_params_default": (None, [P]),
+        "pbf_camera_frame": (st, [P, ctypes.c_uint32, ctypes.c_uint32, P]),
+        "pbf_render_set_scene": (st, [P, P, P, P, sz, P, sz, P, sz]),
+        "pbf_render": (st, [P, P, P, P, P, P]),
         "pbf_size": (sz, [P]),
         "pbf_num_scenes": (ctypes.c_int, [P]),
         "pbf_last_error": (ctypes.c_char_p, [P]),
@@ -129,6 +170,16 @@ def mc_table():
     tri = np.zeros((256, 15), dtype=np.int8)
     lib().pbf_mc_table(_ptr(edges), _ptr(ntri), _ptr(tri))
     return edges, ntri, tri
+
+
+def camera_frame(cam, width: int, height: int) -> CCamera:
+    """Camera::configure + Camera::place of a fluid_gb300.render.CameraDesc (no GPU)."""
+    d = CCameraDesc(cam.hfov, cam.vfov, cam.nclip, cam.fclip, (ctypes.c_double * 3)(*cam.target), cam.phi,
+                    cam.theta, cam.r, cam.min_r, cam.max_r)
+    out = CCamera()
+    if lib().pbf_camera_frame(ctypes.byref(d), width, height, ctypes.byref(out)) != PBF_OK:
+        raise PbfError(1, "pbf_camera_frame: bad camera")
+    return out
 
 
 def default_params_c() -> CParams:
@@ -286,6 +337,47 @@ class Simulator:
         self._check(lib().pbf_surface(self._h, iso, step, _ptr(lo_a), _ptr(hi_a), _ptr(xyz), _ptr(nrm), t,
                                       ctypes.byref(count)))
         return xyz[:t], nrm[:t]
+
+    def set_render_scene(self, scene):
+        """The scene the fluid is rendered in (a fluid_gb300.render.RenderScene)."""
+        tri = np.ascontiguousarray(scene.tri, dtype=np.float32).reshape(-1, 9)
+        nrm = np.ascontiguousarray(scene.nrm, dtype=np.float32).reshape(-1, 9)
+        ids = np.ascontiguousarray(scene.tri_mat, dtype=np.uint32)
+        mats = (CMaterial * max(len(scene.materials), 1))(*[
+            CMaterial(m.kind, (ctypes.c_float * 3)(*m.c1), (ctypes.c_float * 3)(*m.c2), m.ior)
+            for m in scene.materials])
+        lights = (CLight * max(len(scene.lights), 1))(*[
+            CLight(l.kind, *[(ctypes.c_float * 3)(*getattr(l, k)) for k in
+                             ("radiance", "position", "direction", "dim_x", "dim_y")]) for l in scene.lights])
+        self._check(lib().pbf_render_set_scene(self._h, _ptr(tri), _ptr(nrm), _ptr(ids), tri.shape[0],
+                                               ctypes.cast(mats, P), len(scene.materials), ctypes.cast(lights, P),
+                                               len(scene.lights)))
+
+    def render(self, cam, width: int, height: int, ns_aa: int = 1, max_depth: int = 1, ns_area_light: int = 1,
+               seed: int = 1, fluid_surface: bool = True, fluid_albedo=(0.1, 0.1, 0.8), ray_eps: float = 0.0,
+               hdr: bool = True, rgba: bool = True, lo=None, hi=None, iso: float = 0.0, step: float = 0.0) -> dict:
+        """One frame of PathTracer::render_to_file: ``hdr`` (H, W, 3) float32 with row 0 the
+        bottom row, ``rgba`` (H, W, 4) uint8 with the top row first (the reference's PNG),
+        ``stats`` (triangles and device milliseconds per phase). ``cam`` is a CameraDesc or
+        a CCamera from camera_frame. ``lo`` / ``hi``: the surface grid's bounds (default the
+        reference's fixed bounds); ``iso`` / ``step`` <= 0: updateSurface's."""
+        frame = cam if isinstance(cam, CCamera) else camera_frame(cam, width, height)
+        p = CRenderParams()
+        lib().pbf_render_params_default(ctypes.byref(p))
+        p.width, p.height, p.ns_aa, p.max_ray_depth, p.ns_area_light = width, height, ns_aa, max_depth, ns_area_light
+        p.fluid_surface, p.seed, p.ray_eps = int(bool(fluid_surface)), seed, ray_eps
+        p.fluid_albedo = (ctypes.c_float * 3)(*fluid_albedo)
+        p.isolevel, p.step = iso, step
+        if lo is not None:
+            p.surface_bounds = 1
+            p.surface_lo = (ctypes.c_double * 3)(*lo)
+            p.surface_hi = (ctypes.c_double * 3)(*hi)
+        h = np.zeros((height, width, 3), dtype=np.float32) if hdr else None
+        c = np.zeros((height, width, 4), dtype=np.uint8) if rgba else None
+        st = CRenderStats()
+        self._check(lib().pbf_render(self._h, ctypes.byref(frame), ctypes.byref(p), _ptr(h), _ptr(c),
+                                     ctypes.byref(st)))
+        return {"hdr": h, "rgba": c, "stats": {k: getattr(st, k) for k, _ in CRenderStats._fields_}}
 
     def estimate_densities(self) -> np.ndarray:
         """Particles::estimateDensities (particles.cpp:440-444): self term included."""

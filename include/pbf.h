@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define PBF_ABI_VERSION 4
+#define PBF_ABI_VERSION 5
 
 #if defined(__GNUC__)
 #define PBF_API __attribute__((visibility("default")))
@@ -307,6 +307,110 @@ PBF_API pbf_status pbf_set_collider_mesh(pbf_handle* h, size_t n, const float* t
  * triples (tri[256 * 15]). Any pointer may be NULL.
  */
 PBF_API void pbf_mc_table(uint16_t* edges, uint8_t* ntri, int8_t* tri);
+
+/* ---- path tracing of the fluid in its scene (PathTracer, src/pathtracer.cpp) ---------- */
+
+/* BSDFs (src/bsdf.h): DIFFUSE c1 = albedo; MIRROR c1 = reflectance; GLASS c1 =
+ * transmittance, c2 = reflectance, ior; REFRACTION (the reference's RefractionBSDF,
+ * black); EMISSION c1 = radiance. */
+#define PBF_MAT_DIFFUSE 0u
+#define PBF_MAT_MIRROR 1u
+#define PBF_MAT_GLASS 2u
+#define PBF_MAT_REFRACTION 3u
+#define PBF_MAT_EMISSION 4u
+typedef struct pbf_material {
+  uint32_t kind;
+  float c1[3];
+  float c2[3];
+  float ior;
+} pbf_material;
+
+/* Lights (src/static_scene/light.cpp): DIRECTIONAL (direction of travel), HEMISPHERE
+ * (uniform sky over +y), POINT (position, no falloff), AREA (centre position, emission
+ * direction, edges dim_x and dim_y; a point p is lit where dot(q - p, direction) < 0 for
+ * the sampled light point q). Spot, sphere and mesh lights of the reference return
+ * black and are not taken. */
+#define PBF_LIGHT_DIRECTIONAL 0u
+#define PBF_LIGHT_HEMISPHERE 1u
+#define PBF_LIGHT_POINT 2u
+#define PBF_LIGHT_AREA 3u
+typedef struct pbf_light {
+  uint32_t kind;
+  float radiance[3];
+  float position[3];
+  float direction[3];
+  float dim_x[3];
+  float dim_y[3];
+} pbf_light;
+
+/* Camera::configure (fields of view in degrees, clip distances) and Camera::place
+ * (target, polar angle phi from +y, azimuth theta, distance r clamped to [min_r, max_r]),
+ * src/camera.cpp:15-46. */
+typedef struct pbf_camera_desc {
+  double hfov, vfov, nclip, fclip;
+  double target[3];
+  double phi, theta, r, min_r, max_r;
+} pbf_camera_desc;
+
+/* A placed camera: position, c2w columns (screen x, screen y, the view direction
+ * reversed), fields of view in degrees after the aspect adjustment, clip distances. */
+typedef struct pbf_camera {
+  double position[3];
+  double c2w[9];
+  double hfov, vfov, nclip, fclip;
+} pbf_camera;
+
+typedef struct pbf_render_params {
+  uint32_t width, height;
+  uint32_t ns_aa;          /* camera rays per pixel (-s; 1 = through the pixel centre) */
+  uint32_t max_ray_depth;  /* bounces (-m) */
+  uint32_t ns_area_light;  /* samples per area or hemisphere light (-l) */
+  uint32_t fluid_surface;  /* 1: add the particles' surface as Particles::updateSurface does */
+  uint32_t surface_bounds; /* 1: surface grid over [surface_lo, surface_hi]; 0: the reference's
+                              fixed [-1, 1] x [0, 1.5] x [-1, 1] (particles.cpp:330-349) */
+  uint32_t reserved;
+  uint64_t seed;           /* random numbers: a function of (seed, pixel, sample, draw) */
+  double isolevel, step;   /* surface; <= 0: 0.95 rest_density and 0.5 H (particles.cpp:392-401) */
+  double surface_lo[3], surface_hi[3];
+  float fluid_albedo[3];   /* the surface's DiffuseBSDF (particles.cpp:398: 0.1 0.1 0.8) */
+  float ray_eps;           /* start of shadow and bounce rays; <= 0: 1e-4 */
+} pbf_render_params;
+
+typedef struct pbf_render_stats {
+  uint64_t triangles;          /* scene + surface */
+  uint64_t surface_triangles;
+  double ms_surface, ms_bvh, ms_trace, ms_total; /* device time of the phases */
+} pbf_render_stats;
+
+/* The reference's defaults (application.h:48-56: 1 ray per pixel, depth 1, 1 light
+ * sample) at 640 x 480, with the fluid surface. */
+PBF_API void pbf_render_params_default(pbf_render_params* p);
+
+/* Camera::configure + Camera::place: the frame generate_ray uses (no GPU needed). */
+PBF_API pbf_status pbf_camera_frame(const pbf_camera_desc* d, uint32_t width, uint32_t height, pbf_camera* out);
+
+/*
+ * pbf_render_set_scene -- the scene the fluid is rendered in (the reference's Scene of
+ * COLLADA meshes and lights): n_tri triangles of 9 floats (tri_xyz, vertices) with
+ * vertex normals (tri_nrm, 9 floats; NULL: the face normal unit((p2 - p1) x (p3 - p1)) at
+ * all three vertices) and a material index each; host arrays, copied.
+ */
+PBF_API pbf_status pbf_render_set_scene(pbf_handle* h, const float* tri_xyz, const float* tri_nrm,
+                                        const uint32_t* tri_material, size_t n_tri, const pbf_material* materials,
+                                        size_t n_materials, const pbf_light* lights, size_t n_lights);
+
+/*
+ * pbf_render -- one frame of PathTracer::render_to_file (pathtracer.cpp:187-235,
+ * 483-632) of the scene and, with fluid_surface, the surface of the current state: a BVH
+ * over all triangles built on the device (Morton-ordered binary radix tree), one thread
+ * per pixel tracing ns_aa paths of estimate_direct_lighting + estimate_indirect_lighting
+ * with Russian roulette, in FP32. hdr: W * H * 3 floats (HOST or NULL), row 0 = the
+ * bottom row as the reference's sample buffer; rgba: W * H * 4 bytes (HOST or NULL),
+ * HDRImageBuffer::toColor's 8-bit frame with the top row first, as the reference's PNG.
+ * Device memory for the frame and the hierarchy is kept for the next call.
+ */
+PBF_API pbf_status pbf_render(pbf_handle* h, const pbf_camera* cam, const pbf_render_params* p, float* hdr,
+                              uint8_t* rgba, pbf_render_stats* stats);
 
 #define PBF_NOALLOC_MAX_PARTICLES 65536
 #define PBF_NOALLOC_MAX_CELLS 262144
