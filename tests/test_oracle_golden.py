@@ -15,9 +15,9 @@ import pytest
 from tests.golden.make_golden import params_from_json
 
 # reference-step vectors of make_golden.py (the finite-difference fixture of the adjoint
-# workload and the surface fixtures are read by their own tests)
+# workload, the surface and the render fixtures are read by their own tests)
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                if not os.path.basename(p).startswith(("adjoint_", "surface_")))
+                if not os.path.basename(p).startswith(("adjoint_", "surface_", "render_")))
 
 
 def _case_id(path):
