@@ -476,6 +476,75 @@ def bench_surface(sim, prm) -> dict:
             "timing": "wall clock of one pbf_surface call with host output, best of 2 after a warm-up"}
 
 
+RENDER_SETTINGS = (1280, 720, 16, 3, 4)  # width, height, camera rays per pixel, depth, area-light samples
+
+
+def render_reference_sample(settings=(4, 3, 4)) -> dict | None:
+    """The reference's own PathTracer::render_to_file (oracle/_ref, one thread) on the
+    committed Cornell-box fixture (the reference's default 720 particles): two frames,
+    64 x 48 and 128 x 96; the per-path cost is the difference of their times over the
+    difference of their paths, so the reference's surface and BVH build (the same in both)
+    drop out."""
+    from oracle import ref_runner
+
+    if not ref_runner.render_available():
+        return None
+    from tests.golden.make_golden import params_from_json
+    from tests.golden.make_render_golden import camera_from_json, scene_from_arrays
+
+    g = np.load(ROOT / "tests" / "golden" / "render_p_default.npz")
+    scene, cam, prm = scene_from_arrays(g), camera_from_json(str(g["camera"])), params_from_json(str(g["params"]))
+    aa, depth, area = settings
+    t = {}
+    for (W, H) in ((64, 48), (128, 96)):
+        t[(W, H)] = min(ref_runner.render(scene, cam, g["pos"], prm, W, H, ns_aa=aa, max_depth=depth,
+                                          ns_area_light=area, seed=1)["seconds"] for _ in range(2))
+    paths = (128 * 96 - 64 * 48) * aa
+    dt = t[(128, 96)] - t[(64, 48)]
+    return {"paths_per_s": paths / dt if dt > 0 else None, "cores": 1, "kind": "reference",
+            "sample": f"reference render_to_file, Cornell box with the reference's 720 default particles "
+                      f"({len(g['surf_xyz'])} surface triangles), ns_aa {aa}, depth {depth}, area samples {area}: "
+                      f"(t(128x96) - t(64x48)) over the difference in paths",
+            "seconds": {f"{w}x{h}": v for (w, h), v in t.items()}}
+
+
+def bench_render(sim, prm) -> dict:
+    """Path tracing (pbf_render) of the workload's configured state in a Cornell box on the
+    collider box, RENDER_SETTINGS, the surface over the collider box at updateSurface's
+    settings. Device time of each phase from the call's own CUDA events (surface: cell
+    sort, field, count, host read of the count, emit; hierarchy build; trace + tone map),
+    best of 2 frames after a warm-up; the wall time adds the 8-bit frame's copy to the host."""
+    from fluid_gb300 import render as R
+
+    W, H, aa, depth, area = RENDER_SETTINGS
+    scene, cam = R.cornell_box(prm.box_lo, prm.box_hi)
+    sim.restore()
+    sim.set_render_scene(scene)
+    best = None
+    for i in range(3):
+        sim.restore()
+        sim.sync()
+        t0 = time.perf_counter()
+        out = sim.render(cam, W, H, aa, depth, area, seed=1 + i, lo=prm.box_lo, hi=prm.box_hi, hdr=False)
+        wall = time.perf_counter() - t0
+        if i and (best is None or out["stats"]["ms_total"] < best[0]["ms_total"]):
+            best = (out["stats"], wall)
+    st, wall = best
+    paths = W * H * aa
+    line = {"workload": "configured state in a Cornell box on the collider box", "width": W, "height": H,
+            "ns_aa": aa, "max_ray_depth": depth, "ns_area_light": area, "triangles": st["triangles"],
+            "surface_triangles": st["surface_triangles"], "ms_surface": st["ms_surface"], "ms_bvh": st["ms_bvh"],
+            "ms_trace": st["ms_trace"], "ms_frame_wall": wall * 1e3, "paths_per_s": paths / (st["ms_trace"] / 1e3),
+            "timing": "CUDA events per phase inside pbf_render; best of 2 after a warm-up"}
+    try:
+        ref = render_reference_sample((aa, depth, area))
+    except Exception as exc:  # the reference's renderer is a reported baseline only
+        ref = {"unavailable": str(exc)[:200]}
+    if ref:
+        line["cpu_reference"] = ref
+    return line
+
+
 def bench_ours(args, scene, world, rank, local):
     import torch
 
@@ -532,6 +601,7 @@ def bench_ours(args, scene, world, rank, local):
     value = world * n * args.steps / (total_ms / 1e3)
     stats = sim.stats()
     surface = bench_surface(sim, prm) if not args.no_surface else None
+    render = bench_render(sim, prm) if not args.no_render else None
 
     # phase breakdown: the same K steps again, launched stream-ordered (no graph) with
     # CUDA events between phases on the simulator's stream
@@ -627,6 +697,8 @@ def bench_ours(args, scene, world, rank, local):
         line["e2e"] = e2e
     if surface:
         line["surface"] = surface
+    if render:
+        line["render"] = render
     if batched:
         line["batched"] = batched
     if not args.no_adjoint:
@@ -653,6 +725,7 @@ def main(argv=None):
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-surface", action="store_true")
+    ap.add_argument("--no-render", action="store_true")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="run only the adjoint leg and print its object (a profiling aid, not a bench line)")
     args = ap.parse_args(argv)

@@ -9,8 +9,10 @@
 //                      "Maximizing parallelism in the construction of BVHs, octrees
 //                      and k-d trees"), ties broken by sorted position
 //   k_refit            bottom-up boxes: the second child to finish fills its parent
-//   k_render           camera rays, closest hits, direct light from every light,
-//                      one BSDF-sampled bounce per level with Russian roulette
+//   k_render_paths     persistent threads, one path each at a time: camera ray,
+//                      closest hits, direct light from every light, one BSDF-sampled
+//                      bounce per level with Russian roulette
+//   k_accumulate       per-pixel sums of the paths' radiance in sample order
 //   k_tonemap          HDRImageBuffer::toColor + ImageBuffer::update_pixel
 //
 // Every random number is a pure function of (seed, pixel, sample, draw index), so a
@@ -19,6 +21,7 @@
 // Lea and Flood, "Fast splittable pseudorandom number generators", 2014). The draws
 // are consumed in the reference's order: camera jitter (x, y) when ns_aa > 1; at each
 // hit, per light and sample the light's draws, then the BSDF's, then the roulette coin.
+#include <algorithm>
 #include <cfloat>
 #include <cstdint>
 
@@ -339,76 +342,85 @@ __device__ __forceinline__ bool box_test(const float4& lo, const float4& hi, con
   return t0 <= t1;
 }
 
-// Closest hit (ANY = false) or any hit (ANY = true) below r.tmax; *tri = -1 for none.
+// Walk of one hierarchy over triangles tris[base + leaf]: closest hit (ANY = false) below
+// tmax, updating tmax / best / bu / bv; or any hit (ANY = true: returns true at the first).
 template <bool ANY>
-__device__ bool trace(const BvhNode* __restrict__ nodes, const RTri* __restrict__ tris,
-                      const uint32_t* __restrict__ leaf_tri, uint32_t n, const Ray& r, int* hit_tri, float* ht,
-                      float* hu, float* hv, unsigned* err) {
-  float tmax = r.tmax;
-  int best = -1;
-  float bu = 0.f, bv = 0.f;
+__device__ bool walk(const BvhNode* __restrict__ nodes, const RTri* __restrict__ tris,
+                     const uint32_t* __restrict__ leaf_tri, uint32_t n, uint32_t base, const Ray& r, float& tmax,
+                     int& best, float& bu, float& bv, unsigned* err) {
   if (n == 0) return false;
   if (n == 1) {
     float t, u, v;
-    if (tri_test(tris[0], r, tmax, &t, &u, &v)) {
-      best = 0;
+    if (tri_test(tris[base], r, tmax, &t, &u, &v)) {
+      best = static_cast<int>(base);
       tmax = t;
       bu = u;
       bv = v;
+      return ANY;
     }
-  } else {
-    uint32_t stack[kBvhStack];
-    int sp = 0;
-    uint32_t node = 0;
-    while (true) {
-      const BvhNode nd = nodes[node];
-      float tl, tr;
-      bool hl = box_test(nd.lo_l, nd.hi_l, r, tmax, &tl);
-      bool hr = box_test(nd.lo_r, nd.hi_r, r, tmax, &tr);
-      const uint32_t cl = __float_as_uint(nd.lo_l.w), cr = __float_as_uint(nd.lo_r.w);
+    return false;
+  }
+  uint32_t stack[kBvhStack];
+  int sp = 0;
+  uint32_t node = 0;
+  while (true) {
+    const BvhNode nd = nodes[node];
+    float tl, tr;
+    bool hl = box_test(nd.lo_l, nd.hi_l, r, tmax, &tl);
+    bool hr = box_test(nd.lo_r, nd.hi_r, r, tmax, &tr);
+    const uint32_t cl = __float_as_uint(nd.lo_l.w), cr = __float_as_uint(nd.lo_r.w);
 #pragma unroll
-      for (int side = 0; side < 2; ++side) {
-        const uint32_t c = side ? cr : cl;
-        bool& h = side ? hr : hl;
-        if (h && (c & kLeafBit)) {
-          h = false;
-          const uint32_t ti = leaf_tri[c & ~kLeafBit];
-          float t, u, v;
-          if (tri_test(tris[ti], r, tmax, &t, &u, &v)) {
-            best = static_cast<int>(ti);
-            tmax = t;
-            bu = u;
-            bv = v;
-            if (ANY) {
-              *hit_tri = best;
-              return true;
-            }
-          }
+    for (int side = 0; side < 2; ++side) {
+      const uint32_t c = side ? cr : cl;
+      bool& h = side ? hr : hl;
+      if (h && (c & kLeafBit)) {
+        h = false;
+        const uint32_t ti = base + leaf_tri[c & ~kLeafBit];
+        float t, u, v;
+        if (tri_test(tris[ti], r, tmax, &t, &u, &v)) {
+          best = static_cast<int>(ti);
+          tmax = t;
+          bu = u;
+          bv = v;
+          if (ANY) return true;
         }
       }
-      if (hl && hr) {
-        const bool lfirst = tl <= tr;
-        if (sp < kBvhStack) {
-          stack[sp++] = lfirst ? cr : cl;
-        } else {
-          atomicOr(err, 1u);
-        }
-        node = lfirst ? cl : cr;
-      } else if (hl) {
-        node = cl;
-      } else if (hr) {
-        node = cr;
+    }
+    if (hl && hr) {
+      const bool lfirst = tl <= tr;
+      if (sp < kBvhStack) {
+        stack[sp++] = lfirst ? cr : cl;
       } else {
-        if (sp == 0) break;
-        node = stack[--sp];
+        atomicOr(err, 1u);
       }
+      node = lfirst ? cl : cr;
+    } else if (hl) {
+      node = cl;
+    } else if (hr) {
+      node = cr;
+    } else {
+      if (sp == 0) break;
+      node = stack[--sp];
     }
   }
-  *hit_tri = best;
-  *ht = tmax;
-  *hu = bu;
-  *hv = bv;
-  return best >= 0;
+  return false;
+}
+
+// Every triangle of tris[0, n) in index order.
+template <bool ANY>
+__device__ bool brute(const RTri* __restrict__ tris, uint32_t n, const Ray& r, float& tmax, int& best, float& bu,
+                      float& bv) {
+  for (uint32_t k = 0; k < n; ++k) {
+    float t, u, v;
+    if (tri_test(tris[k], r, tmax, &t, &u, &v)) {
+      best = static_cast<int>(k);
+      tmax = t;
+      bu = u;
+      bv = v;
+      if (ANY) return true;
+    }
+  }
+  return false;
 }
 
 // ---- BSDFs and lights (bsdf.cpp, light.cpp) --------------------------------------------------------
@@ -527,38 +539,112 @@ __device__ V3 sample_L(const RLight& l, V3 p, V3* wi, float* dist, float* pdf, R
 }
 
 // ---- the path tracer ---------------------------------------------------------------------------
+// The scene's triangles (few and large: walls, meshes) and the fluid surface's (many and
+// small) sit in two hierarchies, so that the scene's large boxes do not widen the
+// surface tree's nodes; a scene of at most kBruteScene triangles is tested triangle by
+// triangle. tri holds the scene's n_scene triangles, then the surface's.
 struct Scene {
-  const BvhNode* nodes;
   const RTri* tri;
   const RNrm* nrm;
-  const uint32_t* leaf_tri;
-  uint32_t n;
   const RMat* mats;
   const RLight* lights;
+  uint32_t n_scene, n_surf;
+  const BvhNode* scene_nodes;  // null: brute force
+  const uint32_t* scene_leaf;
+  const BvhNode* surf_nodes;
+  const uint32_t* surf_leaf;
 };
 
-__global__ void __launch_bounds__(128) k_render(Scene sc, RCam cam, RArgs a, float* __restrict__ hdr, unsigned* err) {
-  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= a.width * a.height) return;
-  const int px = pix % a.width, py = pix / a.width;
+__device__ __forceinline__ bool closest(const Scene& sc, const Ray& r, int* ti, float* t, float* u, float* v,
+                                        unsigned* err) {
+  float tmax = r.tmax, bu = 0.f, bv = 0.f;
+  int best = -1;
+  if (sc.scene_nodes)
+    walk<false>(sc.scene_nodes, sc.tri, sc.scene_leaf, sc.n_scene, 0u, r, tmax, best, bu, bv, err);
+  else
+    brute<false>(sc.tri, sc.n_scene, r, tmax, best, bu, bv);
+  walk<false>(sc.surf_nodes, sc.tri, sc.surf_leaf, sc.n_surf, sc.n_scene, r, tmax, best, bu, bv, err);
+  *ti = best;
+  *t = tmax;
+  *u = bu;
+  *v = bv;
+  return best >= 0;
+}
+
+__device__ __forceinline__ bool occluded(const Scene& sc, const Ray& r, unsigned* err) {
+  float tmax = r.tmax, bu, bv;
+  int best = -1;
+  if (sc.scene_nodes ? walk<true>(sc.scene_nodes, sc.tri, sc.scene_leaf, sc.n_scene, 0u, r, tmax, best, bu, bv, err)
+                     : brute<true>(sc.tri, sc.n_scene, r, tmax, best, bu, bv))
+    return true;
+  return walk<true>(sc.surf_nodes, sc.tri, sc.surf_leaf, sc.n_surf, sc.n_scene, r, tmax, best, bu, bv, err);
+}
+
+constexpr uint32_t kNoPath = 0xffffffffu;
+
+__device__ __forceinline__ unsigned lane_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Persistent path tracer: each thread carries one path (sample s of pixel p,
+// PathTracer::raytrace_pixel, pathtracer.cpp:584-604) one bounce of trace_ray
+// (pathtracer.cpp:553-582) per loop turn, and takes the next path of the batch as soon as
+// its path ends, so a warp's lanes stay busy however long their paths are. Path q of the
+// batch is sample s0 + q / npix of pixel q % npix; its radiance goes to rad[q].
+__global__ void __launch_bounds__(128) k_render_paths(Scene sc, RCam cam, RArgs a, int s0, uint32_t total,
+                                                      float* __restrict__ rad, unsigned* counter, unsigned* err) {
+  const unsigned full = 0xffffffffu, lane = threadIdx.x & 31u;
+  const uint32_t npix = static_cast<uint32_t>(a.width) * static_cast<uint32_t>(a.height);
   const V3 cpos = ld3(cam.pos), cx = ld3(cam.c2w), cy = ld3(cam.c2w + 3), cz = ld3(cam.c2w + 6);
-  V3 sum = mk(0.f, 0.f, 0.f);
-  for (int s = 0; s < a.ns_aa; ++s) {
-    Rng g{path_key(a.seed, static_cast<unsigned long long>(pix), static_cast<unsigned long long>(s)), 0ull};
-    float jx = 0.5f, jy = 0.5f;
-    if (a.ns_aa > 1) {
-      jx = g.next();
-      jy = g.next();
+  uint32_t q = kNoPath;
+  Ray r = make_ray(cpos, cz, 0.f, 0.f);
+  V3 L = mk(0.f, 0.f, 0.f), beta = mk(1.f, 1.f, 1.f);
+  int depth = 0;
+  bool includeLe = true;
+  Rng g{0ull, 0ull};
+  bool drained = false;
+  while (true) {
+    if (!drained) {
+      const unsigned need = __ballot_sync(full, q == kNoPath);
+      if (need) {
+        const int leader = __ffs(need) - 1;
+        uint32_t base = 0;
+        if (static_cast<int>(lane) == leader) base = atomicAdd(counter, static_cast<unsigned>(__popc(need)));
+        base = __shfl_sync(full, base, leader);
+        if (base + static_cast<uint32_t>(__popc(need)) >= total) drained = true;
+        if (q == kNoPath) {
+          const uint32_t mine = base + static_cast<uint32_t>(__popc(need & lane_lt()));
+          if (mine < total) {
+            q = mine;
+            const uint32_t pix = q % npix;
+            const int s = s0 + static_cast<int>(q / npix);
+            g = Rng{path_key(a.seed, pix, static_cast<unsigned long long>(s)), 0ull};
+            float jx = 0.5f, jy = 0.5f;
+            if (a.ns_aa > 1) {
+              jx = g.next();
+              jy = g.next();
+            }
+            const int px = static_cast<int>(pix % static_cast<uint32_t>(a.width));
+            const int py = static_cast<int>(pix / static_cast<uint32_t>(a.width));
+            const float xn = (px + jx) / a.width, yn = (py + jy) / a.height;
+            r = make_ray(cpos, unit(cx * ((xn - 0.5f) * cam.htan) + cy * ((yn - 0.5f) * cam.vtan) - cz), cam.nclip,
+                         cam.fclip);
+            L = mk(0.f, 0.f, 0.f);
+            beta = mk(1.f, 1.f, 1.f);
+            depth = a.max_depth;
+            includeLe = true;
+          }
+        }
+      }
     }
-    const float xn = (px + jx) / a.width, yn = (py + jy) / a.height;
-    const V3 dir = unit(cx * ((xn - 0.5f) * cam.htan) + cy * ((yn - 0.5f) * cam.vtan) - cz);
-    Ray r = make_ray(cpos, dir, cam.nclip, cam.fclip);
-    V3 L = mk(0.f, 0.f, 0.f), beta = mk(1.f, 1.f, 1.f);
-    bool includeLe = true;
-    for (int depth = a.max_depth;; --depth) {
-      int ti;
-      float t, u, v;
-      if (!trace<false>(sc.nodes, sc.tri, sc.leaf_tri, sc.n, r, &ti, &t, &u, &v, err)) break;
+    if (__ballot_sync(full, q != kNoPath) == 0) break;
+    if (q == kNoPath) continue;
+    bool done = true;
+    int ti;
+    float t, u, v;
+    if (closest(sc, r, &ti, &t, &u, &v, err)) {
       const RTri tr = sc.tri[ti];
       const RMat m = sc.mats[__float_as_int(tr.p1.w)];
       const RNrm nn = sc.nrm[ti];
@@ -581,35 +667,59 @@ __global__ void __launch_bounds__(128) k_render(Scene sc, RCam cam, RArgs a, flo
             const V3 Ls = sample_L(l, hit, &wi, &dist, &pdf, g);
             const float cz_in = dot(f.z, wi);
             if (cz_in < 0.f) continue;
-            const Ray sh = make_ray(hit, wi, a.ray_eps, dist);
-            int st;
-            float s0, s1, s2;
-            if (trace<true>(sc.nodes, sc.tri, sc.leaf_tri, sc.n, sh, &st, &s0, &s1, &s2, err)) continue;
+            if (occluded(sc, make_ray(hit, wi, a.ray_eps, dist), err)) continue;
             Ll = Ll + mulv(Ls, fval) * (fabsf(cz_in) / pdf);
           }
           Ld = Ld + mk(Ll.x / ns, Ll.y / ns, Ll.z / ns);
         }
         L = L + mulv(beta, Ld);
       }
-      if (depth <= 0) break;
-      // estimate_indirect_lighting (pathtracer.cpp:526-551)
-      const V3 wo = f.to_local(mk(-r.d.x, -r.d.y, -r.d.z));
-      V3 wi;
-      float pdf;
-      const V3 fs = sample_f(m, wo, &wi, &pdf, g);
-      const float p_cont = fminf(illum(fs) * 15.f, 1.f);
-      if (!(g.next() < p_cont)) break;
-      beta = mulv(beta, fs) * (fabsf(wi.z) / p_cont / pdf);
-      includeLe = mat_delta(m.kind);
-      r = make_ray(hit, f.to_world(wi), a.ray_eps, FLT_MAX);
+      if (depth > 0) {
+        // estimate_indirect_lighting (pathtracer.cpp:526-551)
+        const V3 wo = f.to_local(mk(-r.d.x, -r.d.y, -r.d.z));
+        V3 wi;
+        float pdf;
+        const V3 fs = sample_f(m, wo, &wi, &pdf, g);
+        const float p_cont = fminf(illum(fs) * 15.f, 1.f);
+        if (g.next() < p_cont) {
+          beta = mulv(beta, fs) * (fabsf(wi.z) / p_cont / pdf);
+          includeLe = mat_delta(m.kind);
+          r = make_ray(hit, f.to_world(wi), a.ray_eps, FLT_MAX);
+          --depth;
+          done = false;
+        }
+      }
     }
-    sum = sum + L;
+    if (done) {
+      float* o = rad + 3 * static_cast<size_t>(q);
+      o[0] = L.x;
+      o[1] = L.y;
+      o[2] = L.z;
+      q = kNoPath;
+    }
   }
-  const float ns = static_cast<float>(a.ns_aa);
-  float* o = hdr + 3 * static_cast<size_t>(pix);
-  o[0] = sum.x / ns;
-  o[1] = sum.y / ns;
-  o[2] = sum.z / ns;
+}
+
+// Sums a batch of nb samples per pixel into acc in sample order (the reference adds
+// trace_ray's results in sample order, pathtracer.cpp:597-602); the last batch divides
+// by ns_aa.
+__global__ void k_accumulate(const float* __restrict__ rad, uint32_t npix, int nb, int first, int last, int ns_aa,
+                             float* __restrict__ acc) {
+  const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= npix) return;
+  float* o = acc + 3 * static_cast<size_t>(pix);
+  V3 v = first ? mk(0.f, 0.f, 0.f) : mk(o[0], o[1], o[2]);
+  for (int s = 0; s < nb; ++s) {
+    const float* x = rad + 3 * (static_cast<size_t>(s) * npix + pix);
+    v = v + mk(x[0], x[1], x[2]);
+  }
+  if (last) {
+    const float ns = static_cast<float>(ns_aa);
+    v = mk(v.x / ns, v.y / ns, v.z / ns);
+  }
+  o[0] = v.x;
+  o[1] = v.y;
+  o[2] = v.z;
 }
 
 // HDRImageBuffer::toColor (image.h:174-189) with ImageBuffer::update_pixel (image.h:49-58):
@@ -673,14 +783,41 @@ cudaError_t launch_bvh_build(const RTri* tri, uint32_t n, const BvhScratch& w, B
   return cudaGetLastError();
 }
 
-cudaError_t launch_render(const BvhNode* nodes, const RTri* tri, const RNrm* nrm, const uint32_t* leaf_tri,
-                          uint32_t n_tri, const RMat* mats, const RLight* lights, const RCam& cam, const RArgs& a,
-                          float* hdr, unsigned* err, cudaStream_t s) {
+uint32_t render_batch_samples(int width, int height, int ns_aa) {
+  const size_t px = static_cast<size_t>(width) * height;
+  const size_t budget = size_t(256) << 20;  // path radiance buffer of one batch
+  const size_t per = std::max<size_t>(1, budget / (12 * std::max<size_t>(px, 1)));
+  return static_cast<uint32_t>(std::min<size_t>(per, static_cast<size_t>(ns_aa)));
+}
+
+cudaError_t launch_render(const RTri* tri, const RNrm* nrm, uint32_t n_scene, uint32_t n_surf,
+                          const BvhNode* scene_nodes, const uint32_t* scene_leaf, const BvhNode* surf_nodes,
+                          const uint32_t* surf_leaf, const RMat* mats, const RLight* lights, const RCam& cam,
+                          const RArgs& a, float* path_rad, unsigned* counter, float* hdr, unsigned* err,
+                          cudaStream_t s) {
   const size_t px = static_cast<size_t>(a.width) * a.height;
   if (px == 0) return cudaSuccess;
-  const Scene sc{nodes, tri, nrm, leaf_tri, n_tri, mats, lights};
-  k_render<<<blocks(px, 128), 128, 0, s>>>(sc, cam, a, hdr, err);
-  return cudaGetLastError();
+  const Scene sc{tri, nrm, mats, lights, n_scene, n_surf, scene_nodes, scene_leaf, surf_nodes, surf_leaf};
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_paths, 128, 0);
+  if (e != cudaSuccess) return e;
+  const uint32_t nb = render_batch_samples(a.width, a.height, a.ns_aa);
+  for (int s0 = 0; s0 < a.ns_aa; s0 += static_cast<int>(nb)) {
+    const int cnt = std::min(static_cast<int>(nb), a.ns_aa - s0);
+    const size_t total = px * static_cast<size_t>(cnt);
+    e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = static_cast<unsigned>(
+        std::max<size_t>(1, std::min<size_t>(static_cast<size_t>(sms) * std::max(per_sm, 1), (total + 127) / 128)));
+    k_render_paths<<<grid, 128, 0, s>>>(sc, cam, a, s0, static_cast<uint32_t>(total), path_rad, counter, err);
+    k_accumulate<<<blocks(px, 256), 256, 0, s>>>(path_rad, static_cast<uint32_t>(px), cnt, s0 == 0,
+                                                 s0 + cnt >= a.ns_aa, a.ns_aa, hdr);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_tonemap(const float* hdr, int width, int height, uint8_t* rgba, cudaStream_t s) {

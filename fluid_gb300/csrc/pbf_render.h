@@ -85,12 +85,20 @@ struct RenderState {
 cudaError_t launch_surface_to_tris(const float* xyz, const float* nrm, uint32_t m, int material, RTri* tri,
                                    RNrm* nn, cudaStream_t s);
 cudaError_t launch_bvh_build(const RTri* tri, uint32_t n, const BvhScratch& w, BvhNode* nodes, cudaStream_t s);
+// Samples per pixel traced in one batch: the batch's path radiance (npix * batch * 3
+// floats, path_rad) stays within 256 MiB.
+uint32_t render_batch_samples(int width, int height, int ns_aa);
 // hdr: W * H * 3 floats, row y = 0 first (the bottom row, as the reference's sample buffer).
-// leaf_tri: the build's vals (sorted position -> triangle); err bit 0: a traversal
-// stack overflowed (deeper than kBvhStack levels).
-cudaError_t launch_render(const BvhNode* nodes, const RTri* tri, const RNrm* nrm, const uint32_t* leaf_tri,
-                          uint32_t n_tri, const RMat* mats, const RLight* lights, const RCam& cam, const RArgs& a,
-                          float* hdr, unsigned* err, cudaStream_t s);
+// *_leaf: a build's vals (sorted position -> triangle of its range); counter: one word;
+// err bit 0: a traversal stack overflowed (deeper than kBvhStack levels).
+// tri / nrm: the scene's n_scene triangles, then the surface's n_surf. scene_nodes null:
+// the scene's triangles are tested one by one (at most kBruteScene of them).
+constexpr uint32_t kBruteScene = 32;
+cudaError_t launch_render(const RTri* tri, const RNrm* nrm, uint32_t n_scene, uint32_t n_surf,
+                          const BvhNode* scene_nodes, const uint32_t* scene_leaf, const BvhNode* surf_nodes,
+                          const uint32_t* surf_leaf, const RMat* mats, const RLight* lights, const RCam& cam,
+                          const RArgs& a, float* path_rad, unsigned* counter, float* hdr, unsigned* err,
+                          cudaStream_t s);
 // rgba: W * H * 4 bytes, rows flipped (top first) as PathTracer::save_image writes them.
 cudaError_t launch_tonemap(const float* hdr, int width, int height, uint8_t* rgba, cudaStream_t s);
 

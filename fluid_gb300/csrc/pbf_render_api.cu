@@ -44,44 +44,59 @@ struct Carve {
   }
 };
 
+struct Tree {
+  pbf::BvhNode* nodes;
+  pbf::BvhScratch w;
+};
+
 struct Frame {
   pbf::RTri* tri;
   pbf::RNrm* nrm;
-  pbf::BvhNode* nodes;
-  pbf::BvhScratch w;
+  Tree scene, surf;
   pbf::RMat* mats;
   pbf::RLight* lights;
-  float *sxyz, *snrm, *hdr;
+  float *sxyz, *snrm, *hdr, *path_rad;
   uint8_t* rgba;
-  unsigned* err;
+  unsigned *err, *counter;
 };
 
-Frame carve(char* base, size_t n, size_t m, int n_mat, int n_light, size_t px, size_t* bytes) {
+Tree carve_tree(Carve& c, size_t n) {
+  Tree t;
+  t.nodes = c.take<pbf::BvhNode>(n > 1 ? n - 1 : 1);
+  const uint32_t nb = pbf::sort_blocks(static_cast<uint32_t>(n));
+  t.w.keys = c.take<uint32_t>(n);
+  t.w.vals = c.take<uint32_t>(n);
+  t.w.keys2 = c.take<uint32_t>(n);
+  t.w.vals2 = c.take<uint32_t>(n);
+  t.w.hist = c.take<uint32_t>(256u * nb);
+  t.w.start = c.take<uint32_t>(256u * nb + 1);
+  t.w.tile_sums = c.take<uint32_t>(pbf::exclusive_scan_tiles(256u * nb) + 1);
+  t.w.parent = c.take<uint32_t>(2 * n);
+  t.w.flags = c.take<uint32_t>(n);
+  t.w.box_lo = c.take<float4>(2 * n);
+  t.w.box_hi = c.take<float4>(2 * n);
+  t.w.bounds = c.take<float4>(2 + 2 * pbf::kBoundsBlocks);
+  return t;
+}
+
+// n_scene_tree: the scene's triangle count when it gets a hierarchy, else 0.
+Frame carve(char* base, size_t n, size_t n_scene_tree, size_t m, int n_mat, int n_light, size_t px, size_t batch,
+            size_t* bytes) {
   Carve c{base};
   Frame f;
   f.tri = c.take<pbf::RTri>(n);
   f.nrm = c.take<pbf::RNrm>(n);
-  f.nodes = c.take<pbf::BvhNode>(n > 1 ? n - 1 : 1);
-  const uint32_t nb = pbf::sort_blocks(static_cast<uint32_t>(n));
-  f.w.keys = c.take<uint32_t>(n);
-  f.w.vals = c.take<uint32_t>(n);
-  f.w.keys2 = c.take<uint32_t>(n);
-  f.w.vals2 = c.take<uint32_t>(n);
-  f.w.hist = c.take<uint32_t>(256u * nb);
-  f.w.start = c.take<uint32_t>(256u * nb + 1);
-  f.w.tile_sums = c.take<uint32_t>(pbf::exclusive_scan_tiles(256u * nb) + 1);
-  f.w.parent = c.take<uint32_t>(2 * n);
-  f.w.flags = c.take<uint32_t>(n);
-  f.w.box_lo = c.take<float4>(2 * n);
-  f.w.box_hi = c.take<float4>(2 * n);
-  f.w.bounds = c.take<float4>(2 + 2 * pbf::kBoundsBlocks);
+  f.scene = carve_tree(c, n_scene_tree);
+  f.surf = carve_tree(c, m);
   f.mats = c.take<pbf::RMat>(n_mat + 1);
   f.lights = c.take<pbf::RLight>(n_light);
   f.sxyz = c.take<float>(9 * m);
   f.snrm = c.take<float>(9 * m);
   f.hdr = c.take<float>(3 * px);
   f.rgba = c.take<uint8_t>(4 * px);
+  f.path_rad = c.take<float>(3 * px * batch);
   f.err = c.take<unsigned>(1);
+  f.counter = c.take<unsigned>(1);
   *bytes = c.off + 256;
   return f;
 }
@@ -294,8 +309,11 @@ pbf_status pbf_render(pbf_handle* hh, const pbf_camera* cam, const pbf_render_pa
   const size_t n = static_cast<size_t>(R.n_scene) + m;
   if (n >= pbf::kLeafBit) return h->fail(PBF_ERR_INVALID, "too many triangles");
   const size_t px = static_cast<size_t>(p->width) * p->height;
+  const size_t batch = pbf::render_batch_samples(static_cast<int>(p->width), static_cast<int>(p->height),
+                                                 static_cast<int>(p->ns_aa));
+  const size_t scene_tree = R.n_scene > pbf::kBruteScene ? R.n_scene : 0;
   size_t need = 0;
-  carve(nullptr, n, m, R.n_mat, R.n_light, px, &need);
+  carve(nullptr, n, scene_tree, m, R.n_mat, R.n_light, px, batch, &need);
   if (need > R.buf_bytes) {
     if (R.buf) cudaFree(R.buf);
     R.buf = nullptr;
@@ -305,7 +323,7 @@ pbf_status pbf_render(pbf_handle* hh, const pbf_camera* cam, const pbf_render_pa
     R.buf_bytes = need;
   }
   size_t used = 0;
-  const Frame f = carve(static_cast<char*>(R.buf), n, m, R.n_mat, R.n_light, px, &used);
+  const Frame f = carve(static_cast<char*>(R.buf), n, scene_tree, m, R.n_mat, R.n_light, px, batch, &used);
   std::vector<pbf::RMat> mats(R.mats_host, R.mats_host + R.n_mat);
   pbf::RMat fluid{};
   fluid.kind = pbf::kMatDiffuse;
@@ -334,8 +352,10 @@ pbf_status pbf_render(pbf_handle* hh, const pbf_camera* cam, const pbf_render_pa
                                              h->stream),
                  "surface triangles");
   if (st == PBF_OK) st = h->cuda(cudaEventRecord(R.ev[1], h->stream), "event");
+  if (st == PBF_OK && scene_tree)
+    st = h->cuda(pbf::launch_bvh_build(f.tri, R.n_scene, f.scene.w, f.scene.nodes, h->stream), "bvh build");
   if (st == PBF_OK)
-    st = h->cuda(pbf::launch_bvh_build(f.tri, static_cast<uint32_t>(n), f.w, f.nodes, h->stream), "bvh build");
+    st = h->cuda(pbf::launch_bvh_build(f.tri + R.n_scene, m, f.surf.w, f.surf.nodes, h->stream), "bvh build");
   if (st == PBF_OK) st = h->cuda(cudaEventRecord(R.ev[2], h->stream), "event");
   pbf::RCam rc;
   for (int k = 0; k < 3; ++k) rc.pos[k] = static_cast<float>(cam->position[k]);
@@ -355,8 +375,9 @@ pbf_status pbf_render(pbf_handle* hh, const pbf_camera* cam, const pbf_render_pa
   a.seed = p->seed;
   a.ray_eps = p->ray_eps > 0 ? p->ray_eps : 1e-4f;
   if (st == PBF_OK)
-    st = h->cuda(pbf::launch_render(f.nodes, f.tri, f.nrm, f.w.vals, static_cast<uint32_t>(n), f.mats, f.lights, rc, a,
-                                    f.hdr, f.err, h->stream),
+    st = h->cuda(pbf::launch_render(f.tri, f.nrm, R.n_scene, m, scene_tree ? f.scene.nodes : nullptr,
+                                    f.scene.w.vals, f.surf.nodes, f.surf.w.vals, f.mats, f.lights, rc, a, f.path_rad,
+                                    f.counter, f.hdr, f.err, h->stream),
                  "render");
   if (st == PBF_OK && rgba)
     st = h->cuda(pbf::launch_tonemap(f.hdr, a.width, a.height, f.rgba, h->stream), "tonemap");

@@ -86,6 +86,41 @@ def test_deterministic_lights_match_closely(pbf, oracle_lib):
     assert out["hdr"].max() > 0.05
 
 
+def _tessellate(scene, k):
+    """Every triangle split into k * k smaller ones (same surface, more triangles)."""
+    tri, nrm, ids = [], [], []
+    for t, n, m in zip(scene.tri, scene.nrm, scene.tri_mat):
+        for i in range(k):
+            for j in range(k - i):
+                corners = [(i, j), (i + 1, j), (i, j + 1)]
+                if j + 1 < k - i:
+                    corners2 = [(i + 1, j), (i + 1, j + 1), (i, j + 1)]
+                else:
+                    corners2 = None
+                for cs in (corners, corners2):
+                    if cs is None:
+                        continue
+                    tri.append([t[0] + (t[1] - t[0]) * a / k + (t[2] - t[0]) * b / k for a, b in cs])
+                    nrm.append([n[0], n[0], n[0]])
+                    ids.append(m)
+    return R.RenderScene(np.array(tri), np.array(nrm), np.array(ids), scene.materials, scene.lights)
+
+
+def test_scene_hierarchy_matches_restatement(pbf, oracle_lib):
+    """A scene of more than 32 triangles gets its own hierarchy (the walls tessellated
+    into 160 triangles each); bars as the fixture cases."""
+    from oracle import oracle
+
+    g, scene, cam, prm = _case("render_materials")
+    big = _tessellate(scene, 4)
+    assert len(big.tri) == 16 * len(scene.tri)
+    W, H, aa, depth, area, seed = (int(v) for v in g["settings"])
+    out, sx, sn = _gpu(pbf, g, big, cam, prm, W, H, aa, depth, area, seed)
+    assert out["stats"]["triangles"] == len(big.tri) + len(sx)
+    ref = oracle.render(big, cam, sx, sn, W, H, aa, depth, area, oracle.RNG_COUNTER, seed)
+    _compare("tessellated scene", out["hdr"], ref["hdr"], 0.99, 1e-3)
+
+
 def test_tonemap_and_small_scenes(pbf):
     """The 8-bit frame is toColor of the HDR frame (rows flipped); a scene of one
     triangle and an empty scene render."""
