@@ -199,6 +199,11 @@ class Particles {
   // print the reference's per-step progress lines (particles.cpp:251-253, 267, 279, 295)
   void set_verbose(bool v) { verbose_ = v; }
   pbf_handle* handle() { return h_; }
+  // The device simulator of the current particles (created or rebuilt if needed).
+  pbf_handle* device_handle() {
+    ensure_handle();
+    return h_;
+  }
 
  private:
   pbf_params prm_{};

@@ -8,14 +8,19 @@
 //   m  one step                                  (fluid_simulate_time_step, :464-469)
 //   c  steps until one second has passed          (fluid_simulate_time(1), :444-462)
 //   g  as c, dumping every frame                  (the reference saves a screenshot)
-//   h  as c, dumping every frame                  (the reference path-traces a PNG;
-//                                                  rendering is not part of this build)
-//   -d T  simulate T seconds, dumping every frame (the -d windowless mode)
+//   h  as c, dumping and path-tracing every frame (fluid_simulate_render_time, :471-479)
+//   -d T  simulate T seconds, dumping and path-tracing every frame (the -d windowless
+//         mode, main.cpp:159-170)
+//   -f file.png  path-trace the loaded state once (the -f windowless mode)
 //
 // A frame dump is <dir>/frame_NNNNNN.bin: "PBFFRAME", int64 n, float64 time,
-// float32 positions (n, 3), float32 densities (n). With --surface every frame also
-// writes <dir>/frame_NNNNNN.obj, the surface updateSurface builds for the path tracer
-// (particles.cpp:387-395; vertices with their normals), in place of the rendered image.
+// float32 positions (n, 3), float32 densities (n). Path-traced frames are
+// <dir>/frame_NNNNNN.png, rendered by pbf_render with the reference's options -s (camera
+// rays per pixel), -l (samples per area light), -m (maximum ray depth) and -r W H
+// (default 640 x 480), in a Cornell box on the particles' collider box (the reference
+// loads its scene from a COLLADA file, which is not read here). With --surface every
+// frame also writes <dir>/frame_NNNNNN.obj, the surface updateSurface builds for the
+// path tracer (particles.cpp:387-395; vertices with their normals).
 #include <cerrno>
 #include <cstdint>
 #include <cstdio>
@@ -28,6 +33,7 @@
 
 #include "pbf.h"
 #include "pbf_particles.h"
+#include "pbf_pathtracer.h"
 #include "pbf_xml.h"
 
 namespace {
@@ -49,18 +55,23 @@ struct Options {
   bool quiet = false;
   bool graph = false;
   bool surface = false;
+  std::string png;  // -f
+  int width = 640, height = 480, ns_aa = 1, ns_area = 1, depth = 1;
 };
 
 void usage() {
   std::fprintf(stderr,
-               "usage: pbf_run -p particles.xml [-k keys] [-d seconds] [-o dir] [--graph] [--surface] [--quiet]\n"
+               "usage: pbf_run -p particles.xml [-k keys] [-d seconds] [-o dir] [-f file.png] [-r W H] [-s rays]\n"
+               "               [-l light_samples] [-m depth] [-t threads] [--graph] [--surface] [--quiet]\n"
                "       pbf_run -p particles.xml --parse-only\n"
-               "  keys: m = one step, c = one second, g / h = one second with a frame dump per step\n");
+               "  keys: m = one step, c = one second, g = one second with a frame dump per step,\n"
+               "        h = one second with a frame dump and a path-traced PNG per step\n");
 }
 
 int frame_no = 0;
 
 bool dump_surface = false;
+pbf_host::PathTracer<Vec3>* tracer = nullptr;  // set while frames are path-traced
 
 bool write_obj(Sim& sim, const std::string& path) {
   sim.surfaceUpToTimestep = false;
@@ -83,6 +94,10 @@ bool dump(Sim& sim, const std::string& dir) {
   if (dump_surface) {
     std::snprintf(name, sizeof(name), "/frame_%06d.obj", frame_no);
     if (!write_obj(sim, dir + name)) return false;
+  }
+  if (tracer) {
+    std::snprintf(name, sizeof(name), "/frame_%06d.png", frame_no);
+    tracer->render_to_file(dir + name);
   }
   std::snprintf(name, sizeof(name), "/frame_%06d.bin", frame_no++);
   std::FILE* f = std::fopen((dir + name).c_str(), "wb");
@@ -136,6 +151,15 @@ int main(int argc, char** argv) {
     else if (a == "--quiet") o.quiet = true;
     else if (a == "--graph") o.graph = true;
     else if (a == "--surface") o.surface = true;
+    else if (a == "-f") o.png = next();
+    else if (a == "-s") o.ns_aa = std::atoi(next().c_str());
+    else if (a == "-l") o.ns_area = std::atoi(next().c_str());
+    else if (a == "-m") o.depth = std::atoi(next().c_str());
+    else if (a == "-t") (void)next();  // render threads: the GPU renders
+    else if (a == "-r") {
+      o.width = std::atoi(next().c_str());
+      o.height = std::atoi(next().c_str());
+    }
     else {
       usage();
       return 2;
@@ -167,7 +191,20 @@ int main(int argc, char** argv) {
                       Vec3(pf.vel[3 * i], pf.vel[3 * i + 1], pf.vel[3 * i + 2]));
     }
     sim.estimateDensities();  // application.cpp:342
-    const bool needs_dir = o.seconds >= 0 || o.keys.find_first_of("gGhH") != std::string::npos;
+    if (o.ns_aa < 1 || o.ns_area < 1 || o.depth < 0 || o.width < 1 || o.height < 1) {
+      usage();
+      return 2;
+    }
+    pbf_host::PathTracer<Vec3> pt(o.ns_aa, o.depth, o.ns_area);
+    pbf_camera_desc cam;
+    pt.set_scene(pbf_host::cornell_box(prm.box_lo, prm.box_hi, &cam));
+    pt.set_camera(cam);
+    pt.set_frame_size(o.width, o.height);
+    pt.fluid_particles = &sim;
+    if (!o.png.empty()) {
+      pt.render_to_file(o.png);
+      std::cout << "[PathTracer] Saved " << o.png << "\n";
+    }    const bool needs_dir = o.seconds >= 0 || o.keys.find_first_of("gGhH") != std::string::npos;
     if (needs_dir && mkdir(o.out.c_str(), 0755) != 0 && errno != EEXIST) {
       std::cerr << "cannot create " << o.out << "\n";
       return EXIT_FAILURE;
@@ -182,17 +219,27 @@ int main(int argc, char** argv) {
           simulate_time(sim, 1.0, false, o.out);
           std::cout << "[Fluid Simulation] Fluid particles updated.\n";
           break;
-        case 'g': case 'G': case 'h': case 'H':
+        case 'g': case 'G':
           if (!simulate_time(sim, 1.0, true, o.out)) return EXIT_FAILURE;
           std::cout << "[Fluid Simulation] Fluid particles updated, frames saved.\n";
+          break;
+        case 'h': case 'H':
+          tracer = &pt;
+          if (!simulate_time(sim, 1.0, true, o.out)) return EXIT_FAILURE;
+          tracer = nullptr;
+          std::cout << "[Fluid Simulation] Fluid particles updated, screenshots saved.\n";
           break;
         default:
           std::cerr << "unknown key '" << k << "'\n";
           return 2;
       }
     }
-    if (o.seconds >= 0 && !simulate_time(sim, o.seconds, true, o.out)) return EXIT_FAILURE;
-    if (o.keys.empty() && o.seconds < 0 && !dump(sim, o.out.empty() ? "." : o.out)) {
+    if (o.seconds >= 0) {
+      tracer = &pt;
+      if (!simulate_time(sim, o.seconds, true, o.out)) return EXIT_FAILURE;
+      tracer = nullptr;
+    }
+    if (o.keys.empty() && o.seconds < 0 && o.png.empty() && !dump(sim, o.out.empty() ? "." : o.out)) {
       // nothing requested: write the loaded state for inspection
     }
   } catch (const std::exception& e) {

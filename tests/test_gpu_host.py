@@ -104,3 +104,35 @@ def test_surface_dumps_match_the_surface_call(pbf_run, tmp_path):
     assert len(fc) == len(xyz) > 100
     assert np.abs(v.reshape(-1, 3, 3) - xyz).max() < 1e-5
     assert np.abs(vn.reshape(-1, 3, 3) - nrm).max() < 1e-5
+
+
+def test_path_traced_frames(pbf_run, tmp_path):
+    """pbf_run -f renders the loaded state (the reference's windowless -f) through the C++
+    PathTracer facade: the PNG is the frame Simulator.render gives for the same state,
+    scene and settings; -d renders one PNG per dumped frame."""
+    from fluid_gb300 import pbf
+    from fluid_gb300 import render as R
+    from oracle.ref_runner import read_png
+
+    g = np.load(GOLDEN / "surface_p_default_0step.npz")
+    prm = params_from_json(str(g["params"]))
+    pos = g["pos"].astype(np.float32).astype(np.float64)
+    f = tmp_path / "p.xml"
+    scenes.write_xml(f, pos, np.zeros_like(pos), prm.rest_density, prm)
+    png = tmp_path / "one.png"
+    r = subprocess.run([pbf_run, "-p", str(f), "-f", str(png), "-r", "64", "48", "-s", "2", "-m", "2", "-l", "2",
+                        "--quiet"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    img = read_png(png)
+    assert img.shape == (48, 64, 4)
+    scene, cam = R.cornell_box(prm.box_lo, prm.box_hi)
+    with pbf.Simulator(pos, np.zeros_like(pos), prm.with_(rest_density=float(np.float32(prm.rest_density)))) as sim:
+        sim.set_render_scene(scene)
+        want = sim.render(cam, 64, 48, 2, 2, 2, seed=1, hdr=False)["rgba"]
+    assert np.array_equal(img, want) and img[..., :3].max() > 0
+    out = tmp_path / "frames"
+    r = subprocess.run([pbf_run, "-p", str(f), "-d", str(prm.dt * 0.5), "-o", str(out), "-r", "32", "24", "--quiet"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    pngs = sorted(out.glob("frame_*.png"))
+    assert len(pngs) == 2 and all(read_png(p).shape == (24, 32, 4) for p in pngs)
