@@ -508,7 +508,7 @@ def render_reference_sample(settings=(4, 3, 4)) -> dict | None:
             "seconds": {f"{w}x{h}": v for (w, h), v in t.items()}}
 
 
-def bench_render(sim, prm) -> dict:
+def bench_render(sim, prm, settings=RENDER_SETTINGS, reference: bool = True) -> dict:
     """Path tracing (pbf_render) of the workload's configured state in a Cornell box on the
     collider box, RENDER_SETTINGS, the surface over the collider box at updateSurface's
     settings. Device time of each phase from the call's own CUDA events (surface: cell
@@ -516,7 +516,7 @@ def bench_render(sim, prm) -> dict:
     best of 2 frames after a warm-up; the wall time adds the 8-bit frame's copy to the host."""
     from fluid_gb300 import render as R
 
-    W, H, aa, depth, area = RENDER_SETTINGS
+    W, H, aa, depth, area = settings
     scene, cam = R.cornell_box(prm.box_lo, prm.box_hi)
     sim.restore()
     sim.set_render_scene(scene)
@@ -537,7 +537,7 @@ def bench_render(sim, prm) -> dict:
             "ms_trace": st["ms_trace"], "ms_frame_wall": wall * 1e3, "paths_per_s": paths / (st["ms_trace"] / 1e3),
             "timing": "CUDA events per phase inside pbf_render; best of 2 after a warm-up"}
     try:
-        ref = render_reference_sample((aa, depth, area))
+        ref = render_reference_sample((aa, depth, area)) if reference else None
     except Exception as exc:  # the reference's renderer is a reported baseline only
         ref = {"unavailable": str(exc)[:200]}
     if ref:
@@ -726,6 +726,10 @@ def main(argv=None):
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-surface", action="store_true")
     ap.add_argument("--no-render", action="store_true")
+    ap.add_argument("--render-only", action="store_true",
+                    help="only the path-tracing leg (one JSON object), e.g. for an ncu capture")
+    ap.add_argument("--render-settings", type=int, nargs=5, default=list(RENDER_SETTINGS),
+                    metavar=("W", "H", "AA", "DEPTH", "LIGHT_SAMPLES"))
     ap.add_argument("--adjoint-only", action="store_true",
                     help="run only the adjoint leg and print its object (a profiling aid, not a bench line)")
     args = ap.parse_args(argv)
@@ -740,6 +744,19 @@ def main(argv=None):
 
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
+    if args.render_only:
+        import torch
+
+        from fluid_gb300 import pbf
+
+        torch.cuda.set_device(local)
+        build = scenes.SCENES[args.workload]
+        scene = build() if args.seed is None else build(args.seed)
+        with pbf.Simulator(scene.pos, scene.vel, scene.params, device=local) as sim:
+            sim.snapshot()
+            line = bench_render(sim, scene.params, tuple(args.render_settings), reference=not args.no_cpu_baseline)
+        print(json.dumps({"render": line}))
+        return 0
     if args.adjoint_only:
         import torch
 
