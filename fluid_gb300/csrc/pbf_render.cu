@@ -783,9 +783,9 @@ cudaError_t launch_bvh_build(const RTri* tri, uint32_t n, const BvhScratch& w, B
   return cudaGetLastError();
 }
 
-uint32_t render_batch_samples(int width, int height, int ns_aa) {
+uint32_t render_batch_samples(int width, int height, int ns_aa, uint32_t budget_mib) {
   const size_t px = static_cast<size_t>(width) * height;
-  const size_t budget = size_t(256) << 20;  // path radiance buffer of one batch
+  const size_t budget = static_cast<size_t>(budget_mib ? budget_mib : 256) << 20;  // path radiance of one batch
   const size_t per = std::max<size_t>(1, budget / (12 * std::max<size_t>(px, 1)));
   return static_cast<uint32_t>(std::min<size_t>(per, static_cast<size_t>(ns_aa)));
 }
@@ -803,7 +803,7 @@ cudaError_t launch_render(const RTri* tri, const RNrm* nrm, uint32_t n_scene, ui
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_paths, 128, 0);
   if (e != cudaSuccess) return e;
-  const uint32_t nb = render_batch_samples(a.width, a.height, a.ns_aa);
+  const uint32_t nb = static_cast<uint32_t>(std::max(a.batch, 1));
   for (int s0 = 0; s0 < a.ns_aa; s0 += static_cast<int>(nb)) {
     const int cnt = std::min(static_cast<int>(nb), a.ns_aa - s0);
     const size_t total = px * static_cast<size_t>(cnt);

@@ -53,6 +53,7 @@ struct RArgs {
   int width, height, ns_aa, max_depth, ns_area;
   int n_mat, n_light;
   unsigned long long seed;
+  int batch;      // samples per pixel per batch (render_batch_samples)
   float ray_eps;  // start of secondary rays (the reference's EPS_D is below FP32 resolution)
 };
 
@@ -86,8 +87,8 @@ cudaError_t launch_surface_to_tris(const float* xyz, const float* nrm, uint32_t 
                                    RNrm* nn, cudaStream_t s);
 cudaError_t launch_bvh_build(const RTri* tri, uint32_t n, const BvhScratch& w, BvhNode* nodes, cudaStream_t s);
 // Samples per pixel traced in one batch: the batch's path radiance (npix * batch * 3
-// floats, path_rad) stays within 256 MiB.
-uint32_t render_batch_samples(int width, int height, int ns_aa);
+// floats, path_rad) stays within budget_mib MiB (0: 256).
+uint32_t render_batch_samples(int width, int height, int ns_aa, uint32_t budget_mib);
 // hdr: W * H * 3 floats, row y = 0 first (the bottom row, as the reference's sample buffer).
 // *_leaf: a build's vals (sorted position -> triangle of its range); counter: one word;
 // err bit 0: a traversal stack overflowed (deeper than kBvhStack levels).

@@ -310,7 +310,7 @@ pbf_status pbf_render(pbf_handle* hh, const pbf_camera* cam, const pbf_render_pa
   if (n >= pbf::kLeafBit) return h->fail(PBF_ERR_INVALID, "too many triangles");
   const size_t px = static_cast<size_t>(p->width) * p->height;
   const size_t batch = pbf::render_batch_samples(static_cast<int>(p->width), static_cast<int>(p->height),
-                                                 static_cast<int>(p->ns_aa));
+                                                 static_cast<int>(p->ns_aa), p->path_buffer_mib);
   const size_t scene_tree = R.n_scene > pbf::kBruteScene ? R.n_scene : 0;
   size_t need = 0;
   carve(nullptr, n, scene_tree, m, R.n_mat, R.n_light, px, batch, &need);
@@ -374,6 +374,7 @@ pbf_status pbf_render(pbf_handle* hh, const pbf_camera* cam, const pbf_render_pa
   a.n_light = R.n_light;
   a.seed = p->seed;
   a.ray_eps = p->ray_eps > 0 ? p->ray_eps : 1e-4f;
+  a.batch = static_cast<int>(batch);
   if (st == PBF_OK)
     st = h->cuda(pbf::launch_render(f.tri, f.nrm, R.n_scene, m, scene_tree ? f.scene.nodes : nullptr,
                                     f.scene.w.vals, f.surf.nodes, f.surf.w.vals, f.mats, f.lights, rc, a, f.path_rad,

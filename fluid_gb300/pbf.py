@@ -76,7 +76,7 @@ class CCamera(ctypes.Structure):
 class CRenderParams(ctypes.Structure):
     _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("ns_aa", ctypes.c_uint32),
                 ("max_ray_depth", ctypes.c_uint32), ("ns_area_light", ctypes.c_uint32),
-                ("fluid_surface", ctypes.c_uint32), ("surface_bounds", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("fluid_surface", ctypes.c_uint32), ("surface_bounds", ctypes.c_uint32), ("path_buffer_mib", ctypes.c_uint32),
                 ("seed", ctypes.c_uint64), ("isolevel", ctypes.c_double), ("step", ctypes.c_double),
                 ("surface_lo", ctypes.c_double * 3), ("surface_hi", ctypes.c_double * 3),
                 ("fluid_albedo", ctypes.c_float * 3), ("ray_eps", ctypes.c_float)]
@@ -355,7 +355,8 @@ class Simulator:
 
     def render(self, cam, width: int, height: int, ns_aa: int = 1, max_depth: int = 1, ns_area_light: int = 1,
                seed: int = 1, fluid_surface: bool = True, fluid_albedo=(0.1, 0.1, 0.8), ray_eps: float = 0.0,
-               hdr: bool = True, rgba: bool = True, lo=None, hi=None, iso: float = 0.0, step: float = 0.0) -> dict:
+               hdr: bool = True, rgba: bool = True, lo=None, hi=None, iso: float = 0.0, step: float = 0.0,
+               path_buffer_mib: int = 0) -> dict:
         """One frame of PathTracer::render_to_file: ``hdr`` (H, W, 3) float32 with row 0 the
         bottom row, ``rgba`` (H, W, 4) uint8 with the top row first (the reference's PNG),
         ``stats`` (triangles and device milliseconds per phase). ``cam`` is a CameraDesc or
@@ -368,6 +369,7 @@ class Simulator:
         p.fluid_surface, p.seed, p.ray_eps = int(bool(fluid_surface)), seed, ray_eps
         p.fluid_albedo = (ctypes.c_float * 3)(*fluid_albedo)
         p.isolevel, p.step = iso, step
+        p.path_buffer_mib = path_buffer_mib
         if lo is not None:
             p.surface_bounds = 1
             p.surface_lo = (ctypes.c_double * 3)(*lo)
