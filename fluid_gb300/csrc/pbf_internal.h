@@ -230,7 +230,8 @@ cudaError_t launch_density_at(const Buffers& b, const DevParams& p, int cur, siz
 cudaError_t launch_surface_count(const Buffers& b, const DevParams& p, int cur, const SurfGrid& g, float iso,
                                  const SurfTable* tab, float* field, uint32_t* count, uint32_t* first,
                                  uint32_t* tile_sums, cudaStream_t s);
-// Triangles with index < cap: 9 floats of vertices and 9 of vertex normals each.
+// Triangles with index < cap (cap at most the total of the counts): 9 floats of vertices
+// and 9 of vertex normals each.
 cudaError_t launch_surface_emit(const Buffers& b, const DevParams& p, int cur, const SurfGrid& g, float iso,
                                 const SurfTable* tab, const float* field, const uint32_t* first, float* xyz,
                                 float* nrm, uint32_t cap, cudaStream_t s);

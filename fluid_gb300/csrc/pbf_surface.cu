@@ -205,56 +205,60 @@ __device__ __forceinline__ float3 vertex_interp(float iso, float3 p1, float3 p2,
   return make_float3(p1.x + mu * (p2.x - p1.x), p1.y + mu * (p2.y - p1.y), p1.z + mu * (p2.z - p1.z));
 }
 
+// One thread per triangle vertex: triangle t lies in the cube c with first[c] <= t <
+// first[c + 1] (binary search; empty cubes have first[c] == first[c + 1]), as the q-th of
+// its cube's triangles. Its vertex v is vertexInterp on the cube's edge in the cube's own
+// corner order, its normal getVertexNormal: normalized central differences of
+// estimateDensityAt at +-GRADIENT_EPS. A thread per cube instead would leave most lanes of
+// a warp on empty cubes while one lane evaluated up to 5 triangles' normals.
 __global__ void k_surf_emit(const float* __restrict__ field, const SurfTable* __restrict__ tab, SurfGrid g,
                             float iso, const uint32_t* __restrict__ first, const float4* __restrict__ pos,
                             const uint32_t* __restrict__ cell_start, const SceneDesc* __restrict__ scenes,
-                            float* __restrict__ xyz, float* __restrict__ nrm, uint32_t cap, DevParams P,
+                            float* __restrict__ xyz, float* __restrict__ nrm, uint32_t count, DevParams P,
                             int64_t ncubes) {
-  const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (c >= ncubes) return;
+  const int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (tid >= 3 * static_cast<int64_t>(count)) return;
+  const uint32_t t = static_cast<uint32_t>(tid / 3);
+  const int v = static_cast<int>(tid % 3);
+  int64_t lo = 0, hi = ncubes;  // first[lo] <= t < first[hi] (first[ncubes] = total > t)
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (first[mid] <= t) lo = mid;
+    else hi = mid;
+  }
+  const int64_t c = lo;
+  const int q = static_cast<int>(t - first[c]);
   int ix, iy, iz;
   cube_of(g, c, &ix, &iy, &iz);
-  float val[8];
-  float3 p[8];
   int ci = 0;
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int i = ix + corner_x(k), j = iy + corner_y(k), l = iz + corner_z(k);
-    val[k] = corner_value(field, g, i, j, l);
-    p[k] = corner_point(g, i, j, l);
-    if (val[k] < iso) ci |= 1 << k;
-  }
-  const int nt = tab->ntri[ci];
-  if (nt == 0) return;
+  for (int k = 0; k < 8; ++k)
+    if (corner_value(field, g, ix + corner_x(k), iy + corner_y(k), iz + corner_z(k)) < iso) ci |= 1 << k;
+  const int e = tab->tri[ci][3 * q + v];
+  const int a = edge_a(e), b = edge_b(e);
+  const int ia = ix + corner_x(a), ja = iy + corner_y(a), ka = iz + corner_z(a);
+  const int ib = ix + corner_x(b), jb = iy + corner_y(b), kb = iz + corner_z(b);
+  const float3 x = vertex_interp(iso, corner_point(g, ia, ja, ka), corner_point(g, ib, jb, kb),
+                                 corner_value(field, g, ia, ja, ka), corner_value(field, g, ib, jb, kb));
   const SceneDesc& sc = scenes[0];
   const float eps = 0.001f;  // GRADIENT_EPS, particles.cpp:16
-  uint32_t t = first[c];
-  for (int q = 0; q < nt; ++q, ++t) {
-    if (t >= cap) return;
-#pragma unroll
-    for (int v = 0; v < 3; ++v) {
-      const int e = tab->tri[ci][3 * q + v];
-      const int a = edge_a(e), b = edge_b(e);
-      const float3 x = vertex_interp(iso, p[a], p[b], val[a], val[b]);
-      float3 n;
-      n.x = density_at_point(make_float3(x.x - eps, x.y, x.z), pos, cell_start, sc, P) -
-            density_at_point(make_float3(x.x + eps, x.y, x.z), pos, cell_start, sc, P);
-      n.y = density_at_point(make_float3(x.x, x.y - eps, x.z), pos, cell_start, sc, P) -
-            density_at_point(make_float3(x.x, x.y + eps, x.z), pos, cell_start, sc, P);
-      n.z = density_at_point(make_float3(x.x, x.y, x.z - eps), pos, cell_start, sc, P) -
-            density_at_point(make_float3(x.x, x.y, x.z + eps), pos, cell_start, sc, P);
-      const float nn = sqrtf(dot3(n, n));
-      if (nn > 0.f) n = n * (1.0f / nn);
-      float* o = xyz + 9 * static_cast<size_t>(t) + 3 * v;
-      float* m = nrm + 9 * static_cast<size_t>(t) + 3 * v;
-      o[0] = x.x;
-      o[1] = x.y;
-      o[2] = x.z;
-      m[0] = n.x;
-      m[1] = n.y;
-      m[2] = n.z;
-    }
-  }
+  float3 n;
+  n.x = density_at_point(make_float3(x.x - eps, x.y, x.z), pos, cell_start, sc, P) -
+        density_at_point(make_float3(x.x + eps, x.y, x.z), pos, cell_start, sc, P);
+  n.y = density_at_point(make_float3(x.x, x.y - eps, x.z), pos, cell_start, sc, P) -
+        density_at_point(make_float3(x.x, x.y + eps, x.z), pos, cell_start, sc, P);
+  n.z = density_at_point(make_float3(x.x, x.y, x.z - eps), pos, cell_start, sc, P) -
+        density_at_point(make_float3(x.x, x.y, x.z + eps), pos, cell_start, sc, P);
+  const float nn = sqrtf(dot3(n, n));
+  if (nn > 0.f) n = n * (1.0f / nn);
+  float* o = xyz + 9 * static_cast<size_t>(t) + 3 * v;
+  float* m = nrm + 9 * static_cast<size_t>(t) + 3 * v;
+  o[0] = x.x;
+  o[1] = x.y;
+  o[2] = x.z;
+  m[0] = n.x;
+  m[1] = n.y;
+  m[2] = n.z;
 }
 
 inline unsigned blocks_for(int64_t n, int block) { return static_cast<unsigned>((n + block - 1) / block); }
@@ -275,8 +279,9 @@ cudaError_t launch_surface_emit(const Buffers& b, const DevParams& P, int cur, c
                                 const SurfTable* tab, const float* field, const uint32_t* first, float* xyz,
                                 float* nrm, uint32_t cap, cudaStream_t s) {
   const int64_t cubes = static_cast<int64_t>(g.nc[0]) * g.nc[1] * g.nc[2];
-  k_surf_emit<<<blocks_for(cubes, 128), 128, 0, s>>>(field, tab, g, iso, first, b.pos[cur], b.cell_start,
-                                                      b.scenes, xyz, nrm, cap, P, cubes);
+  if (cap == 0) return cudaSuccess;
+  k_surf_emit<<<blocks_for(3 * static_cast<int64_t>(cap), 128), 128, 0, s>>>(
+      field, tab, g, iso, first, b.pos[cur], b.cell_start, b.scenes, xyz, nrm, cap, P, cubes);
   return cudaGetLastError();
 }
 
