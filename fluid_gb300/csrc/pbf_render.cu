@@ -9,9 +9,13 @@
 //                      "Maximizing parallelism in the construction of BVHs, octrees
 //                      and k-d trees"), ties broken by sorted position
 //   k_refit            bottom-up boxes: the second child to finish fills its parent
-//   k_render_paths     persistent threads, one path each at a time: camera ray,
-//                      closest hits, direct light from every light, one BSDF-sampled
-//                      bounce per level with Russian roulette
+//   k_wf_camera        a batch of paths (whole samples of every pixel): camera rays
+//   per bounce level, over the queue of live paths (wavefront):
+//     k_wf_trace<false>  closest hits, persistent threads fetching rays as they finish
+//     k_wf_shade         emission, light samples as shadow-ray slots, BSDF sample and
+//                        Russian roulette; continuing paths to the next queue
+//     k_wf_trace<true>   visibility of the shadow-ray slots
+//     k_wf_resolve       visible light samples added to the paths' radiance
 //   k_accumulate       per-pixel sums of the paths' radiance in sample order
 //   k_tonemap          HDRImageBuffer::toColor + ImageBuffer::update_pixel
 //
@@ -342,70 +346,6 @@ __device__ __forceinline__ bool box_test(const float4& lo, const float4& hi, con
   return t0 <= t1;
 }
 
-// Walk of one hierarchy over triangles tris[base + leaf]: closest hit (ANY = false) below
-// tmax, updating tmax / best / bu / bv; or any hit (ANY = true: returns true at the first).
-template <bool ANY>
-__device__ bool walk(const BvhNode* __restrict__ nodes, const RTri* __restrict__ tris,
-                     const uint32_t* __restrict__ leaf_tri, uint32_t n, uint32_t base, const Ray& r, float& tmax,
-                     int& best, float& bu, float& bv, unsigned* err) {
-  if (n == 0) return false;
-  if (n == 1) {
-    float t, u, v;
-    if (tri_test(tris[base], r, tmax, &t, &u, &v)) {
-      best = static_cast<int>(base);
-      tmax = t;
-      bu = u;
-      bv = v;
-      return ANY;
-    }
-    return false;
-  }
-  uint32_t stack[kBvhStack];
-  int sp = 0;
-  uint32_t node = 0;
-  while (true) {
-    const BvhNode nd = nodes[node];
-    float tl, tr;
-    bool hl = box_test(nd.lo_l, nd.hi_l, r, tmax, &tl);
-    bool hr = box_test(nd.lo_r, nd.hi_r, r, tmax, &tr);
-    const uint32_t cl = __float_as_uint(nd.lo_l.w), cr = __float_as_uint(nd.lo_r.w);
-#pragma unroll
-    for (int side = 0; side < 2; ++side) {
-      const uint32_t c = side ? cr : cl;
-      bool& h = side ? hr : hl;
-      if (h && (c & kLeafBit)) {
-        h = false;
-        const uint32_t ti = base + leaf_tri[c & ~kLeafBit];
-        float t, u, v;
-        if (tri_test(tris[ti], r, tmax, &t, &u, &v)) {
-          best = static_cast<int>(ti);
-          tmax = t;
-          bu = u;
-          bv = v;
-          if (ANY) return true;
-        }
-      }
-    }
-    if (hl && hr) {
-      const bool lfirst = tl <= tr;
-      if (sp < kBvhStack) {
-        stack[sp++] = lfirst ? cr : cl;
-      } else {
-        atomicOr(err, 1u);
-      }
-      node = lfirst ? cl : cr;
-    } else if (hl) {
-      node = cl;
-    } else if (hr) {
-      node = cr;
-    } else {
-      if (sp == 0) break;
-      node = stack[--sp];
-    }
-  }
-  return false;
-}
-
 // Every triangle of tris[0, n) in index order.
 template <bool ANY>
 __device__ bool brute(const RTri* __restrict__ tris, uint32_t n, const Ray& r, float& tmax, int& best, float& bu,
@@ -555,32 +495,7 @@ struct Scene {
   const uint32_t* surf_leaf;
 };
 
-__device__ __forceinline__ bool closest(const Scene& sc, const Ray& r, int* ti, float* t, float* u, float* v,
-                                        unsigned* err) {
-  float tmax = r.tmax, bu = 0.f, bv = 0.f;
-  int best = -1;
-  if (sc.scene_nodes)
-    walk<false>(sc.scene_nodes, sc.tri, sc.scene_leaf, sc.n_scene, 0u, r, tmax, best, bu, bv, err);
-  else
-    brute<false>(sc.tri, sc.n_scene, r, tmax, best, bu, bv);
-  walk<false>(sc.surf_nodes, sc.tri, sc.surf_leaf, sc.n_surf, sc.n_scene, r, tmax, best, bu, bv, err);
-  *ti = best;
-  *t = tmax;
-  *u = bu;
-  *v = bv;
-  return best >= 0;
-}
-
-__device__ __forceinline__ bool occluded(const Scene& sc, const Ray& r, unsigned* err) {
-  float tmax = r.tmax, bu, bv;
-  int best = -1;
-  if (sc.scene_nodes ? walk<true>(sc.scene_nodes, sc.tri, sc.scene_leaf, sc.n_scene, 0u, r, tmax, best, bu, bv, err)
-                     : brute<true>(sc.tri, sc.n_scene, r, tmax, best, bu, bv))
-    return true;
-  return walk<true>(sc.surf_nodes, sc.tri, sc.surf_leaf, sc.n_surf, sc.n_scene, r, tmax, best, bu, bv, err);
-}
-
-constexpr uint32_t kNoPath = 0xffffffffu;
+constexpr uint32_t kNoItem = 0xffffffffu;
 
 __device__ __forceinline__ unsigned lane_lt() {
   unsigned m;
@@ -588,130 +503,354 @@ __device__ __forceinline__ unsigned lane_lt() {
   return m;
 }
 
-// Persistent path tracer: each thread carries one path (sample s of pixel p,
-// PathTracer::raytrace_pixel, pathtracer.cpp:584-604) one bounce of trace_ray
-// (pathtracer.cpp:553-582) per loop turn, and takes the next path of the batch as soon as
-// its path ends, so a warp's lanes stay busy however long their paths are. Path q of the
-// batch is sample s0 + q / npix of pixel q % npix; its radiance goes to rad[q].
-__global__ void __launch_bounds__(128) k_render_paths(Scene sc, RCam cam, RArgs a, int s0, uint32_t total,
-                                                      float* __restrict__ rad, unsigned* counter, unsigned* err) {
+// Warp-aggregated append: every lane of the warp calls it (converged); lanes with want
+// get consecutive indices of *counter.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
+  const unsigned full = 0xffffffffu;
+  const unsigned m = __ballot_sync(full, want);
+  if (m == 0) return 0;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (static_cast<int>(threadIdx.x & 31u) == leader) base = atomicAdd(counter, static_cast<uint32_t>(__popc(m)));
+  base = __shfl_sync(full, base, leader);
+  return base + static_cast<uint32_t>(__popc(m & lane_lt()));
+}
+
+// A ray walk that advances one node at a time, so that a lane whose ray is done can take
+// the next ray while the warp's other lanes keep walking theirs (persistent traversal
+// with dynamic ray fetch, Aila and Laine, "Understanding the efficiency of ray traversal
+// on GPUs", 2009). Phase 0 walks the scene's tree (when the scene has one), phase 1 the
+// surface's; phase 2 is done.
+struct Walk {
+  uint32_t node;
+  int sp;
+  int phase;
+  int best;
+  float tmax, bu, bv;
+  uint32_t stack[kBvhStack];
+};
+
+// Enters the first tree from s.phase on with more than one triangle (a tree of one is
+// tested at once).
+template <bool ANY>
+__device__ __forceinline__ void walk_enter(const Scene& sc, const Ray& r, Walk& s) {
+  while (s.phase < 2) {
+    const uint32_t n = s.phase == 0 ? (sc.scene_nodes ? sc.n_scene : 0u) : sc.n_surf;
+    const uint32_t base = s.phase == 0 ? 0u : sc.n_scene;
+    if (n >= 2) {
+      s.node = 0;
+      s.sp = 0;
+      return;
+    }
+    if (n == 1) {
+      float t, u, v;
+      if (tri_test(sc.tri[base], r, s.tmax, &t, &u, &v)) {
+        s.best = static_cast<int>(base);
+        s.tmax = t;
+        s.bu = u;
+        s.bv = v;
+        if (ANY) {
+          s.phase = 2;
+          return;
+        }
+      }
+    }
+    ++s.phase;
+  }
+}
+
+template <bool ANY>
+__device__ __forceinline__ void walk_begin(const Scene& sc, const Ray& r, Walk& s) {
+  s.tmax = r.tmax;
+  s.best = -1;
+  s.bu = s.bv = 0.f;
+  s.phase = 0;
+  if (!sc.scene_nodes && brute<ANY>(sc.tri, sc.n_scene, r, s.tmax, s.best, s.bu, s.bv)) {
+    s.phase = 2;  // any hit found among the scene's triangles
+    return;
+  }
+  walk_enter<ANY>(sc, r, s);
+}
+
+// One node of the current tree: both children's boxes, leaves tested at once, the nearer
+// hit child next and the farther one pushed.
+template <bool ANY>
+__device__ __forceinline__ void walk_step(const Scene& sc, const Ray& r, Walk& s, unsigned* err) {
+  const bool scene = s.phase == 0;
+  const BvhNode* __restrict__ nodes = scene ? sc.scene_nodes : sc.surf_nodes;
+  const uint32_t* __restrict__ leaf = scene ? sc.scene_leaf : sc.surf_leaf;
+  const uint32_t base = scene ? 0u : sc.n_scene;
+  const BvhNode nd = nodes[s.node];
+  float tl, tr;
+  bool hl = box_test(nd.lo_l, nd.hi_l, r, s.tmax, &tl);
+  bool hr = box_test(nd.lo_r, nd.hi_r, r, s.tmax, &tr);
+  const uint32_t cl = __float_as_uint(nd.lo_l.w), cr = __float_as_uint(nd.lo_r.w);
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const uint32_t c = side ? cr : cl;
+    bool& h = side ? hr : hl;
+    if (h && (c & kLeafBit)) {
+      h = false;
+      const uint32_t ti = base + leaf[c & ~kLeafBit];
+      float t, u, v;
+      if (tri_test(sc.tri[ti], r, s.tmax, &t, &u, &v)) {
+        s.best = static_cast<int>(ti);
+        s.tmax = t;
+        s.bu = u;
+        s.bv = v;
+        if (ANY) {
+          s.phase = 2;
+          return;
+        }
+      }
+    }
+  }
+  if (hl && hr) {
+    const bool lfirst = tl <= tr;
+    if (s.sp < kBvhStack) {
+      s.stack[s.sp++] = lfirst ? cr : cl;
+    } else {
+      atomicOr(err, 1u);
+    }
+    s.node = lfirst ? cl : cr;
+  } else if (hl) {
+    s.node = cl;
+  } else if (hr) {
+    s.node = cr;
+  } else if (s.sp > 0) {
+    s.node = s.stack[--s.sp];
+  } else {
+    ++s.phase;
+    walk_enter<ANY>(sc, r, s);
+  }
+}
+
+using WfArgs = WfBuffers;
+
+// Closest hits (ANY = false) of the paths in queue[0, *count), or visibility (ANY = true)
+// of the shadow slots in queue[0, *count); persistent threads with dynamic fetch.
+template <bool ANY>
+__global__ void __launch_bounds__(128) k_wf_trace(Scene sc, WfArgs w, const uint32_t* __restrict__ queue,
+                                                  const uint32_t* __restrict__ count, uint32_t* fetch, float ray_eps,
+                                                  unsigned* err) {
   const unsigned full = 0xffffffffu, lane = threadIdx.x & 31u;
-  const uint32_t npix = static_cast<uint32_t>(a.width) * static_cast<uint32_t>(a.height);
-  const V3 cpos = ld3(cam.pos), cx = ld3(cam.c2w), cy = ld3(cam.c2w + 3), cz = ld3(cam.c2w + 6);
-  uint32_t q = kNoPath;
-  Ray r = make_ray(cpos, cz, 0.f, 0.f);
-  V3 L = mk(0.f, 0.f, 0.f), beta = mk(1.f, 1.f, 1.f);
-  int depth = 0;
-  bool includeLe = true;
-  Rng g{0ull, 0ull};
+  const uint32_t total = *count;
+  uint32_t item = kNoItem;
   bool drained = false;
+  Ray r = make_ray(mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 1.f), 0.f, 0.f);
+  Walk s;
+  s.phase = 2;
   while (true) {
     if (!drained) {
-      const unsigned need = __ballot_sync(full, q == kNoPath);
+      const unsigned need = __ballot_sync(full, item == kNoItem);
       if (need) {
         const int leader = __ffs(need) - 1;
         uint32_t base = 0;
-        if (static_cast<int>(lane) == leader) base = atomicAdd(counter, static_cast<unsigned>(__popc(need)));
+        if (static_cast<int>(lane) == leader) base = atomicAdd(fetch, static_cast<uint32_t>(__popc(need)));
         base = __shfl_sync(full, base, leader);
         if (base + static_cast<uint32_t>(__popc(need)) >= total) drained = true;
-        if (q == kNoPath) {
-          const uint32_t mine = base + static_cast<uint32_t>(__popc(need & lane_lt()));
-          if (mine < total) {
-            q = mine;
-            const uint32_t pix = q % npix;
-            const int s = s0 + static_cast<int>(q / npix);
-            g = Rng{path_key(a.seed, pix, static_cast<unsigned long long>(s)), 0ull};
-            float jx = 0.5f, jy = 0.5f;
-            if (a.ns_aa > 1) {
-              jx = g.next();
-              jy = g.next();
+        if (item == kNoItem) {
+          const uint32_t idx = base + static_cast<uint32_t>(__popc(need & lane_lt()));
+          if (idx < total) {
+            item = queue[idx];
+            if (ANY) {
+              const uint32_t q = item / static_cast<uint32_t>(w.slots);
+              const float4 o = w.o[q], sd = w.sdir[item];
+              r = make_ray(mk(o.x, o.y, o.z), mk(sd.x, sd.y, sd.z), ray_eps, sd.w);
+            } else {
+              const float4 o = w.o[item], d = w.d[item];
+              r = make_ray(mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), o.w, d.w);
             }
-            const int px = static_cast<int>(pix % static_cast<uint32_t>(a.width));
-            const int py = static_cast<int>(pix / static_cast<uint32_t>(a.width));
-            const float xn = (px + jx) / a.width, yn = (py + jy) / a.height;
-            r = make_ray(cpos, unit(cx * ((xn - 0.5f) * cam.htan) + cy * ((yn - 0.5f) * cam.vtan) - cz), cam.nclip,
-                         cam.fclip);
-            L = mk(0.f, 0.f, 0.f);
-            beta = mk(1.f, 1.f, 1.f);
-            depth = a.max_depth;
-            includeLe = true;
+            walk_begin<ANY>(sc, r, s);
           }
         }
       }
     }
-    if (__ballot_sync(full, q != kNoPath) == 0) break;
-    if (q == kNoPath) continue;
-    bool done = true;
-    int ti;
-    float t, u, v;
-    if (closest(sc, r, &ti, &t, &u, &v, err)) {
-      const RTri tr = sc.tri[ti];
-      const RMat m = sc.mats[__float_as_int(tr.p1.w)];
-      const RNrm nn = sc.nrm[ti];
-      const float w = 1.f - u - v;
-      const V3 n = w * v3(nn.n1) + u * v3(nn.n2) + v * v3(nn.n3);
-      const V3 hit = r.o + r.d * t;
-      if (includeLe && m.kind == kMatEmission) L = L + mulv(beta, ld3(m.c1));
-      const Frame f = coord_space(n);
-      if (!mat_delta(m.kind)) {
-        // estimate_direct_lighting (pathtracer.cpp:483-524); only the diffuse BSDF has f != 0
-        const V3 fval = m.kind == kMatDiffuse ? ld3(m.c1) * (1.f / kPi) : mk(0.f, 0.f, 0.f);
-        V3 Ld = mk(0.f, 0.f, 0.f);
-        for (int li = 0; li < a.n_light; ++li) {
-          const RLight& l = sc.lights[li];
-          const int ns = (l.kind == kLightDirectional || l.kind == kLightPoint) ? 1 : a.ns_area;
-          V3 Ll = mk(0.f, 0.f, 0.f);
-          for (int i = 0; i < ns; ++i) {
-            V3 wi;
-            float dist, pdf;
-            const V3 Ls = sample_L(l, hit, &wi, &dist, &pdf, g);
-            const float cz_in = dot(f.z, wi);
-            if (cz_in < 0.f) continue;
-            if (occluded(sc, make_ray(hit, wi, a.ray_eps, dist), err)) continue;
-            Ll = Ll + mulv(Ls, fval) * (fabsf(cz_in) / pdf);
-          }
-          Ld = Ld + mk(Ll.x / ns, Ll.y / ns, Ll.z / ns);
-        }
-        L = L + mulv(beta, Ld);
+    if (__ballot_sync(full, item != kNoItem) == 0) break;
+    if (item == kNoItem) continue;
+    for (int k = 0; k < 4 && s.phase < 2; ++k) walk_step<ANY>(sc, r, s, err);
+    if (s.phase >= 2) {
+      if (ANY) {
+        w.scon[item].w = s.best >= 0 ? 0.f : 1.f;
+      } else {
+        w.hit[item] = make_float4(__int_as_float(s.best), s.tmax, s.bu, s.bv);
       }
+      item = kNoItem;
+    }
+  }
+}
+
+// Camera rays of the batch's paths (PathTracer::raytrace_pixel, pathtracer.cpp:584-604):
+// path q is sample s0 + q / npix of pixel q % npix; all paths join queue a.
+__global__ void k_wf_camera(WfArgs w, RCam cam, RArgs a, int s0, uint32_t paths) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q == 0) {
+    w.cnt[0] = paths;
+    w.cnt[1] = w.cnt[2] = w.cnt[3] = w.cnt[4] = 0;
+  }
+  if (q >= paths) return;
+  const uint32_t npix = static_cast<uint32_t>(a.width) * static_cast<uint32_t>(a.height);
+  const uint32_t pix = q % npix;
+  const int s = s0 + static_cast<int>(q / npix);
+  Rng g{path_key(a.seed, pix, static_cast<unsigned long long>(s)), 0ull};
+  float jx = 0.5f, jy = 0.5f;
+  if (a.ns_aa > 1) {
+    jx = g.next();
+    jy = g.next();
+  }
+  const int px = static_cast<int>(pix % static_cast<uint32_t>(a.width));
+  const int py = static_cast<int>(pix / static_cast<uint32_t>(a.width));
+  const float xn = (px + jx) / a.width, yn = (py + jy) / a.height;
+  const V3 cx = ld3(cam.c2w), cy = ld3(cam.c2w + 3), cz = ld3(cam.c2w + 6);
+  const V3 dir = unit(cx * ((xn - 0.5f) * cam.htan) + cy * ((yn - 0.5f) * cam.vtan) - cz);
+  w.o[q] = make_float4(cam.pos[0], cam.pos[1], cam.pos[2], cam.nclip);
+  w.d[q] = make_float4(dir.x, dir.y, dir.z, cam.fclip);
+  w.beta[q] = make_float4(1.f, 1.f, 1.f, 1.f);
+  w.L[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  w.st[q] = make_uint2(static_cast<uint32_t>(a.max_depth), static_cast<uint32_t>(g.k));
+  w.qa[q] = q;
+}
+
+// Clears the next queue's length, the shadow slot count and the fetch counters.
+__global__ void k_wf_reset(uint32_t* cnt, int next) {
+  cnt[next] = 0;
+  cnt[2] = cnt[3] = cnt[4] = 0;
+}
+
+// One bounce of trace_ray (pathtracer.cpp:553-582) at the closest hit of every queued
+// path: emission, the light samples of estimate_direct_lighting (:483-524) as shadow ray
+// slots (their contribution, throughput included, added by k_wf_resolve when the light is
+// visible), then estimate_indirect_lighting's BSDF sample and roulette (:526-551): the
+// continuing paths join queue_out. Random numbers are drawn in the reference's order.
+// Every lane of a warp runs the loops to the same trip counts so that the appends meet.
+__global__ void __launch_bounds__(128) k_wf_shade(Scene sc, WfArgs w, RArgs a, int s0,
+                                                  const uint32_t* __restrict__ queue,
+                                                  const uint32_t* __restrict__ count, uint32_t* queue_out,
+                                                  uint32_t* count_out) {
+  const uint32_t total = *count;
+  const uint32_t stride = gridDim.x * blockDim.x;  // a multiple of 32: each warp keeps one base
+  const uint32_t S = static_cast<uint32_t>(w.slots);
+  const uint32_t npix = static_cast<uint32_t>(a.width) * static_cast<uint32_t>(a.height);
+  for (uint32_t wbase = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; wbase < total; wbase += stride) {
+    const uint32_t idx = wbase + (threadIdx.x & 31u);
+    const bool live = idx < total;
+    const uint32_t q = live ? queue[idx] : 0u;
+    float4 h = live ? w.hit[q] : make_float4(__int_as_float(-1), 0.f, 0.f, 0.f);
+    const int ti = __float_as_int(h.x);
+    const bool hit = live && ti >= 0;
+    // shading state (only meaningful where hit)
+    RMat m{};
+    V3 n = mk(0.f, 0.f, 1.f), P = mk(0.f, 0.f, 0.f), rd = mk(0.f, 0.f, 1.f), beta = mk(0.f, 0.f, 0.f);
+    V3 L = mk(0.f, 0.f, 0.f);
+    bool includeLe = false;
+    uint2 st = make_uint2(0u, 0u);
+    if (hit) {
+      const RTri tr = sc.tri[ti];
+      m = sc.mats[__float_as_int(tr.p1.w)];
+      const RNrm nn = sc.nrm[ti];
+      const float u = h.z, v = h.w, ww = 1.f - u - v;
+      n = ww * v3(nn.n1) + u * v3(nn.n2) + v * v3(nn.n3);
+      const float4 o = w.o[q], d = w.d[q];
+      rd = mk(d.x, d.y, d.z);
+      P = mk(o.x, o.y, o.z) + rd * h.y;
+      const float4 b = w.beta[q], l = w.L[q];
+      beta = mk(b.x, b.y, b.z);
+      includeLe = b.w != 0.f;
+      L = mk(l.x, l.y, l.z);
+      st = w.st[q];
+      if (includeLe && m.kind == kMatEmission) L = L + mulv(beta, ld3(m.c1));
+    }
+    Rng g{hit ? path_key(a.seed, q % npix, static_cast<unsigned long long>(s0) + q / npix) : 0ull, st.y};
+    const Frame f = coord_space(n);
+    const bool direct = hit && !mat_delta(m.kind);
+    const V3 fval = m.kind == kMatDiffuse ? ld3(m.c1) * (1.f / kPi) : mk(0.f, 0.f, 0.f);
+    uint32_t j = 0;
+    for (int li = 0; li < a.n_light; ++li) {
+      const RLight& l = sc.lights[li];
+      const int ns = (l.kind == kLightDirectional || l.kind == kLightPoint) ? 1 : a.ns_area;
+      for (int i = 0; i < ns; ++i, ++j) {
+        bool want = false;
+        float4 dir4 = make_float4(0.f, 0.f, 0.f, 0.f), con = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (direct) {
+          V3 wi;
+          float dist, pdf;
+          const V3 Ls = sample_L(l, P, &wi, &dist, &pdf, g);
+          const float cz_in = dot(f.z, wi);
+          if (cz_in >= 0.f) {
+            const V3 c = mulv(beta, mulv(Ls, fval) * (fabsf(cz_in) / pdf));
+            con = make_float4(c.x / ns, c.y / ns, c.z / ns, 0.f);
+            dir4 = make_float4(wi.x, wi.y, wi.z, dist);
+            want = true;
+          }
+        }
+        if (hit) {
+          w.scon[static_cast<size_t>(q) * S + j] = con;
+          if (want) w.sdir[static_cast<size_t>(q) * S + j] = dir4;
+        }
+        const uint32_t at = warp_append(&w.cnt[2], want);
+        if (want) w.sq[at] = q * S + j;
+      }
+    }
+    if (hit) {
+      for (uint32_t k = j; k < S; ++k) w.scon[static_cast<size_t>(q) * S + k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    bool cont = false;
+    if (hit) {
+      w.L[q] = make_float4(L.x, L.y, L.z, 0.f);
+      w.o[q] = make_float4(P.x, P.y, P.z, a.ray_eps);  // the shadow rays' origin, and the next ray's
+      uint32_t depth = st.x;
       if (depth > 0) {
-        // estimate_indirect_lighting (pathtracer.cpp:526-551)
-        const V3 wo = f.to_local(mk(-r.d.x, -r.d.y, -r.d.z));
+        const V3 wo = f.to_local(mk(-rd.x, -rd.y, -rd.z));
         V3 wi;
         float pdf;
         const V3 fs = sample_f(m, wo, &wi, &pdf, g);
         const float p_cont = fminf(illum(fs) * 15.f, 1.f);
         if (g.next() < p_cont) {
           beta = mulv(beta, fs) * (fabsf(wi.z) / p_cont / pdf);
-          includeLe = mat_delta(m.kind);
-          r = make_ray(hit, f.to_world(wi), a.ray_eps, FLT_MAX);
+          const V3 nd = f.to_world(wi);
+          w.d[q] = make_float4(nd.x, nd.y, nd.z, FLT_MAX);
+          w.beta[q] = make_float4(beta.x, beta.y, beta.z, mat_delta(m.kind) ? 1.f : 0.f);
           --depth;
-          done = false;
+          cont = true;
         }
       }
+      w.st[q] = make_uint2(depth, static_cast<uint32_t>(g.k));
     }
-    if (done) {
-      float* o = rad + 3 * static_cast<size_t>(q);
-      o[0] = L.x;
-      o[1] = L.y;
-      o[2] = L.z;
-      q = kNoPath;
-    }
+    const uint32_t at = warp_append(count_out, cont);
+    if (cont) queue_out[at] = q;
   }
 }
 
-// Sums a batch of nb samples per pixel into acc in sample order (the reference adds
-// trace_ray's results in sample order, pathtracer.cpp:597-602); the last batch divides
-// by ns_aa.
-__global__ void k_accumulate(const float* __restrict__ rad, uint32_t npix, int nb, int first, int last, int ns_aa,
+// Adds each shaded path's visible light samples, in slot order (light by light, sample by
+// sample, as estimate_direct_lighting sums them).
+__global__ void k_wf_resolve(WfArgs w, const uint32_t* __restrict__ queue, const uint32_t* __restrict__ count) {
+  const uint32_t total = *count;
+  const uint32_t S = static_cast<uint32_t>(w.slots);
+  for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    const uint32_t q = queue[idx];
+    if (__float_as_int(w.hit[q].x) < 0) continue;
+    const float4 l = w.L[q];
+    V3 L = mk(l.x, l.y, l.z);
+    for (uint32_t j = 0; j < S; ++j) {
+      const float4 c = w.scon[static_cast<size_t>(q) * S + j];
+      if (c.w > 0.5f) L = L + mk(c.x, c.y, c.z);
+    }
+    w.L[q] = make_float4(L.x, L.y, L.z, 0.f);
+  }
+}
+
+// Sums a batch of nb samples per pixel (path radiance rad[s * npix + pixel]) into acc in
+// sample order (the reference adds trace_ray's results in sample order,
+// pathtracer.cpp:597-602); the last batch divides by ns_aa.
+__global__ void k_accumulate(const float4* __restrict__ rad, uint32_t npix, int nb, int first, int last, int ns_aa,
                              float* __restrict__ acc) {
   const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= npix) return;
   float* o = acc + 3 * static_cast<size_t>(pix);
   V3 v = first ? mk(0.f, 0.f, 0.f) : mk(o[0], o[1], o[2]);
   for (int s = 0; s < nb; ++s) {
-    const float* x = rad + 3 * (static_cast<size_t>(s) * npix + pix);
-    v = v + mk(x[0], x[1], x[2]);
+    const float4 x = rad[static_cast<size_t>(s) * npix + pix];
+    v = v + mk(x.x, x.y, x.z);
   }
   if (last) {
     const float ns = static_cast<float>(ns_aa);
@@ -783,37 +922,58 @@ cudaError_t launch_bvh_build(const RTri* tri, uint32_t n, const BvhScratch& w, B
   return cudaGetLastError();
 }
 
-uint32_t render_batch_samples(int width, int height, int ns_aa, uint32_t budget_mib) {
+int render_slots(const RLight* lights, int n_light, int ns_area) {
+  int S = 0;
+  for (int l = 0; l < n_light; ++l)
+    S += (lights[l].kind == kLightDirectional || lights[l].kind == kLightPoint) ? 1 : ns_area;
+  return S;
+}
+
+size_t render_path_bytes(int slots) {
+  return 5 * sizeof(float4) + sizeof(uint2) + 2 * sizeof(uint32_t) +
+         static_cast<size_t>(slots) * (2 * sizeof(float4) + sizeof(uint32_t));
+}
+
+uint32_t render_batch_samples(int width, int height, int ns_aa, int slots, uint32_t budget_mib) {
   const size_t px = static_cast<size_t>(width) * height;
-  const size_t budget = static_cast<size_t>(budget_mib ? budget_mib : 256) << 20;  // path radiance of one batch
-  const size_t per = std::max<size_t>(1, budget / (12 * std::max<size_t>(px, 1)));
+  const size_t budget = static_cast<size_t>(budget_mib ? budget_mib : 1024) << 20;
+  const size_t per = std::max<size_t>(1, budget / (render_path_bytes(slots) * std::max<size_t>(px, 1)));
   return static_cast<uint32_t>(std::min<size_t>(per, static_cast<size_t>(ns_aa)));
 }
 
 cudaError_t launch_render(const RTri* tri, const RNrm* nrm, uint32_t n_scene, uint32_t n_surf,
                           const BvhNode* scene_nodes, const uint32_t* scene_leaf, const BvhNode* surf_nodes,
                           const uint32_t* surf_leaf, const RMat* mats, const RLight* lights, const RCam& cam,
-                          const RArgs& a, float* path_rad, unsigned* counter, float* hdr, unsigned* err,
-                          cudaStream_t s) {
+                          const RArgs& a, const WfBuffers& wb, float* hdr, unsigned* err, cudaStream_t s) {
   const size_t px = static_cast<size_t>(a.width) * a.height;
   if (px == 0) return cudaSuccess;
   const Scene sc{tri, nrm, mats, lights, n_scene, n_surf, scene_nodes, scene_leaf, surf_nodes, surf_leaf};
-  int dev = 0, sms = 0, per_sm = 0;
+  int dev = 0, sms = 0, per_trace = 0, per_shade = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_paths, 128, 0);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_trace, k_wf_trace<false>, 128, 0);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_shade, k_wf_shade, 128, 0);
   if (e != cudaSuccess) return e;
+  const unsigned g_trace = static_cast<unsigned>(std::max(1, sms * std::max(per_trace, 1)));
+  const unsigned g_shade = static_cast<unsigned>(std::max(1, sms * std::max(per_shade, 1)));
+  const unsigned g_res = static_cast<unsigned>(std::max(1, sms * 8));
   const uint32_t nb = static_cast<uint32_t>(std::max(a.batch, 1));
   for (int s0 = 0; s0 < a.ns_aa; s0 += static_cast<int>(nb)) {
     const int cnt = std::min(static_cast<int>(nb), a.ns_aa - s0);
-    const size_t total = px * static_cast<size_t>(cnt);
-    e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
-    if (e != cudaSuccess) return e;
-    const unsigned grid = static_cast<unsigned>(
-        std::max<size_t>(1, std::min<size_t>(static_cast<size_t>(sms) * std::max(per_sm, 1), (total + 127) / 128)));
-    k_render_paths<<<grid, 128, 0, s>>>(sc, cam, a, s0, static_cast<uint32_t>(total), path_rad, counter, err);
-    k_accumulate<<<blocks(px, 256), 256, 0, s>>>(path_rad, static_cast<uint32_t>(px), cnt, s0 == 0,
-                                                 s0 + cnt >= a.ns_aa, a.ns_aa, hdr);
+    const uint32_t paths = static_cast<uint32_t>(px * static_cast<size_t>(cnt));
+    k_wf_camera<<<blocks(paths, 128), 128, 0, s>>>(wb, cam, a, s0, paths);
+    for (int level = 0; level <= a.max_depth; ++level) {
+      const int cur = level & 1;
+      const uint32_t* qin = cur ? wb.qb : wb.qa;
+      uint32_t* qout = cur ? wb.qa : wb.qb;
+      k_wf_reset<<<1, 1, 0, s>>>(wb.cnt, 1 - cur);
+      k_wf_trace<false><<<g_trace, 128, 0, s>>>(sc, wb, qin, wb.cnt + cur, wb.cnt + 3, a.ray_eps, err);
+      k_wf_shade<<<g_shade, 128, 0, s>>>(sc, wb, a, s0, qin, wb.cnt + cur, qout, wb.cnt + 1 - cur);
+      k_wf_trace<true><<<g_trace, 128, 0, s>>>(sc, wb, wb.sq, wb.cnt + 2, wb.cnt + 4, a.ray_eps, err);
+      k_wf_resolve<<<g_res, 256, 0, s>>>(wb, qin, wb.cnt + cur);
+    }
+    k_accumulate<<<blocks(px, 256), 256, 0, s>>>(wb.L, static_cast<uint32_t>(px), cnt, s0 == 0, s0 + cnt >= a.ns_aa,
+                                                 a.ns_aa, hdr);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

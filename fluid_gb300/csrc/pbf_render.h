@@ -86,20 +86,33 @@ struct RenderState {
 cudaError_t launch_surface_to_tris(const float* xyz, const float* nrm, uint32_t m, int material, RTri* tri,
                                    RNrm* nn, cudaStream_t s);
 cudaError_t launch_bvh_build(const RTri* tri, uint32_t n, const BvhScratch& w, BvhNode* nodes, cudaStream_t s);
-// Samples per pixel traced in one batch: the batch's path radiance (npix * batch * 3
-// floats, path_rad) stays within budget_mib MiB (0: 256).
-uint32_t render_batch_samples(int width, int height, int ns_aa, uint32_t budget_mib);
+// Path state of one batch (wavefront), device arrays: per path o (next ray origin, w
+// tmin), d (direction, w tmax), beta (throughput, w 1 when the next hit adds emission), L
+// (radiance), hit (x triangle as int bits or -1, y t, z u, w v), st (x depth left, y draws
+// used), queues qa / qb; per path and bounce `slots` shadow-ray slots sdir (direction, w
+// distance) and scon (contribution, w 1 when visible) with their queue sq; cnt[8] counters.
+struct WfBuffers {
+  float4 *o, *d, *beta, *L, *hit, *sdir, *scon;
+  uint2* st;
+  uint32_t *qa, *qb, *sq, *cnt;
+  int slots;
+};
+// Shadow-ray slots per path and bounce: one per delta light, ns_area per other light.
+int render_slots(const RLight* lights, int n_light, int ns_area);
+size_t render_path_bytes(int slots);
+// Samples per pixel traced in one batch, the batch's path state within budget_mib MiB
+// (0: 1024).
+uint32_t render_batch_samples(int width, int height, int ns_aa, int slots, uint32_t budget_mib);
 // hdr: W * H * 3 floats, row y = 0 first (the bottom row, as the reference's sample buffer).
-// *_leaf: a build's vals (sorted position -> triangle of its range); counter: one word;
-// err bit 0: a traversal stack overflowed (deeper than kBvhStack levels).
 // tri / nrm: the scene's n_scene triangles, then the surface's n_surf. scene_nodes null:
-// the scene's triangles are tested one by one (at most kBruteScene of them).
+// the scene's triangles are tested one by one (at most kBruteScene of them). *_leaf: a
+// build's vals (sorted position -> triangle of its range); err bit 0: a traversal stack
+// overflowed (deeper than kBvhStack levels).
 constexpr uint32_t kBruteScene = 32;
 cudaError_t launch_render(const RTri* tri, const RNrm* nrm, uint32_t n_scene, uint32_t n_surf,
                           const BvhNode* scene_nodes, const uint32_t* scene_leaf, const BvhNode* surf_nodes,
                           const uint32_t* surf_leaf, const RMat* mats, const RLight* lights, const RCam& cam,
-                          const RArgs& a, float* path_rad, unsigned* counter, float* hdr, unsigned* err,
-                          cudaStream_t s);
+                          const RArgs& a, const WfBuffers& wb, float* hdr, unsigned* err, cudaStream_t s);
 // rgba: W * H * 4 bytes, rows flipped (top first) as PathTracer::save_image writes them.
 cudaError_t launch_tonemap(const float* hdr, int width, int height, uint8_t* rgba, cudaStream_t s);
 

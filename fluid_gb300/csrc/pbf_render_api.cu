@@ -55,9 +55,10 @@ struct Frame {
   Tree scene, surf;
   pbf::RMat* mats;
   pbf::RLight* lights;
-  float *sxyz, *snrm, *hdr, *path_rad;
+  float *sxyz, *snrm, *hdr;
   uint8_t* rgba;
-  unsigned *err, *counter;
+  unsigned* err;
+  pbf::WfBuffers wf;
 };
 
 Tree carve_tree(Carve& c, size_t n) {
@@ -80,8 +81,9 @@ Tree carve_tree(Carve& c, size_t n) {
 }
 
 // n_scene_tree: the scene's triangle count when it gets a hierarchy, else 0.
-Frame carve(char* base, size_t n, size_t n_scene_tree, size_t m, int n_mat, int n_light, size_t px, size_t batch,
-            size_t* bytes) {
+// paths: the path state of one batch (px * samples per batch), slots per path.
+Frame carve(char* base, size_t n, size_t n_scene_tree, size_t m, int n_mat, int n_light, size_t px, size_t paths,
+            int slots, size_t* bytes) {
   Carve c{base};
   Frame f;
   f.tri = c.take<pbf::RTri>(n);
@@ -94,9 +96,21 @@ Frame carve(char* base, size_t n, size_t n_scene_tree, size_t m, int n_mat, int 
   f.snrm = c.take<float>(9 * m);
   f.hdr = c.take<float>(3 * px);
   f.rgba = c.take<uint8_t>(4 * px);
-  f.path_rad = c.take<float>(3 * px * batch);
   f.err = c.take<unsigned>(1);
-  f.counter = c.take<unsigned>(1);
+  pbf::WfBuffers& w = f.wf;
+  w.o = c.take<float4>(paths);
+  w.d = c.take<float4>(paths);
+  w.beta = c.take<float4>(paths);
+  w.L = c.take<float4>(paths);
+  w.hit = c.take<float4>(paths);
+  w.st = c.take<uint2>(paths);
+  w.qa = c.take<uint32_t>(paths);
+  w.qb = c.take<uint32_t>(paths);
+  w.sdir = c.take<float4>(paths * slots);
+  w.scon = c.take<float4>(paths * slots);
+  w.sq = c.take<uint32_t>(paths * slots);
+  w.cnt = c.take<uint32_t>(8);
+  w.slots = slots;
   *bytes = c.off + 256;
   return f;
 }
@@ -309,11 +323,14 @@ pbf_status pbf_render(pbf_handle* hh, const pbf_camera* cam, const pbf_render_pa
   const size_t n = static_cast<size_t>(R.n_scene) + m;
   if (n >= pbf::kLeafBit) return h->fail(PBF_ERR_INVALID, "too many triangles");
   const size_t px = static_cast<size_t>(p->width) * p->height;
+  const int slots = pbf::render_slots(R.lights_host, R.n_light, static_cast<int>(p->ns_area_light));
   const size_t batch = pbf::render_batch_samples(static_cast<int>(p->width), static_cast<int>(p->height),
-                                                 static_cast<int>(p->ns_aa), p->path_buffer_mib);
+                                                 static_cast<int>(p->ns_aa), slots, p->path_buffer_mib);
+  if (px * batch >= (size_t(1) << 32) / std::max(slots, 1))
+    return h->fail(PBF_ERR_INVALID, "frame too large: more than 2^32 shadow-ray slots in one batch");
   const size_t scene_tree = R.n_scene > pbf::kBruteScene ? R.n_scene : 0;
   size_t need = 0;
-  carve(nullptr, n, scene_tree, m, R.n_mat, R.n_light, px, batch, &need);
+  carve(nullptr, n, scene_tree, m, R.n_mat, R.n_light, px, px * batch, slots, &need);
   if (need > R.buf_bytes) {
     if (R.buf) cudaFree(R.buf);
     R.buf = nullptr;
@@ -323,7 +340,8 @@ pbf_status pbf_render(pbf_handle* hh, const pbf_camera* cam, const pbf_render_pa
     R.buf_bytes = need;
   }
   size_t used = 0;
-  const Frame f = carve(static_cast<char*>(R.buf), n, scene_tree, m, R.n_mat, R.n_light, px, batch, &used);
+  const Frame f = carve(static_cast<char*>(R.buf), n, scene_tree, m, R.n_mat, R.n_light, px, px * batch, slots,
+                        &used);
   std::vector<pbf::RMat> mats(R.mats_host, R.mats_host + R.n_mat);
   pbf::RMat fluid{};
   fluid.kind = pbf::kMatDiffuse;
@@ -377,8 +395,8 @@ pbf_status pbf_render(pbf_handle* hh, const pbf_camera* cam, const pbf_render_pa
   a.batch = static_cast<int>(batch);
   if (st == PBF_OK)
     st = h->cuda(pbf::launch_render(f.tri, f.nrm, R.n_scene, m, scene_tree ? f.scene.nodes : nullptr,
-                                    f.scene.w.vals, f.surf.nodes, f.surf.w.vals, f.mats, f.lights, rc, a, f.path_rad,
-                                    f.counter, f.hdr, f.err, h->stream),
+                                    f.scene.w.vals, f.surf.nodes, f.surf.w.vals, f.mats, f.lights, rc, a, f.wf, f.hdr,
+                                    f.err, h->stream),
                  "render");
   if (st == PBF_OK && rgba)
     st = h->cuda(pbf::launch_tonemap(f.hdr, a.width, a.height, f.rgba, h->stream), "tonemap");
