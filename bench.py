@@ -17,7 +17,7 @@ full PBF time step of every particle (Particles::timeStep, particles.cpp:250-297
   CUDA events between phases (``phases_pass``).
 * ``e2e``: the same metric through the C ABI with host buffers: per step
   pbf_set_state (H2D of positions and velocities from pinned memory), pbf_step, and
-  pbf_get_positions + pbf_get_velocities (D2H), wall-clocked.
+  pbf_get_state (D2H of positions and velocities), wall-clocked.
 * ``roofline``: the dominant kernel's algorithmic bytes per launch over its average
   event-timed launch duration in the phase pass, against the measured HBM copy
   bandwidth.
@@ -652,8 +652,7 @@ def bench_ours(args, scene, world, rank, local):
             t0 = time.perf_counter()
             rc = L.pbf_set_state(sim._h, xp, vp)
             rc |= L.pbf_step(sim._h, dt, 1)
-            rc |= L.pbf_get_positions(sim._h, xp)
-            rc |= L.pbf_get_velocities(sim._h, vp)
+            rc |= L.pbf_get_state(sim._h, xp, vp, None)
             t1 = time.perf_counter()
             if rc:
                 raise RuntimeError(L.pbf_last_error(sim._h).decode())
@@ -662,7 +661,7 @@ def bench_ours(args, scene, world, rank, local):
         tot = reduce_max(tot, world)
         e2e = {"value": world * n * e2e_steps / tot, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 12,
                "d2h_bytes_per_step": 2 * n * 12, "ms_per_step": tot / e2e_steps * 1e3,
-               "path": "pbf_set_state + pbf_step + pbf_get_positions + pbf_get_velocities, pinned host buffers"}
+               "path": "pbf_set_state + pbf_step + pbf_get_state (positions and velocities), pinned host buffers"}
     sim.close()
 
     batched = bench_batched(args, world, rank, local) if not args.no_batched else None

@@ -631,29 +631,28 @@ pbf_status pbf_adjoint_step_device(pbf_handle* hh, double dt, const float* xyz, 
   return h->join_to(static_cast<cudaStream_t>(stream));
 }
 
+// One reordering kernel into the staging arrays, the requested copies, one wait.
 static pbf_status download(Handle* h, float* xyz, float* vel, float* rho) {
   pbf::DeviceGuard g(h->device);
   const size_t n = h->b.n;
-  if (n == 0) return PBF_OK;
-  pbf_status st = PBF_OK;
-  if (xyz) {
-    st = h->cuda(pbf::launch_download(h->b, h->cur, h->b.io, nullptr, nullptr, h->stream), "download");
-    if (st == PBF_OK)
-      st = h->cuda(cudaMemcpyAsync(xyz, h->b.io, 3 * sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
-  }
-  if (st == PBF_OK && vel) {
-    st = h->cuda(pbf::launch_download(h->b, h->cur, nullptr, h->b.io2, nullptr, h->stream), "download");
-    if (st == PBF_OK)
-      st = h->cuda(cudaMemcpyAsync(vel, h->b.io2, 3 * sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
-  }
-  if (st == PBF_OK && rho) {
-    float* tmp = reinterpret_cast<float*>(h->b.disp[0]);  // scratch between steps
-    st = h->cuda(pbf::launch_download(h->b, h->cur, nullptr, nullptr, tmp, h->stream), "download");
-    if (st == PBF_OK)
-      st = h->cuda(cudaMemcpyAsync(rho, tmp, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
-  }
+  if (n == 0 || (!xyz && !vel && !rho)) return PBF_OK;
+  float* tmp = reinterpret_cast<float*>(h->b.disp[0]);  // scratch between steps
+  pbf_status st = h->cuda(pbf::launch_download(h->b, h->cur, xyz ? h->b.io : nullptr, vel ? h->b.io2 : nullptr,
+                                               rho ? tmp : nullptr, h->stream),
+                          "download");
+  if (st == PBF_OK && xyz)
+    st = h->cuda(cudaMemcpyAsync(xyz, h->b.io, 3 * sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
+  if (st == PBF_OK && vel)
+    st = h->cuda(cudaMemcpyAsync(vel, h->b.io2, 3 * sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
+  if (st == PBF_OK && rho)
+    st = h->cuda(cudaMemcpyAsync(rho, tmp, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream), "D2H");
   if (st == PBF_OK) st = h->cuda(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
   return st;
+}
+
+pbf_status pbf_get_state(pbf_handle* hh, float* xyz, float* vel, float* rho) {
+  if (!hh) return PBF_ERR_INVALID;
+  return download(reinterpret_cast<Handle*>(hh), xyz, vel, rho);
 }
 
 pbf_status pbf_get_positions(pbf_handle* hh, float* xyz) {

@@ -247,9 +247,7 @@ class Particles {
   void pull(bool with_density) {
     const size_t n = ps.size();
     std::vector<float> x(3 * n), v(3 * n), rho(with_density ? n : 0);
-    check(pbf_get_positions(h_, x.data()));
-    check(pbf_get_velocities(h_, v.data()));
-    if (with_density) check(pbf_get_densities(h_, rho.data()));
+    check(pbf_get_state(h_, x.data(), v.data(), with_density ? rho.data() : nullptr));
     for (size_t i = 0; i < n; ++i) {
       ParticleT* p = ps[i];
       p->position_ = V(x[3 * i], x[3 * i + 1], x[3 * i + 2]);

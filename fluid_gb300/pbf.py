@@ -133,6 +133,7 @@ def _declare(L):
         "pbf_surface": (st, [P, ctypes.c_double, ctypes.c_double, P, P, P, P, sz, P]),
         "pbf_mc_table": (None, [P, P, P]),
         "pbf_set_collider_mesh": (st, [P, sz, P]),
+        "pbf_get_state": (st, [P, P, P, P]),
         "pbf_render_params_default": (None, [P]),
         "pbf_camera_frame": (st, [P, ctypes.c_uint32, ctypes.c_uint32, P]),
         "pbf_render_set_scene": (st, [P, P, P, P, sz, P, sz, P, sz]),

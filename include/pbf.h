@@ -143,6 +143,9 @@ PBF_API void* pbf_stream(pbf_handle* h);
 PBF_API pbf_status pbf_get_positions(pbf_handle* h, float* xyz);
 PBF_API pbf_status pbf_get_velocities(pbf_handle* h, float* vel);
 PBF_API pbf_status pbf_get_densities(pbf_handle* h, float* rho);
+/* The three at once (any may be NULL): one reordering pass and one wait, for a caller
+ * that mirrors the whole state after every step (the facade's timeStep). */
+PBF_API pbf_status pbf_get_state(pbf_handle* h, float* xyz, float* vel, float* rho);
 /* Replace positions and velocities (host). */
 PBF_API pbf_status pbf_set_state(pbf_handle* h, const float* xyz, const float* vel);
 

@@ -368,3 +368,24 @@ def test_collider_mesh_arguments(pbf):
             sim.adjoint_step_device(sc.params.dt, None, None, None, None, x.data_ptr(), x.data_ptr(), r.data_ptr())
         sim.set_collider_mesh(None)
         sim.time_step(sc.params.dt, 1)
+
+
+def test_get_state_matches_the_single_getters(pbf):
+    """pbf_get_state (one reordering pass, one wait) returns what pbf_get_positions,
+    pbf_get_velocities and pbf_get_densities return one by one; NULL arrays are skipped."""
+    import ctypes
+
+    sc = scenes.block4096(3)
+    with pbf.Simulator(_f32(sc.pos), _f32(sc.vel), sc.params) as sim:
+        sim.time_step(sc.params.dt, 2)
+        x, v, rho = sim.positions(), sim.velocities(), sim.densities()
+        n = len(x)
+        xs, vs, rs = (np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32), np.zeros(n, np.float32))
+        L = pbf.lib()
+        assert L.pbf_get_state(sim._h, xs.ctypes.data_as(pbf.P), vs.ctypes.data_as(pbf.P),
+                               rs.ctypes.data_as(pbf.P)) == 0
+        assert np.array_equal(xs, x) and np.array_equal(vs, v) and np.array_equal(rs, rho)
+        v2 = np.zeros((n, 3), np.float32)
+        assert L.pbf_get_state(sim._h, None, v2.ctypes.data_as(pbf.P), None) == 0
+        assert np.array_equal(v2, v)
+        assert L.pbf_get_state(sim._h, None, None, None) == 0
