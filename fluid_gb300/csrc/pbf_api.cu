@@ -821,12 +821,26 @@ pbf_status Handle::surface_count(double isolevel, double step, const double* lo,
   const size_t nc = static_cast<size_t>(cubes);
   const size_t corners = static_cast<size_t>(g->nc[0] + 1) * (g->nc[1] + 1) * (g->nc[2] + 1);
   const size_t tiles = exclusive_scan_tiles(static_cast<uint32_t>(nc));
-  st = ensure_scratch(4 * (corners + nc + (nc + 1) + tiles) + 256);
+  const size_t naxis = static_cast<size_t>(g->nc[0]) + g->nc[1] + g->nc[2] + 3;
+  st = ensure_scratch(4 * (corners + nc + (nc + 1) + tiles + naxis) + 256);
   if (st != PBF_OK) return st;
   float* field = static_cast<float*>(scratch);
   uint32_t* cnt = reinterpret_cast<uint32_t*>(field + corners);
   uint32_t* first = cnt + nc;
   uint32_t* tile = first + nc + 1;
+  float* axis = reinterpret_cast<float*>(tile + tiles);
+  std::vector<float> ax;
+  ax.reserve(naxis);
+  for (int a = 0; a < 3; ++a)
+    for (int i = 0; i <= g->nc[a]; ++i) {
+      // i * step and the sum rounded separately (no fused multiply-add), as the reference's
+      // x1 = xmin + ix * fStepSize
+      const volatile double t = i * g->step;
+      ax.push_back(static_cast<float>(std::min(g->lo[a] + t, g->hi[a])));
+    }
+  st = cuda(cudaMemcpyAsync(axis, ax.data(), sizeof(float) * naxis, cudaMemcpyHostToDevice, stream), "H2D axis");
+  if (st != PBF_OK) return st;
+  g->axis = axis;
   st = cuda(launch_surface_count(b, dp, cur, *g, static_cast<float>(isolevel), surf_table_dev, field, cnt, first,
                                  tile, stream),
             "surface count");

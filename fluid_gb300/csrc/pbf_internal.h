@@ -139,6 +139,9 @@ struct SurfTable {
 struct SurfGrid {
   double lo[3], hi[3], step;
   int nc[3];
+  // device: the corner coordinates per axis, float(min(lo + i step, hi)) computed in FP64
+  // on the host (x: nc[0] + 1 values, then y, then z), so no kernel needs FP64
+  const float* axis = nullptr;
 };
 void build_table(SurfTable* t);
 const SurfTable& surf_table();

@@ -153,12 +153,10 @@ __device__ __forceinline__ int corner_z(int k) { return k >> 2; }
 __device__ __forceinline__ int edge_a(int e) { return e < 8 ? e : e - 8; }
 __device__ __forceinline__ int edge_b(int e) { return e < 8 ? ((e & 4) | ((e + 1) & 3)) : e - 4; }
 
+// x1 = min(lo + i step, hi) per axis, computed in FP64 as the reference computes it (on
+// the host, SurfGrid::axis)
 __device__ __forceinline__ float3 corner_point(const SurfGrid& g, int i, int j, int k) {
-  // x1 = min(lo + i step, hi) per axis, in FP64 as the reference computes it
-  const double x = fmin(g.lo[0] + i * g.step, g.hi[0]);
-  const double y = fmin(g.lo[1] + j * g.step, g.hi[1]);
-  const double z = fmin(g.lo[2] + k * g.step, g.hi[2]);
-  return make_float3(static_cast<float>(x), static_cast<float>(y), static_cast<float>(z));
+  return make_float3(__ldg(&g.axis[i]), __ldg(&g.axis[g.nc[0] + 1 + j]), __ldg(&g.axis[g.nc[0] + g.nc[1] + 2 + k]));
 }
 
 __global__ void k_surf_density(const float4* __restrict__ pos, const uint32_t* __restrict__ cell_start,
