@@ -162,6 +162,9 @@ void Handle::free_all() {
   free_tape();
   if (surf_table_dev) cudaFree(surf_table_dev);
   surf_table_dev = nullptr;
+  if (surf_hash) cudaFree(surf_hash);
+  surf_hash = nullptr;
+  surf_hash_bytes = 0;
   if (mesh_dev) cudaFree(mesh_dev);
   mesh_dev = nullptr;
   render.release();
@@ -857,8 +860,25 @@ pbf_status Handle::surface_emit(const SurfGrid& g, double isolevel, float* xyz, 
   const size_t corners = static_cast<size_t>(g.nc[0] + 1) * (g.nc[1] + 1) * (g.nc[2] + 1);
   const float* field = static_cast<const float*>(scratch);
   const uint32_t* first = reinterpret_cast<const uint32_t*>(field + corners) + nc;
+  if (cap > (1u << 28)) return fail(PBF_ERR_INVALID, "surface too large: more than 2^28 triangles");
+  const size_t slots = surface_hash_slots(cap);
+  const size_t need = slots * (sizeof(unsigned long long) + sizeof(float4)) + 6 * sizeof(uint32_t) * cap + 512;
+  if (need > surf_hash_bytes) {
+    if (surf_hash) cudaFree(surf_hash);
+    surf_hash = nullptr;
+    surf_hash_bytes = 0;
+    pbf_status st = cuda(cudaMalloc(&surf_hash, need), "cudaMalloc(surface table)");
+    if (st != PBF_OK) return st;
+    surf_hash_bytes = need;
+  }
+  SurfHash hs;
+  hs.keys = static_cast<unsigned long long*>(surf_hash);
+  hs.nslot = reinterpret_cast<float4*>(hs.keys + slots);
+  hs.vslot = reinterpret_cast<uint32_t*>(hs.nslot + slots);
+  hs.ulist = hs.vslot + 3 * static_cast<size_t>(cap);
+  hs.ucount = hs.ulist + 3 * static_cast<size_t>(cap);
   return cuda(launch_surface_emit(b, dp, cur, g, static_cast<float>(isolevel), surf_table_dev, field, first, xyz, nrm,
-                                  cap, stream),
+                                  cap, hs, stream),
               "surface emit");
 }
 

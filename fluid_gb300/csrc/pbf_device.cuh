@@ -519,20 +519,36 @@ __device__ __forceinline__ bool spiky_s(float r2, float h, float* s) {
 
 // Particles::estimateDensityAt (particles.cpp:446-453): sum of poly6 over all particles
 // (self included for a particle's own position), gathered from the 27 cells of size
-// >= h around p in the cell order of `pos` (cell_start of that order).
+// >= h around p in the cell order of `pos` (cell_start of that order). As in the
+// neighbour build, a row of cells farther than h in y/z is skipped and the others are
+// trimmed in x to the cells that reach [x - w, x + w], w = sqrt(h^2 - d_yz^2), with a
+// margin of 1e-3 cell: only particles that add nothing are left out, so the sum (same
+// rows, same slot order) is the same.
 __device__ __forceinline__ float density_at_point(const float3 p, const float4* __restrict__ pos,
                                                   const uint32_t* __restrict__ cell_start, const SceneDesc& sc,
                                                   const DevParams& P) {
   const CellCoord cc = cell_of(p, sc, P.inv_cell);
-  const int x0 = cc.x > 0 ? cc.x - 1 : 0;
-  const int x1 = cc.x + 1 < sc.dim[0] ? cc.x + 1 : sc.dim[0] - 1;
+  const float m = 1e-3f;
+  const float reach = sqrtf(P.h2) * P.inv_cell + m;
+  const float reach2 = reach * reach;
+  const float ux = (p.x - sc.origin[0]) * P.inv_cell, uy = (p.y - sc.origin[1]) * P.inv_cell,
+              uz = (p.z - sc.origin[2]) * P.inv_cell;
   float qsum = 0.f;
   for (int r = 0; r < 9; ++r) {
     const int z = cc.z + r / 3 - 1, y = cc.y + r % 3 - 1;
     if (z < 0 || z >= sc.dim[2] || y < 0 || y >= sc.dim[1]) continue;
+    // distance in cells from p to the row's y and z extents, less the margin
+    const float dy = fmaxf(fmaxf(static_cast<float>(y) - uy, uy - static_cast<float>(y + 1)) - m, 0.f);
+    const float dz = fmaxf(fmaxf(static_cast<float>(z) - uz, uz - static_cast<float>(z + 1)) - m, 0.f);
+    const float w2 = reach2 - (dy * dy + dz * dz);
+    if (w2 < 0.f) continue;
+    const float w = sqrtf(w2);
+    const int xa = max(max(static_cast<int>(floorf(ux - w)), cc.x - 1), 0);
+    const int xb = min(min(static_cast<int>(floorf(ux + w)), cc.x + 1), sc.dim[0] - 1);
+    if (xa > xb) continue;
     const uint32_t row = sc.cell_off + static_cast<uint32_t>((z * sc.dim[1] + y) * sc.dim[0]);
-    const uint32_t e = __ldg(&cell_start[row + x1 + 1]);
-    for (uint32_t j = __ldg(&cell_start[row + x0]); j < e; ++j) {
+    const uint32_t e = __ldg(&cell_start[row + xb + 1]);
+    for (uint32_t j = __ldg(&cell_start[row + xa]); j < e; ++j) {
       const float4 xj = __ldg(&pos[j]);
       const float3 d = make_float3(xj.x - p.x, xj.y - p.y, xj.z - p.z);
       const float r2 = dot3(d, d);

@@ -59,6 +59,8 @@ struct Handle {
   double snap_time = 0;
   Tape tape;                 // recording + work arrays of the adjoint (first use)
   SurfTable* surf_table_dev = nullptr;  // marching-cubes table (first pbf_surface)
+  void* surf_hash = nullptr;            // grow-only scratch of the surface's vertex-normal table
+  size_t surf_hash_bytes = 0;
   float4* mesh_dev = nullptr;           // collider triangles (pbf_set_collider_mesh)
   RenderState render;                   // path tracer (pbf_render_set_scene, pbf_render)
   double phase_ms[kNumPhases] = {};

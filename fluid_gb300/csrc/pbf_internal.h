@@ -233,10 +233,18 @@ cudaError_t launch_density_at(const Buffers& b, const DevParams& p, int cur, siz
 cudaError_t launch_surface_count(const Buffers& b, const DevParams& p, int cur, const SurfGrid& g, float iso,
                                  const SurfTable* tab, float* field, uint32_t* count, uint32_t* first,
                                  uint32_t* tile_sums, cudaStream_t s);
+// Scratch of launch_surface_emit for cap triangles: keys and nslot hold
+// surface_hash_slots(cap) entries, vslot and ulist 3 * cap, ucount one.
+struct SurfHash {
+  unsigned long long* keys;
+  float4* nslot;
+  uint32_t *vslot, *ulist, *ucount;
+};
+uint32_t surface_hash_slots(uint32_t triangles);
 // Triangles with index < cap (cap at most the total of the counts): 9 floats of vertices
-// and 9 of vertex normals each.
+// and 9 of vertex normals each. Each vertex normal is evaluated once per grid edge.
 cudaError_t launch_surface_emit(const Buffers& b, const DevParams& p, int cur, const SurfGrid& g, float iso,
                                 const SurfTable* tab, const float* field, const uint32_t* first, float* xyz,
-                                float* nrm, uint32_t cap, cudaStream_t s);
+                                float* nrm, uint32_t cap, const SurfHash& hs, cudaStream_t s);
 
 }  // namespace pbf

@@ -203,41 +203,113 @@ __device__ __forceinline__ float3 vertex_interp(float iso, float3 p1, float3 p2,
   return make_float3(p1.x + mu * (p2.x - p1.x), p1.y + mu * (p2.y - p1.y), p1.z + mu * (p2.z - p1.z));
 }
 
-// One thread per triangle vertex: triangle t lies in the cube c with first[c] <= t <
-// first[c + 1] (binary search; empty cubes have first[c] == first[c + 1]), as the q-th of
-// its cube's triangles. Its vertex v is vertexInterp on the cube's edge in the cube's own
-// corner order, its normal getVertexNormal: normalized central differences of
-// estimateDensityAt at +-GRADIENT_EPS. A thread per cube instead would leave most lanes of
-// a warp on empty cubes while one lane evaluated up to 5 triangles' normals.
-__global__ void k_surf_emit(const float* __restrict__ field, const SurfTable* __restrict__ tab, SurfGrid g,
-                            float iso, const uint32_t* __restrict__ first, const float4* __restrict__ pos,
-                            const uint32_t* __restrict__ cell_start, const SceneDesc* __restrict__ scenes,
-                            float* __restrict__ xyz, float* __restrict__ nrm, uint32_t count, DevParams P,
-                            int64_t ncubes) {
-  const int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (tid >= 3 * static_cast<int64_t>(count)) return;
-  const uint32_t t = static_cast<uint32_t>(tid / 3);
-  const int v = static_cast<int>(tid % 3);
+// Triangle t lies in the cube c with first[c] <= t < first[c + 1] (binary search; empty
+// cubes have first[c] == first[c + 1]), as the q-th of its cube's triangles; its vertex v
+// sits on cube edge e between corners a and b (the cube's own corner order).
+struct TriVertex {
+  int ix, iy, iz, a, b;
+};
+__device__ __forceinline__ TriVertex tri_vertex(const float* __restrict__ field, const SurfTable* __restrict__ tab,
+                                                const SurfGrid& g, float iso, const uint32_t* __restrict__ first,
+                                                int64_t ncubes, uint32_t t, int v) {
   int64_t lo = 0, hi = ncubes;  // first[lo] <= t < first[hi] (first[ncubes] = total > t)
   while (hi - lo > 1) {
     const int64_t mid = (lo + hi) >> 1;
     if (first[mid] <= t) lo = mid;
     else hi = mid;
   }
-  const int64_t c = lo;
-  const int q = static_cast<int>(t - first[c]);
-  int ix, iy, iz;
-  cube_of(g, c, &ix, &iy, &iz);
+  TriVertex r;
+  cube_of(g, lo, &r.ix, &r.iy, &r.iz);
   int ci = 0;
 #pragma unroll
   for (int k = 0; k < 8; ++k)
-    if (corner_value(field, g, ix + corner_x(k), iy + corner_y(k), iz + corner_z(k)) < iso) ci |= 1 << k;
-  const int e = tab->tri[ci][3 * q + v];
-  const int a = edge_a(e), b = edge_b(e);
-  const int ia = ix + corner_x(a), ja = iy + corner_y(a), ka = iz + corner_z(a);
-  const int ib = ix + corner_x(b), jb = iy + corner_y(b), kb = iz + corner_z(b);
-  const float3 x = vertex_interp(iso, corner_point(g, ia, ja, ka), corner_point(g, ib, jb, kb),
-                                 corner_value(field, g, ia, ja, ka), corner_value(field, g, ib, jb, kb));
+    if (corner_value(field, g, r.ix + corner_x(k), r.iy + corner_y(k), r.iz + corner_z(k)) < iso) ci |= 1 << k;
+  const int e = tab->tri[ci][3 * static_cast<int>(t - first[lo]) + v];
+  r.a = edge_a(e);
+  r.b = edge_b(e);
+  return r;
+}
+
+// The grid edge of a cube edge, independent of the cube: 3 * (index of its lower corner)
+// + its axis.
+__device__ __forceinline__ unsigned long long edge_key(const SurfGrid& g, const TriVertex& r) {
+  const int i = r.ix + min(corner_x(r.a), corner_x(r.b)), j = r.iy + min(corner_y(r.a), corner_y(r.b)),
+            k = r.iz + min(corner_z(r.a), corner_z(r.b));
+  const int axis = corner_x(r.a) != corner_x(r.b) ? 0 : (corner_y(r.a) != corner_y(r.b) ? 1 : 2);
+  const unsigned long long corner =
+      (static_cast<unsigned long long>(k) * (g.nc[1] + 1) + j) * static_cast<unsigned long long>(g.nc[0] + 1) + i;
+  return 3ull * corner + static_cast<unsigned long long>(axis);
+}
+
+constexpr unsigned long long kNoKey = ~0ull;
+
+__device__ __forceinline__ uint32_t key_hash(unsigned long long k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  return static_cast<uint32_t>(k);
+}
+
+// One thread per triangle vertex: the vertex's grid edge goes into an open-addressing table
+// (linear probing, compare-and-swap; the table holds at least twice the vertices, so a probe
+// ends) and the vertex keeps its slot. Vertices shared by the triangles around an edge get
+// one slot, so each normal is evaluated once; the thread that filled a slot lists it in
+// ulist (warp-aggregated count in *ucount), so that the normals are computed by a dense grid.
+__global__ void k_surf_vkeys(const float* __restrict__ field, const SurfTable* __restrict__ tab, SurfGrid g,
+                             float iso, const uint32_t* __restrict__ first, uint32_t count, int64_t ncubes,
+                             unsigned long long* keys, uint32_t cap_mask, uint32_t* __restrict__ vslot,
+                             uint32_t* __restrict__ ulist, uint32_t* ucount) {
+  const int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (tid >= 3 * static_cast<int64_t>(count)) return;
+  const TriVertex r = tri_vertex(field, tab, g, iso, first, ncubes, static_cast<uint32_t>(tid / 3),
+                                 static_cast<int>(tid % 3));
+  const unsigned long long key = edge_key(g, r);
+  uint32_t h = key_hash(key) & cap_mask;
+  bool fresh = false;
+  for (uint32_t probe = 0; probe <= cap_mask; ++probe) {
+    const unsigned long long prev = atomicCAS(&keys[h], kNoKey, key);
+    if (prev == kNoKey || prev == key) {
+      fresh = prev == kNoKey;
+      break;
+    }
+    h = (h + 1) & cap_mask;
+  }
+  vslot[tid] = h;
+  const unsigned act = __activemask();
+  const unsigned m = __ballot_sync(act, fresh);
+  if (m) {
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (static_cast<int>(threadIdx.x & 31u) == leader) base = atomicAdd(ucount, static_cast<uint32_t>(__popc(m)));
+    base = __shfl_sync(act, base, leader);
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    if (fresh) ulist[base + __popc(m & lt)] = h;
+  }
+}
+
+// One thread per filled table slot (ulist[0, *ucount)): the normal of the slot's edge
+// vertex (getVertexNormal: normalized central differences of estimateDensityAt at
+// +-GRADIENT_EPS), the vertex taken by vertexInterp from the edge's lower corner to its
+// upper corner.
+__global__ void k_surf_vnormals(const float* __restrict__ field, SurfGrid g, float iso,
+                                const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ ulist,
+                                const uint32_t* __restrict__ ucount, float4* __restrict__ nslot,
+                                const float4* __restrict__ pos, const uint32_t* __restrict__ cell_start,
+                                const SceneDesc* __restrict__ scenes, DevParams P) {
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= *ucount) return;
+  const uint32_t sidx = ulist[u];
+  const unsigned long long key = keys[sidx];
+  const int axis = static_cast<int>(key % 3ull);
+  unsigned long long c = key / 3ull;
+  const int nx = g.nc[0] + 1, ny = g.nc[1] + 1;
+  const int i = static_cast<int>(c % nx);
+  c /= nx;
+  const int j = static_cast<int>(c % ny), k = static_cast<int>(c / ny);
+  const int i2 = i + (axis == 0), j2 = j + (axis == 1), k2 = k + (axis == 2);
+  const float3 x = vertex_interp(iso, corner_point(g, i, j, k), corner_point(g, i2, j2, k2),
+                                 corner_value(field, g, i, j, k), corner_value(field, g, i2, j2, k2));
   const SceneDesc& sc = scenes[0];
   const float eps = 0.001f;  // GRADIENT_EPS, particles.cpp:16
   float3 n;
@@ -249,6 +321,27 @@ __global__ void k_surf_emit(const float* __restrict__ field, const SurfTable* __
         density_at_point(make_float3(x.x, x.y, x.z + eps), pos, cell_start, sc, P);
   const float nn = sqrtf(dot3(n, n));
   if (nn > 0.f) n = n * (1.0f / nn);
+  nslot[sidx] = make_float4(n.x, n.y, n.z, 0.f);
+}
+
+// One thread per triangle vertex: the vertex by vertexInterp on its cube's edge in the
+// cube's own corner order (as the reference computes it per cube), the normal of its
+// grid edge from the table. A thread per cube instead would leave most lanes of a warp on
+// empty cubes while one lane did up to 5 triangles.
+__global__ void k_surf_emit(const float* __restrict__ field, const SurfTable* __restrict__ tab, SurfGrid g,
+                            float iso, const uint32_t* __restrict__ first, const uint32_t* __restrict__ vslot,
+                            const float4* __restrict__ nslot, float* __restrict__ xyz, float* __restrict__ nrm,
+                            uint32_t count, int64_t ncubes) {
+  const int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (tid >= 3 * static_cast<int64_t>(count)) return;
+  const uint32_t t = static_cast<uint32_t>(tid / 3);
+  const int v = static_cast<int>(tid % 3);
+  const TriVertex r = tri_vertex(field, tab, g, iso, first, ncubes, t, v);
+  const int ia = r.ix + corner_x(r.a), ja = r.iy + corner_y(r.a), ka = r.iz + corner_z(r.a);
+  const int ib = r.ix + corner_x(r.b), jb = r.iy + corner_y(r.b), kb = r.iz + corner_z(r.b);
+  const float3 x = vertex_interp(iso, corner_point(g, ia, ja, ka), corner_point(g, ib, jb, kb),
+                                 corner_value(field, g, ia, ja, ka), corner_value(field, g, ib, jb, kb));
+  const float4 n = nslot[vslot[tid]];
   float* o = xyz + 9 * static_cast<size_t>(t) + 3 * v;
   float* m = nrm + 9 * static_cast<size_t>(t) + 3 * v;
   o[0] = x.x;
@@ -273,13 +366,28 @@ cudaError_t launch_surface_count(const Buffers& b, const DevParams& P, int cur, 
   return launch_exclusive_scan(count, first, tile_sums, static_cast<uint32_t>(cubes), s);
 }
 
+uint32_t surface_hash_slots(uint32_t triangles) {
+  uint32_t c = 1024;
+  while (c < 6ull * triangles && c < (1u << 31)) c <<= 1;
+  return c;
+}
+
 cudaError_t launch_surface_emit(const Buffers& b, const DevParams& P, int cur, const SurfGrid& g, float iso,
                                 const SurfTable* tab, const float* field, const uint32_t* first, float* xyz,
-                                float* nrm, uint32_t cap, cudaStream_t s) {
+                                float* nrm, uint32_t cap, const SurfHash& hs, cudaStream_t s) {
   const int64_t cubes = static_cast<int64_t>(g.nc[0]) * g.nc[1] * g.nc[2];
   if (cap == 0) return cudaSuccess;
-  k_surf_emit<<<blocks_for(3 * static_cast<int64_t>(cap), 128), 128, 0, s>>>(
-      field, tab, g, iso, first, b.pos[cur], b.cell_start, b.scenes, xyz, nrm, cap, P, cubes);
+  const uint32_t slots = surface_hash_slots(cap);
+  cudaError_t e = cudaMemsetAsync(hs.keys, 0xff, sizeof(unsigned long long) * slots, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(hs.ucount, 0, sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  const int64_t verts = 3 * static_cast<int64_t>(cap);
+  k_surf_vkeys<<<blocks_for(verts, 128), 128, 0, s>>>(field, tab, g, iso, first, cap, cubes, hs.keys, slots - 1,
+                                                      hs.vslot, hs.ulist, hs.ucount);
+  k_surf_vnormals<<<blocks_for(verts, 128), 128, 0, s>>>(field, g, iso, hs.keys, hs.ulist, hs.ucount, hs.nslot,
+                                                          b.pos[cur], b.cell_start, b.scenes, P);
+  k_surf_emit<<<blocks_for(verts, 128), 128, 0, s>>>(field, tab, g, iso, first, hs.vslot, hs.nslot, xyz, nrm, cap,
+                                                      cubes);
   return cudaGetLastError();
 }
 
