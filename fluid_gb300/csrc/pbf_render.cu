@@ -936,7 +936,7 @@ size_t render_path_bytes(int slots) {
 
 uint32_t render_batch_samples(int width, int height, int ns_aa, int slots, uint32_t budget_mib) {
   const size_t px = static_cast<size_t>(width) * height;
-  const size_t budget = static_cast<size_t>(budget_mib ? budget_mib : 1024) << 20;
+  const size_t budget = static_cast<size_t>(budget_mib ? budget_mib : 2048) << 20;
   const size_t per = std::max<size_t>(1, budget / (render_path_bytes(slots) * std::max<size_t>(px, 1)));
   return static_cast<uint32_t>(std::min<size_t>(per, static_cast<size_t>(ns_aa)));
 }

@@ -101,7 +101,7 @@ struct WfBuffers {
 int render_slots(const RLight* lights, int n_light, int ns_area);
 size_t render_path_bytes(int slots);
 // Samples per pixel traced in one batch, the batch's path state within budget_mib MiB
-// (0: 1024).
+// (0: 2048).
 uint32_t render_batch_samples(int width, int height, int ns_aa, int slots, uint32_t budget_mib);
 // hdr: W * H * 3 floats, row y = 0 first (the bottom row, as the reference's sample buffer).
 // tri / nrm: the scene's n_scene triangles, then the surface's n_surf. scene_nodes null:

@@ -372,7 +372,7 @@ typedef struct pbf_render_params {
   uint32_t surface_bounds; /* 1: surface grid over [surface_lo, surface_hi]; 0: the reference's
                               fixed [-1, 1] x [0, 1.5] x [-1, 1] (particles.cpp:330-349) */
   uint32_t path_buffer_mib; /* the path state of one batch of samples per pixel is kept under
-                              this many MiB (0: 1024); batches are summed in sample order */
+                              this many MiB (0: 2048); batches are summed in sample order */
   uint64_t seed;           /* random numbers: a function of (seed, pixel, sample, draw) */
   double isolevel, step;   /* surface; <= 0: 0.95 rest_density and 0.5 H (particles.cpp:392-401) */
   double surface_lo[3], surface_hi[3];
