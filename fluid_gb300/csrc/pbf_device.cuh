@@ -387,9 +387,21 @@ constexpr uint32_t kOffsetMask = (1u << kOffsetBits) - 1u;
 
 __device__ __forceinline__ int nbr_total(const uint4& h) { return static_cast<int>(h.w); }
 
+// Two forms of the same decode (slab tags are 0, 1 and 2, so both give the same slot).
+// The compiler schedules a pass's gathers differently around them; measured per pass on
+// the 1M colliding blocks (ms per step): lambda 0.238 / 0.256 and delta-p 0.282 / 0.315
+// with kBits / kCompare, XSPH 0.113 / 0.104.
+enum class Decode { kBits, kCompare };
+
+template <Decode DC = Decode::kBits>
 __device__ __forceinline__ uint32_t nbr_decode(const uint4& h, uint32_t e) {
-  const uint32_t g = e >> kOffsetBits;
-  const uint32_t base = g == 0u ? h.x : (g == 1u ? h.y : h.z);
+  uint32_t base;
+  if (DC == Decode::kBits) {
+    base = (e & (2u << kOffsetBits)) ? h.z : ((e & (1u << kOffsetBits)) ? h.y : h.x);
+  } else {
+    const uint32_t g = e >> kOffsetBits;
+    base = g == 0u ? h.x : (g == 1u ? h.y : h.z);
+  }
   return base + (e & kOffsetMask);
 }
 
@@ -413,8 +425,9 @@ __device__ __forceinline__ void for_each_neighbor(int i, int n, const uint4 h,
 // As for_each_neighbor, with each neighbour's data gathered ahead of the computation:
 // load(j) returns what f needs of neighbour j; per round D list entries are decoded and
 // their loads issued before f runs on any of them, so every thread keeps D independent
-// gathers in flight. Calls f(j, load(j)) in the same (ascending) order. D = 2, 4 or 8.
-template <int D, typename L, typename F>
+// gathers in flight. Calls f(j, load(j)) in the same (ascending) order. D = 2, 4 or 8;
+// DC picks the decode form.
+template <int D, Decode DC = Decode::kBits, typename L, typename F>
 __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h,
                                                      const uint32_t* __restrict__ words, L&& load, F&& f) {
   const int total = nbr_total(h);
@@ -425,10 +438,10 @@ __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h
     for (; k + 7 < total; k += 8) {
       const uint32_t w0 = __ldg(wp), w1 = __ldg(wp + sn), w2 = __ldg(wp + 2 * sn), w3 = __ldg(wp + 3 * sn);
       wp += 4 * sn;
-      const uint32_t j0 = nbr_decode(h, w0 & 0xffffu), j1 = nbr_decode(h, w0 >> 16);
-      const uint32_t j2 = nbr_decode(h, w1 & 0xffffu), j3 = nbr_decode(h, w1 >> 16);
-      const uint32_t j4 = nbr_decode(h, w2 & 0xffffu), j5 = nbr_decode(h, w2 >> 16);
-      const uint32_t j6 = nbr_decode(h, w3 & 0xffffu), j7 = nbr_decode(h, w3 >> 16);
+      const uint32_t j0 = nbr_decode<DC>(h, w0 & 0xffffu), j1 = nbr_decode<DC>(h, w0 >> 16);
+      const uint32_t j2 = nbr_decode<DC>(h, w1 & 0xffffu), j3 = nbr_decode<DC>(h, w1 >> 16);
+      const uint32_t j4 = nbr_decode<DC>(h, w2 & 0xffffu), j5 = nbr_decode<DC>(h, w2 >> 16);
+      const uint32_t j6 = nbr_decode<DC>(h, w3 & 0xffffu), j7 = nbr_decode<DC>(h, w3 >> 16);
       const auto a0 = load(j0);
       const auto a1 = load(j1);
       const auto a2 = load(j2);
@@ -451,8 +464,8 @@ __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h
     for (; k + 3 < total; k += 4) {
       const uint32_t w0 = __ldg(wp), w1 = __ldg(wp + sn);
       wp += 2 * sn;
-      const uint32_t j0 = nbr_decode(h, w0 & 0xffffu), j1 = nbr_decode(h, w0 >> 16);
-      const uint32_t j2 = nbr_decode(h, w1 & 0xffffu), j3 = nbr_decode(h, w1 >> 16);
+      const uint32_t j0 = nbr_decode<DC>(h, w0 & 0xffffu), j1 = nbr_decode<DC>(h, w0 >> 16);
+      const uint32_t j2 = nbr_decode<DC>(h, w1 & 0xffffu), j3 = nbr_decode<DC>(h, w1 >> 16);
       const auto a0 = load(j0);
       const auto a1 = load(j1);
       const auto a2 = load(j2);
@@ -466,14 +479,14 @@ __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h
   for (; k + 1 < total; k += 2) {
     const uint32_t w = __ldg(wp);
     wp += sn;
-    const uint32_t j0 = nbr_decode(h, w & 0xffffu), j1 = nbr_decode(h, w >> 16);
+    const uint32_t j0 = nbr_decode<DC>(h, w & 0xffffu), j1 = nbr_decode<DC>(h, w >> 16);
     const auto a0 = load(j0);
     const auto a1 = load(j1);
     f(j0, a0);
     f(j1, a1);
   }
   if (k < total) {
-    const uint32_t j0 = nbr_decode(h, __ldg(wp) & 0xffffu);
+    const uint32_t j0 = nbr_decode<DC>(h, __ldg(wp) & 0xffffu);
     f(j0, load(j0));
   }
 }
@@ -495,12 +508,22 @@ struct Pair {
   float3 r;
   float r2, q, s;
 };
+// FTZ selects the flush-to-zero form of the approximate reciprocal square root. The two
+// forms differ only for a subnormal r2, far below EPS_D^2, where s is 0 either way (and
+// both give +inf at r2 = 0, where hr is 0), so the pair values are the same; the vorticity
+// pass measured faster with it (0.066 against 0.071 ms per step on the 1M colliding
+// blocks), the other passes did not.
+template <bool FTZ = false>
 __device__ __forceinline__ Pair pair_of(const float4& xi, const float4& xj, float h, float h2) {
   Pair p;
   p.r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
   p.r2 = dot3(p.r, p.r);
   p.q = fmaxf(h2 - p.r2, 0.0f);
-  const float rinv = rsqrtf(p.r2);
+  float rinv;
+  if (FTZ)
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rinv) : "f"(p.r2));
+  else
+    rinv = rsqrtf(p.r2);
   const float hr = fmaxf(h - p.r2 * rinv, 0.0f);
   p.s = p.r2 >= kEps * kEps ? hr * hr * rinv : 0.0f;
   return p;

@@ -445,7 +445,7 @@ __global__ void __launch_bounds__(BLOCK) k_xsph(float4* xs, const float4* __rest
   struct XD {
     float4 x, d;
   };
-  for_each_neighbor_pf<8>(
+  for_each_neighbor_pf<8, Decode::kCompare>(
       i, n, hdr[i], words, [&](uint32_t j) { return XD{xs[j], __ldg(&disp[j])}; },
       [&](uint32_t, const XD& a) {
     const Pair p = pair_of(xi, a.x, P.h, P.h2);
@@ -479,7 +479,7 @@ __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
   float3 eta = make_float3(0.f, 0.f, 0.f);
   for_each_neighbor_pf<8>(i, n, hdr[i], words, [&](uint32_t j) -> float4 { return __ldg(&xs[j]); },
                           [&](uint32_t, const float4& xj) {
-    const Pair p = pair_of(xi, xj, P.h, P.h2);
+    const Pair p = pair_of<true>(xi, xj, P.h, P.h2);
     eta = eta + p.r * (xj.w * p.s);  // |omega_j| (k_xsph stores it in x*.w)
   });
   eta = eta * P.spiky_c;
