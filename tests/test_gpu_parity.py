@@ -389,3 +389,37 @@ def test_get_state_matches_the_single_getters(pbf):
         assert L.pbf_get_state(sim._h, None, v2.ctypes.data_as(pbf.P), None) == 0
         assert np.array_equal(v2, v)
         assert L.pbf_get_state(sim._h, None, None, None) == 0
+
+
+@pytest.mark.gpu
+def test_page_locked_host_buffers_match_pageable_ones(pbf):
+    """pbf_set_state / pbf_get_state with page-locked host buffers (views into the middle
+    of one larger page-locked block) carry the same state, bit for bit, as with pageable
+    ones."""
+    import torch
+
+    sc = scenes.block4096(4)
+    n = len(sc.pos)
+    L = pbf.lib()
+    x0, v0 = _f32(sc.pos), _f32(sc.vel)
+    outs = []
+    for pinned in (False, True):
+        with pbf.Simulator(x0, v0, sc.params) as sim:
+            if pinned:
+                blk = torch.zeros(3 * n * 4 + 64, dtype=torch.float32, pin_memory=True).numpy()
+                xh, vh = blk[16:16 + 3 * n].reshape(n, 3), blk[32 + 3 * n:32 + 6 * n].reshape(n, 3)
+                xo = blk[48 + 6 * n:48 + 9 * n].reshape(n, 3)
+                ro = blk[48 + 9 * n:48 + 10 * n]
+            else:
+                xh, vh, xo, ro = (np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32),
+                                  np.zeros((n, 3), np.float32), np.zeros(n, np.float32))
+            xh[:] = x0
+            vh[:] = v0
+            assert L.pbf_set_state(sim._h, xh.ctypes.data_as(pbf.P), vh.ctypes.data_as(pbf.P)) == 0
+            sim.time_step(sc.params.dt, 1)
+            assert L.pbf_get_state(sim._h, xo.ctypes.data_as(pbf.P), vh.ctypes.data_as(pbf.P),
+                                   ro.ctypes.data_as(pbf.P)) == 0
+            outs.append((xo.copy(), vh.copy(), ro.copy()))
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+    assert np.all(np.isfinite(outs[1][0])) and not np.array_equal(outs[1][0], x0)
