@@ -153,7 +153,7 @@ void Handle::free_all() {
     graph[k] = nullptr;
   }
   void* ptrs[] = {b.pos[0], b.pos[1], b.disp[0], b.disp[1], b.xs[0], b.xs[1], b.vel[0], b.vel[1],
-                  b.omega, b.pred, b.lam, b.rho, b.rho_iter0, b.id[0], b.id[1], b.key, b.rank,
+                  b.omega, b.pred, b.xkey, b.rho, b.rho_iter0, b.id[0], b.id[1], b.key, b.rank,
                   b.perm, b.nbr_hdr, b.nbr_w, b.cell_count, b.cell_start, b.scan_tmp, b.big_cells, b.big_count, b.scenes, b.stats_part,
                   b.stats, b.err, b.io, b.io2, scratch, snap_pos, snap_vel, snap_id};
   for (void* q : ptrs)
@@ -187,7 +187,7 @@ pbf_status Handle::alloc_all() {
   } list[] = {
       {(void**)&b.pos[0], f4}, {(void**)&b.pos[1], f4}, {(void**)&b.disp[0], f4}, {(void**)&b.disp[1], f4},
       {(void**)&b.xs[0], f4}, {(void**)&b.xs[1], f4}, {(void**)&b.vel[0], f4}, {(void**)&b.vel[1], f4},
-      {(void**)&b.omega, f4}, {(void**)&b.lam, u4}, {(void**)&b.rho, u4}, {(void**)&b.rho_iter0, u4},
+      {(void**)&b.omega, f4}, {(void**)&b.xkey, u4}, {(void**)&b.rho, u4}, {(void**)&b.rho_iter0, u4},
       {(void**)&b.id[0], u4}, {(void**)&b.id[1], u4}, {(void**)&b.key, u4}, {(void**)&b.rank, u4},
       {(void**)&b.perm, u4}, {(void**)&b.nbr_hdr, sizeof(uint4) * n},
       {(void**)&b.nbr_w, u4 * static_cast<size_t>(b.max_words)},

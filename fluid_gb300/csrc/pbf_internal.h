@@ -80,7 +80,7 @@ struct Buffers {
   float4* vel[2] = {nullptr, nullptr};
   float4* omega = nullptr;
   float4* pred = nullptr;  // optional copy of x* after prediction (sorted order)
-  float* lam = nullptr;
+  uint32_t* xkey = nullptr;  // order_bits(x*.x) per pre-sort slot (cell sort key)
   float* rho = nullptr;
   float* rho_iter0 = nullptr;  // density after the first lambda pass (stats)
   uint32_t* id[2] = {nullptr, nullptr};

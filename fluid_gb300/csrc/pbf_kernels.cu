@@ -7,7 +7,7 @@
 //                 count and rank (particles.cpp:175-183, 87-132)
 //   k_scan_*      exclusive prefix sum of the cell counts
 //   k_scatter     slot = cell start + rank
-//   k_cellsort    order each cell's slots by original index (determinism)
+//   k_cellsort    order each cell's slots by x, then original index (determinism)
 //   k_gather      reorder x, delta, id into cell order; x* = x + delta
 //   k_nbr_build   neighbour sets |x*_i - x*_j|^2 <= H2 over the 27 cells,
 //                 stored row-compressed (particles.cpp:258-265)
@@ -41,6 +41,12 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 
 __device__ __forceinline__ int scene_of_slot(const float4& p) { return __float_as_int(p.w); }
 
+// Order-preserving unsigned image of a float (a total order, NaN included).
+__device__ __forceinline__ uint32_t order_bits(float x) {
+  const uint32_t u = __float_as_uint(x);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
 // ---------------------------------------------------------------------------
 // prediction + cell count
 // ---------------------------------------------------------------------------
@@ -48,7 +54,8 @@ __device__ __forceinline__ int scene_of_slot(const float4& p) { return __float_a
 template <bool REC>
 __global__ void k_predict(const float4* __restrict__ pos, const float4* __restrict__ vel,
                           float4* __restrict__ disp_out, uint32_t* __restrict__ key_out,
-                          uint32_t* __restrict__ rank_out, uint32_t* __restrict__ cell_count,
+                          uint32_t* __restrict__ xkey_out, uint32_t* __restrict__ rank_out,
+                          uint32_t* __restrict__ cell_count,
                           const SceneDesc* __restrict__ scenes, DevParams P, float dt, int move,
                           int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -65,8 +72,10 @@ __global__ void k_predict(const float4* __restrict__ pos, const float4* __restri
       collide<REC>(x, d, predict_delta(v4, P, dt), true, sc, P, &code);
       disp_out[i] = make_float4(d.x, d.y, d.z, REC ? __uint_as_float(code) : 0.f);
     }
-    key = cell_key(cell_of(x + d, sc, P.inv_cell), sc);
+    const float3 xp = x + d;  // x*, as k_gather forms it
+    key = cell_key(cell_of(xp, sc, P.inv_cell), sc);
     key_out[i] = key;
+    xkey_out[i] = order_bits(xp.x);
   }
   // warp-aggregated per-cell rank
   const unsigned active = __ballot_sync(0xffffffffu, live);
@@ -168,11 +177,20 @@ __global__ void k_scatter(const uint32_t* __restrict__ key, const uint32_t* __re
   if (i < n) perm[cell_start[key[i]] + rank[i]] = static_cast<uint32_t>(i);
 }
 
-// Order each cell's slots by original particle index, so the cell order (hence every
-// neighbour sum) is independent of atomic timing. Cells up to kSmallCell particles are
+// Order each cell's slots by the x coordinate of x* (pos + disp, as k_gather forms it;
+// pos for a resort), ties by original particle index: the cell order (hence every
+// neighbour sum) is independent of atomic timing, and since cells along x are adjacent
+// slot ranges, every row of cells is sorted by x, which lets the neighbour build stop a
+// row at the first candidate beyond the reach. Cells up to kSmallCell particles are
 // insertion-sorted by one thread; larger ones go to a worklist for k_cellsort_big.
+// The x keys (order_bits of x*.x) are written by k_predict, indexed by the pre-sort slot.
+__device__ __forceinline__ uint64_t slot_order_key(const uint32_t* __restrict__ xkey, const uint32_t* __restrict__ id,
+                                                   uint32_t v) {
+  return (static_cast<uint64_t>(xkey[v]) << 32) | id[v];
+}
+
 __global__ void k_cellsort(const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ perm,
-                           const uint32_t* __restrict__ id, uint32_t* __restrict__ big_cells,
+                           const uint32_t* __restrict__ xkey, const uint32_t* __restrict__ id, uint32_t* __restrict__ big_cells,
                            uint32_t* __restrict__ big_count, uint32_t m) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m) return;
@@ -184,9 +202,9 @@ __global__ void k_cellsort(const uint32_t* __restrict__ cell_start, uint32_t* __
   }
   for (uint32_t x = b + 1; x < e; ++x) {
     const uint32_t v = perm[x];
-    const uint32_t kv = id[v];
+    const uint64_t kv = slot_order_key(xkey, id, v);
     uint32_t y = x;
-    while (y > b && id[perm[y - 1]] > kv) {
+    while (y > b && slot_order_key(xkey, id, perm[y - 1]) > kv) {
       perm[y] = perm[y - 1];
       --y;
     }
@@ -195,15 +213,18 @@ __global__ void k_cellsort(const uint32_t* __restrict__ cell_start, uint32_t* __
 }
 
 // Rank sort of the worklist's cells, one block per cell: the rank of an element is the
-// number of the cell's elements with a smaller original index (indices are distinct).
-// Cells over kMaxSortedCell particles keep the atomic order (bounded time).
+// number of the cell's elements with a smaller key (keys are distinct). Cells over
+// kMaxSortedCell particles keep the atomic order (bounded time); such a cell makes its
+// rows exceed kMaxRowCandidates, which the neighbour build reports as an error.
 __global__ void __launch_bounds__(kBigSortThreads) k_cellsort_big(const uint32_t* __restrict__ cell_start,
                                                                  uint32_t* __restrict__ perm,
+                                                                 const uint32_t* __restrict__ xkey,
                                                                  const uint32_t* __restrict__ id,
                                                                  const uint32_t* __restrict__ big_cells,
                                                                  const uint32_t* __restrict__ big_count) {
   __shared__ uint32_t slot[kMaxSortedCell];
-  __shared__ uint32_t key[kMaxSortedCell];
+  __shared__ uint32_t khi[kMaxSortedCell];
+  __shared__ uint32_t klo[kMaxSortedCell];
   const uint32_t cnt = *big_count;
   for (uint32_t w = blockIdx.x; w < cnt; w += gridDim.x) {
     const uint32_t c = big_cells[w];
@@ -212,14 +233,16 @@ __global__ void __launch_bounds__(kBigSortThreads) k_cellsort_big(const uint32_t
     if (m > kMaxSortedCell) continue;  // uniform across the block
     for (uint32_t t = threadIdx.x; t < m; t += blockDim.x) {
       const uint32_t v = perm[b + t];
+      const uint64_t k = slot_order_key(xkey, id, v);
       slot[t] = v;
-      key[t] = id[v];
+      khi[t] = static_cast<uint32_t>(k >> 32);
+      klo[t] = static_cast<uint32_t>(k);
     }
     __syncthreads();
     for (uint32_t t = threadIdx.x; t < m; t += blockDim.x) {
-      const uint32_t k = key[t];
+      const uint32_t kh = khi[t], kl = klo[t];
       uint32_t r = 0;
-      for (uint32_t u = 0; u < m; ++u) r += key[u] < k ? 1u : 0u;
+      for (uint32_t u = 0; u < m; ++u) r += (khi[u] < kh || (khi[u] == kh && klo[u] < kl)) ? 1u : 0u;
       perm[b + r] = slot[t];
     }
     __syncthreads();
@@ -256,9 +279,10 @@ __global__ void k_gather(const uint32_t* __restrict__ perm, const float4* __rest
 // ---------------------------------------------------------------------------
 // Each of the 9 candidate rows (3 z-slabs x 3 y-rows) is skipped when its cells lie
 // beyond h in y/z, and otherwise trimmed in x to the cells that reach [x - w, x + w],
-// w = sqrt(h^2 - d_yz^2): about 20 of the 27 cells on average. Both tests keep a margin
-// of 1e-3 cell, far above the FP32 rounding of the cell binning and of the predicate,
-// so no pair within h is dropped.
+// w = sqrt(h^2 - d_yz^2): about 20 of the 27 cells on average. Within the trimmed row
+// (sorted by x, see k_cellsort) only candidates with |dx| <= w are tested. All tests keep
+// a margin of 1e-3 cell, far above the FP32 rounding of the cell binning and of the
+// predicate, so no pair within h is dropped.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ xs,
                                                      const float4* __restrict__ pos,
@@ -284,6 +308,7 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
   const float reach = sqrtf(P.h2) * P.inv_cell + m;
   const float reach2 = reach * reach;
   const float ux = (xi.x - sc.origin[0]) * P.inv_cell;
+  const float cell_w = 1.0f / P.inv_cell;
   const int y0 = cc.y > 0 ? cc.y - 1 : 0;
 #pragma unroll
   for (int g = 0; g < 3; ++g) {
@@ -317,11 +342,22 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
       const uint32_t ui = static_cast<uint32_t>(i);
       const uint32_t mid0 = ui < start ? start : (ui < end ? ui : end);
       const uint32_t mid1 = ui < start ? start : (ui < end ? ui + 1 : end);
+      // the row is sorted by x: a binary search finds the first candidate at or above
+      // x - W and the first one above x + W ends the row (W = w cells, margin included;
+      // with NaN coordinates in the row the search may start early, never late)
+      const float W = w * cell_w;
       for (int half = 0; half < 2; ++half) {
-        const uint32_t a = half ? mid1 : start, b = half ? end : mid0;
+        uint32_t a = half ? mid1 : start, hi = half ? end : mid0;
+        const uint32_t b = hi;
+        while (a < hi) {
+          const uint32_t md = (a + hi) >> 1;
+          if (__ldg(&xs[md].x) - xi.x < -W) a = md + 1; else hi = md;
+        }
         for (uint32_t j = a; j < b; ++j) {
           const float4 xj = __ldg(&xs[j]);
-          if (dist2_rn(xi, xj) <= P.h2) {
+          const float dx = xj.x - xi.x;
+          if (dx > W) break;
+          if (dx >= -W && dist2_rn(xi, xj) <= P.h2) {
             const uint32_t off = j - gb;
             if (off > kOffsetMask) {
               flags |= PBF_ERRBIT_ROW_CAPACITY;
@@ -356,7 +392,7 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs, const uint4* __restrict__ hdr,
                                                   const uint32_t* __restrict__ words,
-                                                  float* __restrict__ lam, float* __restrict__ rho_iter0,
+                                                  float* __restrict__ rho_iter0,
                                                   DevParams P, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -375,7 +411,6 @@ __global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs, const uint4* __res
   const float kg = P.spiky_c * P.inv_rho0;
   const float denom = kg * kg * (g2 + dot3(gs, gs)) + P.epsilon;
   const float l = -(rho * P.inv_rho0 - 1.0f) / denom;
-  lam[i] = l;
   reinterpret_cast<float*>(xs)[4 * i + 3] = l;
   if (rho_iter0) rho_iter0[i] = rho;
 }
@@ -739,10 +774,10 @@ cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& 
   if (e != cudaSuccess) return e;
   if (rec)
     k_predict<true><<<blocks_for(n, t.block_predict), t.block_predict, 0, s>>>(
-        b.pos[cur], b.vel[cur], b.disp[0], b.key, b.rank, b.cell_count, b.scenes, P, dt, move ? 1 : 0, n);
+        b.pos[cur], b.vel[cur], b.disp[0], b.key, b.xkey, b.rank, b.cell_count, b.scenes, P, dt, move ? 1 : 0, n);
   else
     k_predict<false><<<blocks_for(n, t.block_predict), t.block_predict, 0, s>>>(
-        b.pos[cur], b.vel[cur], b.disp[0], b.key, b.rank, b.cell_count, b.scenes, P, dt, move ? 1 : 0, n);
+        b.pos[cur], b.vel[cur], b.disp[0], b.key, b.xkey, b.rank, b.cell_count, b.scenes, P, dt, move ? 1 : 0, n);
   if (mk) mk->mark(kPhasePredict, s);
   const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
   k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(b.cell_count, b.cell_start, b.scan_tmp, m);
@@ -750,9 +785,9 @@ cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& 
   k_scan_add<<<tiles, kScanThreads, 0, s>>>(b.cell_start, b.scan_tmp, m);
   if (mk) mk->mark(kPhaseScan, s);
   k_scatter<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(b.key, b.rank, b.cell_start, b.perm, n);
-  k_cellsort<<<blocks_for(m, t.block_misc), t.block_misc, 0, s>>>(b.cell_start, b.perm, b.id[cur], b.big_cells,
-                                                                   b.big_count, m);
-  k_cellsort_big<<<kBigSortBlocks, kBigSortThreads, 0, s>>>(b.cell_start, b.perm, b.id[cur], b.big_cells,
+  k_cellsort<<<blocks_for(m, t.block_misc), t.block_misc, 0, s>>>(b.cell_start, b.perm, b.xkey, b.id[cur],
+                                                                   b.big_cells, b.big_count, m);
+  k_cellsort_big<<<kBigSortBlocks, kBigSortThreads, 0, s>>>(b.cell_start, b.perm, b.xkey, b.id[cur], b.big_cells,
                                                              b.big_count);
   if (mk) mk->mark(kPhaseSort, s);
   return cudaGetLastError();
@@ -792,7 +827,7 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
     float4* dprec = rec ? tape->dp + static_cast<size_t>(it) * b.n : nullptr;
     PBF_BLOCK_SWITCH(t.block_solve,
                      k_lambda<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                         xcur, b.nbr_hdr, b.nbr_w, b.lam, (it == 0 && P.stats) ? b.rho_iter0 : nullptr, P, n));
+                         xcur, b.nbr_hdr, b.nbr_w, (it == 0 && P.stats) ? b.rho_iter0 : nullptr, P, n));
     if (mk) mk->mark(kPhaseLambda, s);
     if (rec) {
       if (P.scorr_n == 4) {
