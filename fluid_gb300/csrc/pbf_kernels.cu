@@ -342,22 +342,27 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
       const uint32_t ui = static_cast<uint32_t>(i);
       const uint32_t mid0 = ui < start ? start : (ui < end ? ui : end);
       const uint32_t mid1 = ui < start ? start : (ui < end ? ui + 1 : end);
-      // the row is sorted by x: a binary search finds the first candidate at or above
-      // x - W and the first one above x + W ends the row (W = w cells, margin included;
-      // with NaN coordinates in the row the search may start early, never late)
+      // the row is sorted by x: a binary search over the window's first cell (the only
+      // one reaching below x - W) finds the first candidate at or above x - W, and the
+      // first one above x + W ends the row (W = w cells, margin included; with NaN
+      // coordinates in the cell the search may start early, never late). The predicate
+      // reuses the x difference: the same _rn arithmetic as dist2_rn.
       const float W = w * cell_w;
+      const uint32_t first_end = __ldg(&cell_start[row + xa + 1]);
       for (int half = 0; half < 2; ++half) {
         uint32_t a = half ? mid1 : start, hi = half ? end : mid0;
         const uint32_t b = hi;
+        hi = min(hi, first_end);
         while (a < hi) {
           const uint32_t md = (a + hi) >> 1;
           if (__ldg(&xs[md].x) - xi.x < -W) a = md + 1; else hi = md;
         }
         for (uint32_t j = a; j < b; ++j) {
           const float4 xj = __ldg(&xs[j]);
-          const float dx = xj.x - xi.x;
-          if (dx > W) break;
-          if (dx >= -W && dist2_rn(xi, xj) <= P.h2) {
+          const float ndx = __fsub_rn(xi.x, xj.x);
+          if (ndx < -W) break;
+          const float dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
+          if (__fadd_rn(__fadd_rn(__fmul_rn(ndx, ndx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)) <= P.h2) {
             const uint32_t off = j - gb;
             if (off > kOffsetMask) {
               flags |= PBF_ERRBIT_ROW_CAPACITY;
