@@ -425,8 +425,9 @@ __device__ __forceinline__ void for_each_neighbor(int i, int n, const uint4 h,
 // As for_each_neighbor, with each neighbour's data gathered ahead of the computation:
 // load(j) returns what f needs of neighbour j; per round D list entries are decoded and
 // their loads issued before f runs on any of them, so every thread keeps D independent
-// gathers in flight. Calls f(j, load(j)) in the same (ascending) order. D = 2, 4 or 8;
-// DC picks the decode form.
+// gathers in flight. With D = 8 the next round's list words are loaded before this
+// round's computation, so their latency overlaps it. Calls f(j, load(j)) in the same
+// (ascending) order. D = 2, 4 or 8; DC picks the decode form.
 template <int D, Decode DC = Decode::kBits, typename L, typename F>
 __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h,
                                                      const uint32_t* __restrict__ words, L&& load, F&& f) {
@@ -435,9 +436,16 @@ __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h
   const uint32_t* wp = words + i;
   int k = 0;
   if (D == 8) {
+    uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u;
+    if (total >= 8) {
+      w0 = __ldg(wp); w1 = __ldg(wp + sn); w2 = __ldg(wp + 2 * sn); w3 = __ldg(wp + 3 * sn);
+    }
     for (; k + 7 < total; k += 8) {
-      const uint32_t w0 = __ldg(wp), w1 = __ldg(wp + sn), w2 = __ldg(wp + 2 * sn), w3 = __ldg(wp + 3 * sn);
       wp += 4 * sn;
+      uint32_t n0 = 0u, n1 = 0u, n2 = 0u, n3 = 0u;
+      if (k + 15 < total) {
+        n0 = __ldg(wp); n1 = __ldg(wp + sn); n2 = __ldg(wp + 2 * sn); n3 = __ldg(wp + 3 * sn);
+      }
       const uint32_t j0 = nbr_decode<DC>(h, w0 & 0xffffu), j1 = nbr_decode<DC>(h, w0 >> 16);
       const uint32_t j2 = nbr_decode<DC>(h, w1 & 0xffffu), j3 = nbr_decode<DC>(h, w1 >> 16);
       const uint32_t j4 = nbr_decode<DC>(h, w2 & 0xffffu), j5 = nbr_decode<DC>(h, w2 >> 16);
@@ -458,6 +466,7 @@ __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h
       f(j5, a5);
       f(j6, a6);
       f(j7, a7);
+      w0 = n0; w1 = n1; w2 = n2; w3 = n3;
     }
   }
   if (D >= 4) {
