@@ -465,7 +465,13 @@ pbf_status pbf_batch_create(const pbf_params* params, int n_scenes, const size_t
     return PBF_ERR_INVALID;
   }
   size_t n = 0;
-  for (int s = 0; s < n_scenes; ++s) n += counts[s];
+  for (int s = 0; s < n_scenes; ++s) {
+    if (counts[s] >= (size_t(1) << 31)) {  // also keeps the sum below from wrapping
+      g_create_error = "at most 2^31 - 1 particles";
+      return PBF_ERR_INVALID;
+    }
+    n += counts[s];
+  }
   if (n > 0 && !xyz) {
     g_create_error = "xyz is NULL";
     return PBF_ERR_INVALID;

@@ -94,3 +94,28 @@ def test_struct_layout_matches_header(tmp_path):
     expect = [ctypes.sizeof(CParams)] + [getattr(CParams, f).offset for f in fields_p]
     expect += [ctypes.sizeof(CStats)] + [getattr(CStats, f).offset for f in fields_s]
     assert vals == expect
+
+
+def test_create_rejects_bad_arguments_before_any_device_work(libpbf):
+    """pbf_batch_create validates its arguments on the host first (no GPU is touched):
+    a NULL out pointer, no scenes, NULL xyz with particles, or a count of 2^31 or more
+    (also where the sum over scenes would wrap) give PBF_ERR_INVALID and a message."""
+    from fluid_gb300.pbf import default_params_c
+
+    prm = default_params_c()
+    out = ctypes.c_void_p()
+    SizeArr = ctypes.c_size_t * 2
+    L = libpbf
+    xyz = (ctypes.c_float * 6)()
+    invalid = 1  # PBF_ERR_INVALID
+    header = (ROOT / "include" / "pbf.h").read_text()
+    assert re.search(r"PBF_ERR_INVALID\s*=\s*1\b", header)
+    args = lambda n_scenes, counts, x, o: (ctypes.byref(prm), n_scenes, counts, None, None, x, None, 0, o)
+    assert L.pbf_batch_create(*args(1, SizeArr(2, 0), xyz, None)) == invalid
+    assert L.pbf_batch_create(*args(0, SizeArr(2, 0), xyz, ctypes.byref(out))) == invalid
+    assert L.pbf_batch_create(*args(1, SizeArr(2, 0), None, ctypes.byref(out))) == invalid
+    assert L.pbf_batch_create(*args(1, SizeArr(1 << 31, 0), xyz, ctypes.byref(out))) == invalid
+    wrap = SizeArr((1 << 64) - 1, 2)  # sums to 1 modulo 2^64
+    assert L.pbf_batch_create(*args(2, wrap, xyz, ctypes.byref(out))) == invalid
+    assert b"2^31" in L.pbf_last_error(None)
+    assert not out.value
