@@ -145,7 +145,9 @@ __device__ __forceinline__ uint32_t coll_clamped(uint32_t c) { return (c >> 12) 
 // the wall), the predict move slides once along the wall for half the
 // remaining length unless a clip plane was crossed, then the clamp box.
 // REC additionally writes the collision record to *code (same arithmetic).
-template <bool REC = false>
+// MESH = false compiles the collider-triangle tests out (for launches with no triangles:
+// they hold registers a neighbour pass would otherwise spend on occupancy).
+template <bool REC = false, bool MESH = true>
 __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 delta, bool slide,
                                         const SceneDesc& sc, const DevParams& P, uint32_t* code = nullptr) {
   const float3 p = x + d;
@@ -169,7 +171,7 @@ __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 
   uint32_t rc = kCollFree;
   int wall;
   const float t = wall_hit(p, dir, l, sc, P.open_mask, &wall);
-  if (P.n_mesh > 0) {  // a collider triangle nearer than the wall or clip plane stops the move instead
+  if (MESH && P.n_mesh > 0) {  // a collider triangle nearer than the wall or clip plane stops the move instead
     float3 mn;
     bool mh;
     const float tm = mesh_hit(p, dir, t, P, &mn, &mh);
@@ -235,7 +237,7 @@ __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 
           int wall2;
           const float3 p1 = x + nd;
           const float t2 = wall_hit(p1, dir2, l2, sc, P.open_mask, &wall2);
-          if (P.n_mesh > 0) {  // the slide stops at a collider triangle before the wall
+          if (MESH && P.n_mesh > 0) {  // the slide stops at a collider triangle before the wall
             float3 mn2;
             bool mh2;
             const float tm2 = mesh_hit(p1, dir2, t2, P, &mn2, &mh2);

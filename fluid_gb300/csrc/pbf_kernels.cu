@@ -422,8 +422,10 @@ __global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs, const uint4* __res
 
 // (lambda_i + lambda_j + s_corr) grad W summed over neighbours; N4 specialises the
 // tensile exponent N = 4 of particles.cpp:40. REC (recording forward of the adjoint)
-// also stores the requested displacement and the collision record in dp_rec.
-template <int BLOCK, bool N4, bool REC>
+// also stores the requested displacement and the collision record in dp_rec. MESH =
+// false (no collider triangles) leaves the triangle tests out of the collision: 40
+// registers a thread instead of 55.
+template <int BLOCK, bool N4, bool REC, bool MESH>
 __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
                                                   const float4* __restrict__ pos,
                                                   const uint4* __restrict__ hdr,
@@ -459,7 +461,7 @@ __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
   float3 d = f3(d4);
   const float3 x = f3(x4);
   uint32_t code = 0u;
-  collide<REC>(x, d, dp, false, sc, P, &code);
+  collide<REC, MESH>(x, d, dp, false, sc, P, &code);
   if (REC) dp_rec[i] = make_float4(dp.x, dp.y, dp.z, __uint_as_float(code));
   disp[i] = make_float4(d.x, d.y, d.z, 0.f);
   xs_next[i] = make_float4(x.x + d.x, x.y + d.y, x.z + d.z, 0.f);
@@ -770,6 +772,15 @@ __global__ void k_density_at(const float4* __restrict__ pos, const uint32_t* __r
 
 inline unsigned blocks_for(size_t n, int block) { return static_cast<unsigned>((n + block - 1) / block); }
 
+// One delta-p pass (B = the buffer index holding this step's cell-ordered x and delta).
+template <bool N4, bool REC, bool MESH>
+void launch_deltap(const Tuning& t, const Buffers& b, int B, float4* xcur, float4* xnext, float4* dprec,
+                   const DevParams& P, int n, cudaStream_t s) {
+  PBF_BLOCK_SWITCH(t.block_solve,
+                   (k_deltap<BLOCK, N4, REC, MESH><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
+                       xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, dprec, P, n)));
+}
+
 // Shared front half of a step and of a resort: keys, counts, scan, slots.
 cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& t, int cur, float dt,
                             bool move, cudaStream_t s, PhaseMarks* mk = nullptr, bool rec = false) {
@@ -834,24 +845,16 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
                      k_lambda<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
                          xcur, b.nbr_hdr, b.nbr_w, (it == 0 && P.stats) ? b.rho_iter0 : nullptr, P, n));
     if (mk) mk->mark(kPhaseLambda, s);
-    if (rec) {
-      if (P.scorr_n == 4) {
-        PBF_BLOCK_SWITCH(t.block_solve,
-                         (k_deltap<BLOCK, true, true><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                             xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, dprec, P, n)));
-      } else {
-        PBF_BLOCK_SWITCH(t.block_solve,
-                         (k_deltap<BLOCK, false, true><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                             xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, dprec, P, n)));
-      }
-    } else if (P.scorr_n == 4) {
-      PBF_BLOCK_SWITCH(t.block_solve,
-                       (k_deltap<BLOCK, true, false><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                           xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, nullptr, P, n)));
+    const bool n4 = P.scorr_n == 4, mesh = P.n_mesh > 0;
+    if (rec) {  // the adjoint takes box colliders only; the recording keeps the general form
+      if (n4) launch_deltap<true, true, true>(t, b, B, xcur, xnext, dprec, P, n, s);
+      else launch_deltap<false, true, true>(t, b, B, xcur, xnext, dprec, P, n, s);
+    } else if (n4) {
+      if (mesh) launch_deltap<true, false, true>(t, b, B, xcur, xnext, nullptr, P, n, s);
+      else launch_deltap<true, false, false>(t, b, B, xcur, xnext, nullptr, P, n, s);
     } else {
-      PBF_BLOCK_SWITCH(t.block_solve,
-                       (k_deltap<BLOCK, false, false><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                           xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, nullptr, P, n)));
+      if (mesh) launch_deltap<false, false, true>(t, b, B, xcur, xnext, nullptr, P, n, s);
+      else launch_deltap<false, false, false>(t, b, B, xcur, xnext, nullptr, P, n, s);
     }
     if (mk) mk->mark(kPhaseDeltaP, s);
   }
