@@ -490,9 +490,9 @@ struct Scene {
   const RLight* lights;
   uint32_t n_scene, n_surf;
   const BvhNode* scene_nodes;  // null: brute force
-  const uint32_t* scene_leaf;
+  const RTri* scene_ltri;      // leaf-ordered triangles of each tree
   const BvhNode* surf_nodes;
-  const uint32_t* surf_leaf;
+  const RTri* surf_ltri;
 };
 
 constexpr uint32_t kNoItem = 0xffffffffu;
@@ -578,7 +578,7 @@ template <bool ANY>
 __device__ __forceinline__ void walk_step(const Scene& sc, const Ray& r, Walk& s, unsigned* err) {
   const bool scene = s.phase == 0;
   const BvhNode* __restrict__ nodes = scene ? sc.scene_nodes : sc.surf_nodes;
-  const uint32_t* __restrict__ leaf = scene ? sc.scene_leaf : sc.surf_leaf;
+  const RTri* __restrict__ ltri = scene ? sc.scene_ltri : sc.surf_ltri;
   const uint32_t base = scene ? 0u : sc.n_scene;
   const BvhNode nd = nodes[s.node];
   float tl, tr;
@@ -591,9 +591,10 @@ __device__ __forceinline__ void walk_step(const Scene& sc, const Ray& r, Walk& s
     bool& h = side ? hr : hl;
     if (h && (c & kLeafBit)) {
       h = false;
-      const uint32_t ti = base + leaf[c & ~kLeafBit];
+      const RTri tv = ltri[c & ~kLeafBit];
+      const uint32_t ti = base + __float_as_uint(tv.p1.w);
       float t, u, v;
-      if (tri_test(sc.tri[ti], r, s.tmax, &t, &u, &v)) {
+      if (tri_test(tv, r, s.tmax, &t, &u, &v)) {
         s.best = static_cast<int>(ti);
         s.tmax = t;
         s.bu = u;
@@ -894,6 +895,17 @@ cudaError_t launch_surface_to_tris(const float* xyz, const float* nrm, uint32_t 
   return cudaGetLastError();
 }
 
+// Triangles in leaf order with their index in p1.w (walk_step reads them directly).
+__global__ void k_leaf_tris(const RTri* __restrict__ tri, const uint32_t* __restrict__ vals, uint32_t n,
+                            RTri* __restrict__ ltri) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t i = vals[k];
+  RTri t = tri[i];
+  t.p1.w = __uint_as_float(i);
+  ltri[k] = t;
+}
+
 cudaError_t launch_bvh_build(const RTri* tri, uint32_t n, const BvhScratch& w, BvhNode* nodes, cudaStream_t s) {
   if (n < 2) return cudaSuccess;
   k_bounds_part<<<kBoundsBlocks, 256, 0, s>>>(tri, n, w.bounds);
@@ -919,6 +931,7 @@ cudaError_t launch_bvh_build(const RTri* tri, uint32_t n, const BvhScratch& w, B
   if (e != cudaSuccess) return e;
   k_refit<<<blocks(n, 256), 256, 0, s>>>(tri, w.vals, static_cast<int>(n), nodes, w.parent, w.flags, w.box_lo,
                                          w.box_hi);
+  k_leaf_tris<<<blocks(n, 256), 256, 0, s>>>(tri, w.vals, n, w.ltri);
   return cudaGetLastError();
 }
 
@@ -942,12 +955,12 @@ uint32_t render_batch_samples(int width, int height, int ns_aa, int slots, uint3
 }
 
 cudaError_t launch_render(const RTri* tri, const RNrm* nrm, uint32_t n_scene, uint32_t n_surf,
-                          const BvhNode* scene_nodes, const uint32_t* scene_leaf, const BvhNode* surf_nodes,
-                          const uint32_t* surf_leaf, const RMat* mats, const RLight* lights, const RCam& cam,
+                          const BvhNode* scene_nodes, const RTri* scene_ltri, const BvhNode* surf_nodes,
+                          const RTri* surf_ltri, const RMat* mats, const RLight* lights, const RCam& cam,
                           const RArgs& a, const WfBuffers& wb, float* hdr, unsigned* err, cudaStream_t s) {
   const size_t px = static_cast<size_t>(a.width) * a.height;
   if (px == 0) return cudaSuccess;
-  const Scene sc{tri, nrm, mats, lights, n_scene, n_surf, scene_nodes, scene_leaf, surf_nodes, surf_leaf};
+  const Scene sc{tri, nrm, mats, lights, n_scene, n_surf, scene_nodes, scene_ltri, surf_nodes, surf_ltri};
   int dev = 0, sms = 0, per_trace = 0, per_shade = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

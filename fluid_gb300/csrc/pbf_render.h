@@ -61,10 +61,13 @@ struct RArgs {
 // keys / vals / keys2 / vals2 n each (after the build vals maps a leaf's sorted position
 // to its triangle), hist 256 * sort_blocks(n), start 256 * sort_blocks(n) + 1,
 // tile_sums exclusive_scan_tiles(256 * sort_blocks(n)), parent 2n - 1, flags n - 1,
-// box_lo / box_hi 2n - 1, bounds 2 + 2 * kBoundsBlocks float4.
+// box_lo / box_hi 2n - 1, bounds 2 + 2 * kBoundsBlocks float4; ltri n: the triangles in
+// leaf order, p1.w holding each one's index in the build's range (int bits), so a leaf
+// visit reads its triangle without a dependent index load.
 struct BvhScratch {
   uint32_t *keys, *vals, *keys2, *vals2, *hist, *start, *tile_sums, *parent, *flags;
   float4 *box_lo, *box_hi, *bounds;
+  RTri* ltri;
 };
 uint32_t sort_blocks(uint32_t n);
 constexpr int kBoundsBlocks = 128;
@@ -105,13 +108,13 @@ size_t render_path_bytes(int slots);
 uint32_t render_batch_samples(int width, int height, int ns_aa, int slots, uint32_t budget_mib);
 // hdr: W * H * 3 floats, row y = 0 first (the bottom row, as the reference's sample buffer).
 // tri / nrm: the scene's n_scene triangles, then the surface's n_surf. scene_nodes null:
-// the scene's triangles are tested one by one (at most kBruteScene of them). *_leaf: a
-// build's vals (sorted position -> triangle of its range); err bit 0: a traversal stack
-// overflowed (deeper than kBvhStack levels).
+// the scene's triangles are tested one by one (at most kBruteScene of them). *_ltri: a
+// build's leaf-ordered triangles; err bit 0: a traversal stack overflowed (deeper than
+// kBvhStack levels).
 constexpr uint32_t kBruteScene = 32;
 cudaError_t launch_render(const RTri* tri, const RNrm* nrm, uint32_t n_scene, uint32_t n_surf,
-                          const BvhNode* scene_nodes, const uint32_t* scene_leaf, const BvhNode* surf_nodes,
-                          const uint32_t* surf_leaf, const RMat* mats, const RLight* lights, const RCam& cam,
+                          const BvhNode* scene_nodes, const RTri* scene_ltri, const BvhNode* surf_nodes,
+                          const RTri* surf_ltri, const RMat* mats, const RLight* lights, const RCam& cam,
                           const RArgs& a, const WfBuffers& wb, float* hdr, unsigned* err, cudaStream_t s);
 // rgba: W * H * 4 bytes, rows flipped (top first) as PathTracer::save_image writes them.
 cudaError_t launch_tonemap(const float* hdr, int width, int height, uint8_t* rgba, cudaStream_t s);

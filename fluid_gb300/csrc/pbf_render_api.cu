@@ -77,6 +77,7 @@ Tree carve_tree(Carve& c, size_t n) {
   t.w.box_lo = c.take<float4>(2 * n);
   t.w.box_hi = c.take<float4>(2 * n);
   t.w.bounds = c.take<float4>(2 + 2 * pbf::kBoundsBlocks);
+  t.w.ltri = c.take<pbf::RTri>(n);
   return t;
 }
 
@@ -395,7 +396,7 @@ pbf_status pbf_render(pbf_handle* hh, const pbf_camera* cam, const pbf_render_pa
   a.batch = static_cast<int>(batch);
   if (st == PBF_OK)
     st = h->cuda(pbf::launch_render(f.tri, f.nrm, R.n_scene, m, scene_tree ? f.scene.nodes : nullptr,
-                                    f.scene.w.vals, f.surf.nodes, f.surf.w.vals, f.mats, f.lights, rc, a, f.wf, f.hdr,
+                                    f.scene.w.ltri, f.surf.nodes, f.surf.w.ltri, f.mats, f.lights, rc, a, f.wf, f.hdr,
                                     f.err, h->stream),
                  "render");
   if (st == PBF_OK && rgba)
