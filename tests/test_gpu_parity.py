@@ -1,6 +1,6 @@
 """GPU parity: the CUDA step through the C ABI against the FP64 oracle and the golden vectors.
 
-Tolerances (the spec bar): after one step, positions, velocities and densities within
+Tolerances: after one step, positions, velocities and densities within
 1e-5 normwise relative error of the FP64 reference step in the order-independent XSPH form;
 neighbour sets and cell ids bit-exact against a host check that evaluates the same FP32
 predicate on the same FP32 x*. Every test also reports the FP32-vs-FP64 error it saw.
