@@ -1,7 +1,7 @@
 """ctypes wrapper of the FP64 restatement oracle (oracle/pbf_oracle.c).
 
 TEST INFRASTRUCTURE (the oracle): imported only by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline leg, as the checker or the timed CPU baseline. ``build()``
+bench.py's CPU-baseline leg, as the values results are compared with or the timed CPU baseline. ``build()``
 compiles the restatement with ``-ffp-contract=off`` so that x86-64 and aarch64 round
 identically; it is called by ``__graft_entry__.build()``.
 """

@@ -2,7 +2,7 @@
  * pbf_oracle.c — FP64 CPU restatement of the reference's PBF step.
  *
  * TEST INFRASTRUCTURE (the oracle). Only tests/, __graft_entry__.smoke() and
- * bench.py's CPU-baseline leg load this library, and only as the checker or
+ * bench.py's CPU-baseline leg load this library, and only as the values results are compared with or
  * the timed CPU baseline; the product path never calls it.
  *
  * It restates src/particles.cpp of the reference with the same floating-point
