@@ -345,7 +345,10 @@ pbf_status Handle::enqueue_steps(float dt, int nsteps) {
   const bool use_graph = (params.flags & PBF_FLAG_GRAPH) != 0;
   const bool keep_pred = b.pred != nullptr;
   const int it = params.iters;
-  const uint64_t per_step[kNumPhases] = {1, 3, 2, 1, 1, static_cast<uint64_t>(it), static_cast<uint64_t>(it),
+  // kernels per phase: k_predict; k_scan_tiles/sums/add; k_scatter, k_cellsort, k_cellsort_big;
+  // k_gather; k_nbr_build; k_lambda and k_deltap per iteration; k_xsph; k_vort; k_stats and
+  // k_stats_final when statistics are on
+  const uint64_t per_step[kNumPhases] = {1, 3, 3, 1, 1, static_cast<uint64_t>(it), static_cast<uint64_t>(it),
                                          1, 1, dp.stats ? 2u : 0u};
   for (int k = 0; k < nsteps; ++k) {
     if (use_graph && graph_dt != dt) {
