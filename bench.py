@@ -55,7 +55,7 @@ ALGO_BYTES = {"predict": 64 + 24, "sort": 104, "gather": 0, "lambda": 20, "delta
 # DRAM bytes per particle per launch measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum) on the 1M colliding-blocks scene; see profiles/.
 # Source: profiles/k_deltap_k_lambda_k_nbr_build_colliding_blocks_1m.md.
-NCU_TRAFFIC_PER_PARTICLE: dict[str, float] = {"deltap": 142.2, "lambda": 100.1, "neighbors": 62.6}
+NCU_TRAFFIC_PER_PARTICLE: dict[str, float] = {"deltap": 141.9, "lambda": 99.1, "neighbors": 62.2}
 
 
 def peaks():
