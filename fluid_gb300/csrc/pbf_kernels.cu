@@ -361,8 +361,8 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
           const float4 xj = __ldg(&xs[j]);
           const float ndx = __fsub_rn(xi.x, xj.x);
           if (ndx < -W) break;
-          const float dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
-          if (__fadd_rn(__fadd_rn(__fmul_rn(ndx, ndx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)) <= P.h2) {
+          const float ndy = __fsub_rn(xi.y, xj.y), ndz = __fsub_rn(xi.z, xj.z);
+          if (__fadd_rn(__fadd_rn(__fmul_rn(ndx, ndx), __fmul_rn(ndy, ndy)), __fmul_rn(ndz, ndz)) <= P.h2) {
             const uint32_t off = j - gb;
             if (off > kOffsetMask) {
               flags |= PBF_ERRBIT_ROW_CAPACITY;
