@@ -77,6 +77,8 @@ def lib(fp32: bool = False, adjoint: bool = False):
         L.orc_surface.argtypes = [P, ctypes.c_int64, P, ctypes.c_double, ctypes.c_double, P, P, P, P, P, P, P,
                                   ctypes.c_int64, ctypes.c_int]
         L.orc_surface.restype = ctypes.c_int64
+        L.orc_nbr_check_fp32.argtypes = [ctypes.c_int64, P, ctypes.c_float, P, P, P, P, P, P, ctypes.c_int]
+        L.orc_nbr_check_fp32.restype = ctypes.c_int
         _libs[path] = L
     return _libs[path]
 
@@ -133,6 +135,28 @@ def step(pos, vel, params: PbfParams, steps: int = 1, dt: float | None = None,
     if predicted:
         out["pred"] = pred
     return out
+
+
+def check_neighbors_fp32(xs32, h2: float, off, ids, threads: int = 0) -> dict:
+    """Compares ascending CSR neighbour lists (``off[n+1]``, ``ids``) with the sets the FP32
+    predicate fl32(|x_i - x_j|^2) <= fl32(h2) gives on the FP32 positions ``xs32``.
+
+    Returns the number of particles whose sets differ (``bad``), the pairs the lists miss
+    (``missing``) and hold in excess (``extra``), and the first differing particle
+    (``first``, -1 if none)."""
+    xs = np.ascontiguousarray(xs32, dtype=np.float32).reshape(-1, 3)
+    off = np.ascontiguousarray(off, dtype=np.int64)
+    ids = np.ascontiguousarray(ids, dtype=np.uint32)
+    if ids.size == 0:
+        ids = np.zeros(1, dtype=np.uint32)
+    if off.shape[0] != xs.shape[0] + 1:
+        raise ValueError("offsets must have n + 1 entries")
+    out = [ctypes.c_int64(0) for _ in range(4)]
+    rc = lib().orc_nbr_check_fp32(xs.shape[0], _ptr(xs), float(np.float32(h2)), _ptr(off), _ptr(ids),
+                                  *(ctypes.byref(o) for o in out), threads)
+    if rc:
+        raise RuntimeError(f"orc_nbr_check_fp32 failed: {rc}")
+    return dict(zip(("bad", "missing", "extra", "first"), (o.value for o in out)))
 
 
 def estimate_densities(pos, params: PbfParams, threads: int = 0) -> np.ndarray:

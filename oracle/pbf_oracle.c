@@ -667,6 +667,146 @@ int orc_estimate_density_at(const pbf_params* prm, int64_t n, const double* pos,
   return 0;
 }
 
+/* ---- neighbour sets under the FP32 predicate ------------------------------------ */
+
+typedef struct {
+  int64_t* a;
+  int64_t n, cap;
+} i64buf_t;
+
+static int buf_push(i64buf_t* b, int64_t v) {
+  if (b->n == b->cap) {
+    int64_t nc = b->cap ? 2 * b->cap : 256;
+    int64_t* na = (int64_t*)realloc(b->a, sizeof(int64_t) * (size_t)nc);
+    if (!na) return -1;
+    b->a = na;
+    b->cap = nc;
+  }
+  b->a[b->n++] = v;
+  return 0;
+}
+
+/*
+ * The neighbour relation of particles.cpp:258-265, N(i) = { j != i : |x_i - x_j|^2 <= H2 },
+ * evaluated in FP32 on FP32 positions exactly as an FP32 implementation must round it:
+ * dx = fl(x_i - x_j) per axis, r2 = fl(fl(fl(dx dx) + fl(dy dy)) + fl(dz dz)), r2 <= h2
+ * (this file is built with -ffp-contract=off, so nothing is fused). A uniform grid of
+ * cell 1.01 sqrt(h2) (pruning only) lists the candidates; the sets are compared with the
+ * given ascending CSR lists (off[n+1], ids). Returns 0 and writes the number of
+ * particles whose sets differ, the pairs the given lists miss and the pairs they hold
+ * in excess, and the first differing particle (-1 if none); -1 when out of memory,
+ * -2 for a non-finite or absurd extent.
+ */
+int orc_nbr_check_fp32(int64_t n, const float* xs, float h2, const int64_t* off, const uint32_t* ids,
+                       int64_t* bad, int64_t* missing, int64_t* extra, int64_t* first_bad, int nthreads) {
+  set_threads(nthreads);
+  *bad = *missing = *extra = 0;
+  *first_bad = -1;
+  if (n == 0) return 0;
+  double lo[3] = {xs[0], xs[1], xs[2]}, hi[3] = {lo[0], lo[1], lo[2]};
+  for (int64_t i = 1; i < n; i++)
+    for (int k = 0; k < 3; k++) {
+      const double v = xs[3 * i + k];
+      if (v < lo[k]) lo[k] = v;
+      if (v > hi[k]) hi[k] = v;
+    }
+  const double cell = 1.01 * sqrt((double)h2);
+  int64_t dim[3];
+  for (int k = 0; k < 3; k++) {
+    if (!(hi[k] - lo[k] < 1e6 * cell)) return -2;
+    dim[k] = (int64_t)floor((hi[k] - lo[k]) / cell) + 1;
+  }
+  const int64_t ncell = dim[0] * dim[1] * dim[2];
+  if (ncell > ((int64_t)1 << 31)) return -2;
+  int64_t* cell_of = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
+  int64_t* start = (int64_t*)calloc((size_t)ncell + 1, sizeof(int64_t));
+  int64_t* sorted = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
+  int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (size_t)ncell);
+  if (!cell_of || !start || !sorted || !fill) return -1;
+  for (int64_t i = 0; i < n; i++) {
+    int64_t ci[3];
+    for (int k = 0; k < 3; k++) {
+      ci[k] = (int64_t)floor(((double)xs[3 * i + k] - lo[k]) / cell);
+      if (ci[k] < 0) ci[k] = 0;
+      if (ci[k] >= dim[k]) ci[k] = dim[k] - 1;
+    }
+    cell_of[i] = (ci[2] * dim[1] + ci[1]) * dim[0] + ci[0];
+    start[cell_of[i] + 1]++;
+  }
+  for (int64_t q = 0; q < ncell; q++) start[q + 1] += start[q];
+  memcpy(fill, start, sizeof(int64_t) * (size_t)ncell);
+  for (int64_t i = 0; i < n; i++) sorted[fill[cell_of[i]]++] = i;
+  free(fill);
+  int64_t nbad = 0, nmiss = 0, nextra = 0, first = -1;
+  int oom = 0;
+#pragma omp parallel reduction(+ : nbad, nmiss, nextra)
+  {
+    i64buf_t b = {NULL, 0, 0};
+    int64_t my_first = -1;
+#pragma omp for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < n; i++) {
+      const int64_t q = cell_of[i];
+      const int64_t cx = q % dim[0], cy = (q / dim[0]) % dim[1], cz = q / (dim[0] * dim[1]);
+      const float xi = xs[3 * i], yi = xs[3 * i + 1], zi = xs[3 * i + 2];
+      b.n = 0;
+      for (int64_t z = cz - 1; z <= cz + 1; z++) {
+        if (z < 0 || z >= dim[2]) continue;
+        for (int64_t y = cy - 1; y <= cy + 1; y++) {
+          if (y < 0 || y >= dim[1]) continue;
+          for (int64_t x = cx - 1; x <= cx + 1; x++) {
+            if (x < 0 || x >= dim[0]) continue;
+            const int64_t qq = (z * dim[1] + y) * dim[0] + x;
+            for (int64_t s = start[qq]; s < start[qq + 1]; s++) {
+              const int64_t j = sorted[s];
+              if (j == i) continue;
+              const float dx = xi - xs[3 * j], dy = yi - xs[3 * j + 1], dz = zi - xs[3 * j + 2];
+              const float ax = dx * dx, ay = dy * dy, az = dz * dz;
+              const float sxy = ax + ay;
+              const float r2 = sxy + az;
+              if (r2 <= h2 && buf_push(&b, j) != 0) oom = 1;
+            }
+          }
+        }
+      }
+      qsort(b.a, (size_t)b.n, sizeof(int64_t), cmp_i64);
+      /* merge the expected set b with the given list */
+      int64_t u = 0, e = off[i], ee = off[i + 1], m = 0, x = 0;
+      while (u < b.n || e < ee) {
+        if (e >= ee || (u < b.n && b.a[u] < (int64_t)ids[e])) {
+          m++;
+          u++;
+        } else if (u >= b.n || (int64_t)ids[e] < b.a[u]) {
+          x++;
+          e++;
+        } else {
+          u++;
+          e++;
+        }
+      }
+      if (m || x) {
+        nbad++;
+        nmiss += m;
+        nextra += x;
+        if (my_first < 0 || i < my_first) my_first = i;
+      }
+    }
+#pragma omp critical
+    {
+      if (my_first >= 0 && (first < 0 || my_first < first)) first = my_first;
+    }
+    free(b.a);
+  }
+  free(cell_of);
+  free(start);
+  free(sorted);
+  if (oom) return -1;
+  *bad = nbad;
+  *missing = nmiss;
+  *extra = nextra;
+  *first_bad = first;
+  return 0;
+}
+
 /* ---- surface (Particles::getSurfacePrims, particles.cpp:352-385) ------------------- */
 
 /* estimateDensityAt, particles.cpp:446-453: poly6 summed over every particle in index order */

@@ -1,0 +1,219 @@
+"""GPU parity at the workload sizes: the 1,048,576-particle colliding blocks, the 262,144-particle
+dam break, the full 256-scene batch, and rollouts at the configured horizons.
+
+Every check runs the CUDA step through the C ABI and compares it with the FP64 restatement
+(``fp64-grid``: oracle/pbf_oracle.c, pinned bit for bit to the reference's own step on the
+golden cases) on the same FP32 inputs:
+
+- neighbour sets and cell ids bit-exact against the FP32 predicate evaluated on the CPU on
+  the GPU's own x* (oracle ``check_neighbors_fp32``, ``cells_fp32``);
+- positions, velocities and densities after one step within 1e-5 normwise relative error,
+  or within 3x the FP64 step's own sensitivity to one FP32 rounding of its inputs where
+  that sensitivity exceeds the 1e-5 bar (the configured colliding blocks, whose tensile
+  term k = 0.1 blows the blocks apart within the step: the FP64 step itself moves by
+  6e-3 in positions when its inputs move by one ulp). The sensitivity is measured on the
+  GPU's neighbour sets, so it holds arithmetic only;
+- the error flags (row and neighbour capacity, non-finite values) stay clear;
+- rollouts by the mean and 99th percentile of |rho/rho0 - 1| against ensembles of FP64 and
+  FP32 oracle rollouts from ulp-perturbed inputs.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from fluid_gb300 import scenes
+from fluid_gb300.params import PBF_FLAG_KEEP_PREDICTED, PBF_FLAG_STATS
+from tests.helpers import cells_fp32, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL_1STEP = 1e-5
+SENS_FACTOR = 3.0
+FIELDS = ("pos", "vel", "density")
+
+
+@pytest.fixture(scope="module")
+def pbf():
+    from fluid_gb300 import pbf as mod
+
+    mod.lib()
+    return mod
+
+
+def _f32(a):
+    return np.asarray(a, dtype=np.float32).astype(np.float64)
+
+
+def _gpu_step(pbf, pos, vel, prm, counts=None, boxes=None, steps=1):
+    prm = prm.with_(flags=PBF_FLAG_STATS | PBF_FLAG_KEEP_PREDICTED)
+    with pbf.Simulator(pos, vel, prm, counts=counts, boxes=boxes) as sim:
+        sim.time_step(prm.dt, steps)
+        out = {"pos": sim.positions(), "vel": sim.velocities(), "density": sim.densities(),
+               "stats": sim.stats(), "pred": sim.predicted(), "nbr": sim.neighbors()}
+        out["cells"] = sim.cells()
+    return out
+
+
+def _elementwise(a, b):
+    """99th percentile and maximum of the per-particle relative error (vector norms for
+    positions and velocities), each particle's scale floored at 1e-3 of the median."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    d = np.linalg.norm(a - b, axis=-1) if a.ndim > 1 else np.abs(a - b)
+    s = np.linalg.norm(b, axis=-1) if b.ndim > 1 else np.abs(b)
+    r = d / np.maximum(s, 1e-3 * np.median(s) + 1e-30)
+    return float(np.percentile(r, 99)), float(r.max())
+
+
+def _sensitivity(oracle_lib, pos, vel, prm, sets, ref, seed=0):
+    """How far the FP64 step moves (same neighbour sets) when its FP32 inputs are perturbed by
+    about one ulp: the floor under any FP32 evaluation of this step."""
+    rng = np.random.default_rng(seed)
+    p2 = pos * (1 + rng.uniform(-6e-8, 6e-8, pos.shape))
+    b = oracle_lib.step(p2, vel, prm, 1, given_neighbors=sets)
+    return {k: rel_err(b[k], ref[k]) for k in FIELDS}
+
+
+def _check_sets_and_cells(oracle_lib, g, prm, lo=None, hi=None):
+    off, ids = g["nbr"]
+    chk = oracle_lib.check_neighbors_fp32(g["pred"], prm.h2, off, ids)
+    assert chk["bad"] == 0, chk
+    assert np.array_equal(g["cells"].astype(np.int64), cells_fp32(g["pred"], prm, lo, hi))
+    return int(off[-1])
+
+
+def _compare_one_step(name, oracle_lib, pos, vel, prm, g, strict=()):
+    """GPU vs FP64 on the same FP32 inputs, with the oracle's own neighbour search; the
+    bar is 1e-5, or SENS_FACTOR x the FP64 sensitivity where that is larger (never for the
+    fields in ``strict``)."""
+    ref = oracle_lib.step(pos, vel, prm, 1)
+    got = {k: rel_err(g[k], ref[k]) for k in FIELDS}
+    sens = _sensitivity(oracle_lib, pos, vel, prm, g["nbr"], oracle_lib.step(pos, vel, prm, 1,
+                                                                             given_neighbors=g["nbr"]))
+    el = {k: _elementwise(g[k], ref[k]) for k in FIELDS}
+    print(f"{name}: GPU vs FP64 normwise " + ", ".join(f"{k} {got[k]:.2e}" for k in FIELDS)
+          + "; elementwise p99/max " + ", ".join(f"{k} {el[k][0]:.1e}/{el[k][1]:.1e}" for k in FIELDS)
+          + "; FP64 sensitivity to FP32 input rounding " + ", ".join(f"{k} {sens[k]:.2e}" for k in FIELDS))
+    for k in FIELDS:
+        bar = TOL_1STEP if k in strict else max(TOL_1STEP, SENS_FACTOR * sens[k])
+        assert got[k] < bar, (k, got[k], bar)
+    return got, sens
+
+
+def test_colliding_blocks_1m_one_step_well_conditioned(pbf, oracle_lib):
+    """The headline layout (1,048,576 particles, h = 0.0125, 80^3 cells, rows of 64 occupied
+    cells, ~28 neighbours) with the mass-scaled default tensile constant, where the step is
+    well conditioned: positions, velocities and densities within 1e-5 of FP64, sets and
+    cells bit-exact, no capacity flag."""
+    sc = scenes.colliding_blocks_1m()
+    prm = sc.params.with_(scorr_k=scenes.physical_params(sc.params.h, sc.params.h / 2).scorr_k)
+    pos, vel = _f32(sc.pos), _f32(sc.vel)
+    g = _gpu_step(pbf, pos, vel, prm)
+    assert g["stats"]["error_flags"] == 0
+    pairs = _check_sets_and_cells(oracle_lib, g, prm)
+    _compare_one_step("colliding_blocks_1m (default k)", oracle_lib, pos, vel, prm, g, strict=FIELDS)
+    assert pairs > 25 * sc.n
+
+
+def test_colliding_blocks_1m_one_step_configured(pbf, oracle_lib):
+    """The configured scene (tensile k = 0.1, n = 4): the same work as the bench's timed step.
+    Sets, cells and flags as above; the fields against FP64 within 1e-5 or 3x the FP64
+    step's own input sensitivity (which is ~6e-3 in positions here)."""
+    sc = scenes.colliding_blocks_1m()
+    pos, vel = _f32(sc.pos), _f32(sc.vel)
+    g = _gpu_step(pbf, pos, vel, sc.params)
+    assert g["stats"]["error_flags"] == 0
+    _check_sets_and_cells(oracle_lib, g, sc.params)
+    _compare_one_step("colliding_blocks_1m (k = 0.1)", oracle_lib, pos, vel, sc.params, g)
+
+
+def test_dam_break_262k_one_step(pbf, oracle_lib):
+    """262,144 particles, h = 0.025, the 0.8 m cube against the x = 0 wall."""
+    sc = scenes.dam_break_262k()
+    pos, vel = _f32(sc.pos), _f32(sc.vel)
+    g = _gpu_step(pbf, pos, vel, sc.params)
+    assert g["stats"]["error_flags"] == 0
+    _check_sets_and_cells(oracle_lib, g, sc.params)
+    _compare_one_step("dam_break_262k", oracle_lib, pos, vel, sc.params, g, strict=("pos", "density"))
+
+
+def test_batched_256_scenes_against_oracle(pbf, oracle_lib):
+    """The full 256-scene batch (2,048-32,768 particles per scene, 2.8M in all) in one handle,
+    one step; eleven scenes spanning the count range (smallest, largest and the deciles
+    between) are each compared with the FP64 oracle stepping that scene alone, with their
+    neighbour sets checked against the FP32 predicate."""
+    b = scenes.batched_256()
+    pos, vel = _f32(b.pos), _f32(b.vel)
+    g = _gpu_step(pbf, pos, vel, b.params, counts=b.counts, boxes=b.boxes)
+    assert g["stats"]["error_flags"] == 0
+    counts = np.asarray(b.counts)
+    starts = np.concatenate([[0], np.cumsum(counts)])
+    order = np.argsort(counts, kind="stable")
+    pick = sorted({int(order[int(round(q * (len(order) - 1)))]) for q in np.linspace(0, 1, 11)})
+    assert len(pick) >= 8
+    off, ids = g["nbr"]
+    for s in pick:
+        a, e = int(starts[s]), int(starts[s + 1])
+        so = off[a:e + 1] - off[a]
+        si = ids[off[a]:off[e]].astype(np.int64) - a
+        assert si.min() >= 0 and si.max() < e - a  # no pair crosses scenes
+        chk = oracle_lib.check_neighbors_fp32(g["pred"][a:e], b.params.h2, so, si.astype(np.uint32))
+        assert chk["bad"] == 0, (s, chk)
+        sub = {k: g[k][a:e] for k in FIELDS}
+        sub["nbr"] = (so, si)
+        _compare_one_step(f"batched scene {s} ({e - a} particles)", oracle_lib, pos[a:e], vel[a:e], b.params, sub,
+                          strict=("pos", "density"))
+
+
+def _ensemble(oracle_lib, pos, vel, prm, steps, members, seed=0):
+    rng = np.random.default_rng(seed)
+    base = _f32(pos)
+    out = {False: [], True: []}
+    for fp32 in (False, True):
+        for k in range(members):
+            p = base if k == 0 else base * (1 + rng.uniform(-6e-8, 6e-8, base.shape))
+            out[fp32].append(oracle_lib.step(p, _f32(vel), prm, steps, fp32=fp32)["density"])
+    return out
+
+
+def _cstats(rho, prm):
+    c = np.abs(np.asarray(rho, dtype=np.float64) / prm.rest_density - 1)
+    return float(c.mean()), float(np.percentile(c, 99))
+
+
+def _rollout_band(name, pbf, oracle_lib, pos, vel, prm, steps, members):
+    """The GPU rollout's mean and p99 |C| inside the band the FP64 and FP32 oracle ensembles
+    span, widened by their own spread (or 10% / 25% of the mean where that is larger)."""
+    g = _gpu_step(pbf, _f32(pos), _f32(vel), prm, steps=steps)
+    assert g["stats"]["error_flags"] == 0
+    assert np.all(np.isfinite(g["pos"])) and np.all(np.isfinite(g["vel"]))
+    ens = _ensemble(oracle_lib, pos, vel, prm, steps, members)
+    m, p99 = _cstats(g["density"], prm)
+    st = {fp: np.array([_cstats(r, prm) for r in ens[fp]]) for fp in ens}
+    allm = np.concatenate([st[False][:, 0], st[True][:, 0]])
+    allp = np.concatenate([st[False][:, 1], st[True][:, 1]])
+    print(f"{name} {steps} steps: mean|C| gpu {m:.4f}, FP64 {st[False][:, 0].min():.4f}..{st[False][:, 0].max():.4f}, "
+          f"FP32 {st[True][:, 0].min():.4f}..{st[True][:, 0].max():.4f}; p99|C| gpu {p99:.4f}, "
+          f"FP64 {st[False][:, 1].min():.4f}..{st[False][:, 1].max():.4f}, "
+          f"FP32 {st[True][:, 1].min():.4f}..{st[True][:, 1].max():.4f}")
+    mm = max(allm.max() - allm.min(), 0.1 * allm.mean()) + 1e-3
+    assert allm.min() - mm <= m <= allm.max() + mm
+    mp = max(allp.max() - allp.min(), 0.25 * allp.mean()) + 1e-3
+    assert allp.min() - mp <= p99 <= allp.max() + mp
+    return m, p99
+
+
+def test_block4096_rollout_60_steps(pbf, oracle_lib):
+    """The config-1 block over its configured 60 steps. At this horizon the clumping of the
+    reference's formulation depends on the arithmetic precision itself (FP64 ensemble mean
+    |C| ~1.25, FP32 ~0.65), so the band spans both ensembles."""
+    sc = scenes.block4096(1)
+    _rollout_band("block4096", pbf, oracle_lib, sc.pos, sc.vel, sc.params, 60, 3)
+
+
+def test_dam_break_262k_rollout_8_steps(pbf, oracle_lib):
+    """The dam break over 8 steps. With 4 Jacobi iterations the reference's formulation lets
+    this fluid clump (FP64: max neighbours 93 at step 8, 140 at step 11, 728 at step 20,
+    against the scene's capacity of 128), so the rollout stops at 8 steps."""
+    sc = scenes.dam_break_262k()
+    _rollout_band("dam_break_262k", pbf, oracle_lib, sc.pos, sc.vel, sc.params, 8, 2)
