@@ -117,7 +117,8 @@ def sample_block(scene, side=16):
 
 
 def run_reference_sample(scene, steps, procs, side=16):
-    """The reference step (oracle/_ref) on `procs` disjoint side^3 samples in parallel."""
+    """The reference step (oracle/_ref) on `procs` disjoint side^3 samples in parallel
+    (side^3 sub-lattices of the first block, moved along z, so side <= 64)."""
     from oracle import ref_runner
 
     if not ref_runner.available():
@@ -141,6 +142,37 @@ def run_reference_sample(scene, steps, procs, side=16):
     return {"value": procs * n * steps / secs, "seconds": secs, "n": n, "steps": steps, "procs": procs}
 
 
+def reference_fit_1m(scene, sides=(12, 16, 24, 32)) -> dict | None:
+    """The reference step's cost at the workload's full size, extrapolated: one process
+    steps side^3 sub-lattices of the workload (3 steps below 10,000 particles, 1 above);
+    the reference's all-pairs neighbour search makes its time per step grow with N^2, and
+    the least-squares fit t(N) = a N^2 + b N over the measured sizes (each point weighted by
+    1/t, so each counts by its relative error) gives t at the full N. Labelled
+    "extrapolated": the full step is not run. Its per-pair cost grows from 13,824 to 32,768
+    particles as the particles outgrow the host's caches, so the fit is a floor."""
+    from oracle import ref_runner
+
+    if not ref_runner.available():
+        return None
+    pts = []
+    for side in sides:
+        steps = 3 if side ** 3 < 10000 else 1
+        r = run_reference_sample(scene, steps, 1, side)
+        pts.append((r["n"], r["seconds"] / steps))
+    n = np.array([p[0] for p in pts], dtype=np.float64)
+    t = np.array([p[1] for p in pts], dtype=np.float64)
+    A = np.stack([n * n, n], 1) / t[:, None]
+    (a, b), *_ = np.linalg.lstsq(A, np.ones_like(t), rcond=None)
+    big = float(scene.n)
+    t_big = a * big * big + b * big
+    return {"value": big / t_big, "unit": UNIT, "kind": "extrapolated", "cores": 1,
+            "seconds_per_step": t_big, "fit": "t(N) = a N^2 + b N, least squares in relative error",
+            "a": float(a), "b": float(b),
+            "measured": [{"particles": int(p[0]), "seconds_per_step": p[1]} for p in pts],
+            "sample": f"reference step on {', '.join(f'{s}^3' for s in sides)} sub-lattices of {scene.name}, "
+                      f"1 process; extrapolated to {scene.n} particles"}
+
+
 def port_steps(pos, vel, params, steps, threads):
     """The FP64 restatement, `steps` single steps each from (pos, vel); returns seconds."""
     from oracle import oracle
@@ -162,11 +194,16 @@ def cpu_baseline(scene, budget_s: float):
         per_step = probe["seconds"] / 2
         steps = max(2, min(400, int(budget_s / max(per_step, 1e-4))))
         r = run_reference_sample(scene, steps, 1)
-        return {"value": r["value"], "unit": UNIT, "cores": 1, "kind": "reference",
-                "sample": f"reference particles.cpp step (FP64, O(N^2) all-pairs) on a {r['n']}-particle "
-                          f"16^3 sub-lattice of the workload, {steps} steps each from the sample's configured "
-                          f"initial state, 1 thread; the reference's cost "
-                          f"per particle grows with N, so this sample overstates its speed on the full scene"}
+        out = {"value": r["value"], "unit": UNIT, "cores": 1, "kind": "reference",
+               "sample": f"reference particles.cpp step (FP64, O(N^2) all-pairs) on a {r['n']}-particle "
+                         f"16^3 sub-lattice of the workload, {steps} steps each from the sample's configured "
+                         f"initial state, 1 thread; the reference's cost "
+                         f"per particle grows with N, so this sample overstates its speed on the full scene",
+               "sample_particles": r["n"]}
+        fit = reference_fit_1m(scene)
+        if fit:
+            out["extrapolated_1m"] = fit
+        return out
     pos, vel = sample_block(scene, 32)
     dt = port_steps(pos, vel, scene.params, 2, 1) / 2
     steps = max(1, min(200, int(budget_s / max(dt, 1e-4))))
@@ -177,16 +214,18 @@ def cpu_baseline(scene, budget_s: float):
 
 
 def cpu_port_all_cores(scene, budget_s: float):
+    """The FP64 restatement (fp64-grid: uniform grid, OpenMP) on the full workload, every
+    step from the configured state, on all host threads: the same-size CPU figure."""
     from oracle import oracle
 
-    pos, vel = sample_block(scene, 48)
+    pos, vel = scene.pos, scene.vel
     threads = oracle.max_threads()
     dt = port_steps(pos, vel, scene.params, 1, threads)
-    steps = max(1, min(200, int(budget_s / max(dt, 1e-4))))
+    steps = max(1, min(20, int(budget_s / max(dt, 1e-4))))
     secs = port_steps(pos, vel, scene.params, steps, threads)
     return {"value": pos.shape[0] * steps / secs, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"FP64 restatement (uniform grid, OpenMP) on a {pos.shape[0]}-particle sub-lattice, "
-                      f"{steps} steps"}
+            "sample": f"FP64 restatement (uniform grid, OpenMP) on the full {pos.shape[0]}-particle workload, "
+                      f"{steps} steps each from the configured state"}
 
 
 def workload_config(scene, extra=None):
@@ -316,6 +355,8 @@ def bench_reference(args, scene, world, rank):
         kind, cores = "port", threads
         sample = f"FP64 restatement (OpenMP) on a {pos.shape[0]}-particle sub-lattice, {args.steps} steps"
         ms = secs / args.steps * 1e3
+        run_n = pos.shape[0]
+        fit = None
     else:
         run_reference_sample(scene, max(args.warmup, 1), procs)  # warm-up
         r = run_reference_sample(scene, args.steps, procs)
@@ -324,12 +365,19 @@ def bench_reference(args, scene, world, rank):
                   f"{r['n']}-particle disjoint 16^3 sub-lattices of the workload, {args.steps} steps each; "
                   f"its all-pairs search makes the full {scene.n}-particle step far slower than this sample")
         ms = r["seconds"] / args.steps * 1e3
+        run_n = procs * r["n"]
+        fit = reference_fit_1m(scene)
+    cfg = workload_config(scene, {"particles": int(run_n), "source_workload": scene.name,
+                                  "source_particles": int(scene.n),
+                                  "sample": "disjoint sub-lattices of the source workload, stepped independently"})
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload_config(scene),
+            "config": cfg,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if fit:
+        line["extrapolated_1m"] = fit
     print(json.dumps(line))
     return 0
 
@@ -599,6 +647,28 @@ def bench_ours(args, scene, world, rank, local):
     clk = clocks.stop()
     total_ms = reduce_max(sum(step_ms), world)
     value = world * n * args.steps / (total_ms / 1e3)
+
+    # The same step from the caller's particle order: the state is uploaded in its original
+    # (unsorted) order before every step (pbf_set_state_device, untimed), so the step's cell
+    # sort starts from an unsorted array, as it does after pbf_set_state.
+    x0d = torch.tensor(scene.pos.astype(np.float32), device=f"cuda:{local}")
+    v0d = torch.tensor(scene.vel.astype(np.float32), device=f"cuda:{local}")
+    uns = []
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps + 1):
+            sim.set_state_device(x0d.data_ptr(), v0d.data_ptr(), stream.cuda_stream)
+            flush.zero_()
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            sim.step_async(dt, 1)
+            z.record(stream)
+            if k:  # the first step warms the unsorted-start graph
+                uns.append((a, z))
+    sim.sync()
+    torch.cuda.synchronize()
+    uns_ms = reduce_max(sum(a.elapsed_time(z) for a, z in uns), world) / len(uns)
+    del x0d, v0d
     stats = sim.stats()
     surface = bench_surface(sim, prm) if not args.no_surface else None
     render = bench_render(sim, prm) if not args.no_render else None
@@ -672,6 +742,10 @@ def bench_ours(args, scene, world, rank, local):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(scene, {"launch": "CUDA graph replay of each step"}),
+        "start_order": {"presorted": {"ms_per_step": total_ms / args.steps, "value": value},
+                        "unsorted": {"ms_per_step": uns_ms, "value": world * n / (uns_ms / 1e3)},
+                        "note": "value is timed from the cell-sorted configured state; 'unsorted' times the "
+                                "same step from the caller's particle order (state uploaded before each step)"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": None if traffic is None else traffic * n,

@@ -1109,6 +1109,8 @@ pbf_status pbf_get_tuning(pbf_handle* hh, pbf_tuning* out) {
   out->block_nbr = t.block_nbr;
   out->block_solve = t.block_solve;
   out->block_misc = t.block_misc;
+  out->gather_depth = t.gather_depth;
+  out->list_stream = t.list_stream;
   return PBF_OK;
 }
 
@@ -1120,10 +1122,14 @@ pbf_status pbf_set_tuning(pbf_handle* hh, const pbf_tuning* t) {
   if (!valid_block(t->block_predict) || !valid_block(t->block_nbr) || !valid_block(t->block_solve) ||
       !valid_block(t->block_misc))
     return h->fail(PBF_ERR_INVALID, "block sizes must be 64, 128, 256 or 512");
+  if ((t->gather_depth != 4 && t->gather_depth != 8) || (t->list_stream != 0 && t->list_stream != 1))
+    return h->fail(PBF_ERR_INVALID, "gather_depth must be 4 or 8, list_stream 0 or 1");
   h->tune.block_predict = t->block_predict;
   h->tune.block_nbr = t->block_nbr;
   h->tune.block_solve = t->block_solve;
   h->tune.block_misc = t->block_misc;
+  h->tune.gather_depth = t->gather_depth;
+  h->tune.list_stream = t->list_stream;
   h->drop_graphs();
   return PBF_OK;
 }
@@ -1173,21 +1179,28 @@ pbf_status pbf_autotune(pbf_handle* hh, double dt, int reps, pbf_tuning* out) {
   h->params.flags &= ~PBF_FLAG_GRAPH;
   h->drop_graphs();
   h->profiling = true;
-  static const int kCand[4] = {64, 128, 256, 512};
   pbf::Tuning best = h->tune;
+  // one dimension at a time, each timed over the phases it launches, the others held at
+  // their best value so far
   struct Family {
     int* field;
     int phases[4];
+    int cand[4];
+    int ncand;
   } fams[] = {
-      {&best.block_nbr, {pbf::kPhaseNeighbors, -1, -1, -1}},
-      {&best.block_solve, {pbf::kPhaseLambda, pbf::kPhaseDeltaP, pbf::kPhaseXsph, pbf::kPhaseVorticity}},
-      {&best.block_predict, {pbf::kPhasePredict, -1, -1, -1}},
-      {&best.block_misc, {pbf::kPhaseSort, pbf::kPhaseGather, -1, -1}},
+      {&best.block_nbr, {pbf::kPhaseNeighbors, -1, -1, -1}, {64, 128, 256, 512}, 4},
+      {&best.gather_depth, {pbf::kPhaseLambda, pbf::kPhaseDeltaP, pbf::kPhaseXsph, pbf::kPhaseVorticity}, {4, 8}, 2},
+      {&best.list_stream, {pbf::kPhaseLambda, pbf::kPhaseDeltaP, pbf::kPhaseXsph, pbf::kPhaseVorticity}, {0, 1}, 2},
+      {&best.block_solve, {pbf::kPhaseLambda, pbf::kPhaseDeltaP, pbf::kPhaseXsph, pbf::kPhaseVorticity},
+       {64, 128, 256, 512}, 4},
+      {&best.block_predict, {pbf::kPhasePredict, -1, -1, -1}, {64, 128, 256, 512}, 4},
+      {&best.block_misc, {pbf::kPhaseSort, pbf::kPhaseGather, -1, -1}, {64, 128, 256, 512}, 4},
   };
   for (auto& f : fams) {
     double best_ms = 1e300;
     int best_b = *f.field;
-    for (int c : kCand) {
+    for (int ci = 0; ci < f.ncand; ++ci) {
+      const int c = f.cand[ci];
       pbf::Tuning trial = best;
       *reinterpret_cast<int*>(reinterpret_cast<char*>(&trial) +
                               (reinterpret_cast<char*>(f.field) - reinterpret_cast<char*>(&best))) = c;

@@ -430,7 +430,19 @@ __device__ __forceinline__ void for_each_neighbor(int i, int n, const uint4 h,
 // gathers in flight. With D = 8 the next round's list words are loaded before this
 // round's computation, so their latency overlaps it. Calls f(j, load(j)) in the same
 // (ascending) order. D = 2, 4 or 8; DC picks the decode form.
-template <int D, Decode DC = Decode::kBits, typename L, typename F>
+// List words are read once per pass: ST = true loads them with the streaming policy
+// (ld.global.cs, evict-first in L1 and L2), so they displace less of the neighbours' x*
+// that the pass gathers repeatedly.
+template <bool ST>
+__device__ __forceinline__ uint32_t ld_list(const uint32_t* p) {
+  return ST ? __ldcs(p) : __ldg(p);
+}
+template <bool ST>
+__device__ __forceinline__ uint4 ld_hdr(const uint4* p) {
+  return ST ? __ldcs(p) : __ldg(p);
+}
+
+template <int D, Decode DC = Decode::kBits, bool ST = false, typename L, typename F>
 __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h,
                                                      const uint32_t* __restrict__ words, L&& load, F&& f) {
   const int total = nbr_total(h);
@@ -440,13 +452,13 @@ __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h
   if (D == 8) {
     uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u;
     if (total >= 8) {
-      w0 = __ldg(wp); w1 = __ldg(wp + sn); w2 = __ldg(wp + 2 * sn); w3 = __ldg(wp + 3 * sn);
+      w0 = ld_list<ST>(wp); w1 = ld_list<ST>(wp + sn); w2 = ld_list<ST>(wp + 2 * sn); w3 = ld_list<ST>(wp + 3 * sn);
     }
     for (; k + 7 < total; k += 8) {
       wp += 4 * sn;
       uint32_t n0 = 0u, n1 = 0u, n2 = 0u, n3 = 0u;
       if (k + 15 < total) {
-        n0 = __ldg(wp); n1 = __ldg(wp + sn); n2 = __ldg(wp + 2 * sn); n3 = __ldg(wp + 3 * sn);
+        n0 = ld_list<ST>(wp); n1 = ld_list<ST>(wp + sn); n2 = ld_list<ST>(wp + 2 * sn); n3 = ld_list<ST>(wp + 3 * sn);
       }
       const uint32_t j0 = nbr_decode<DC>(h, w0 & 0xffffu), j1 = nbr_decode<DC>(h, w0 >> 16);
       const uint32_t j2 = nbr_decode<DC>(h, w1 & 0xffffu), j3 = nbr_decode<DC>(h, w1 >> 16);
@@ -473,7 +485,7 @@ __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h
   }
   if (D >= 4) {
     for (; k + 3 < total; k += 4) {
-      const uint32_t w0 = __ldg(wp), w1 = __ldg(wp + sn);
+      const uint32_t w0 = ld_list<ST>(wp), w1 = ld_list<ST>(wp + sn);
       wp += 2 * sn;
       const uint32_t j0 = nbr_decode<DC>(h, w0 & 0xffffu), j1 = nbr_decode<DC>(h, w0 >> 16);
       const uint32_t j2 = nbr_decode<DC>(h, w1 & 0xffffu), j3 = nbr_decode<DC>(h, w1 >> 16);
@@ -488,7 +500,7 @@ __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h
     }
   }
   for (; k + 1 < total; k += 2) {
-    const uint32_t w = __ldg(wp);
+    const uint32_t w = ld_list<ST>(wp);
     wp += sn;
     const uint32_t j0 = nbr_decode<DC>(h, w & 0xffffu), j1 = nbr_decode<DC>(h, w >> 16);
     const auto a0 = load(j0);
@@ -497,7 +509,7 @@ __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h
     f(j1, a1);
   }
   if (k < total) {
-    const uint32_t j0 = nbr_decode<DC>(h, __ldg(wp) & 0xffffu);
+    const uint32_t j0 = nbr_decode<DC>(h, ld_list<ST>(wp) & 0xffffu);
     f(j0, load(j0));
   }
 }
@@ -524,20 +536,31 @@ struct Pair {
 // both give +inf at r2 = 0, where hr is 0), so the pair values are the same; the vorticity
 // pass measured faster with it (0.066 against 0.071 ms per step on the 1M colliding
 // blocks), the other passes did not.
+// Every rounding is explicit (_rn intrinsics, fused where written as an fma), so the
+// compiler cannot contract differently in differently unrolled loops: every form of a
+// neighbour pass gives the same bits.
 template <bool FTZ = false>
 __device__ __forceinline__ Pair pair_of(const float4& xi, const float4& xj, float h, float h2) {
   Pair p;
-  p.r = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
-  p.r2 = dot3(p.r, p.r);
-  p.q = fmaxf(h2 - p.r2, 0.0f);
+  p.r = make_float3(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
+  p.r2 = __fmaf_rn(p.r.z, p.r.z, __fmaf_rn(p.r.y, p.r.y, __fmul_rn(p.r.x, p.r.x)));
+  p.q = fmaxf(__fsub_rn(h2, p.r2), 0.0f);
   float rinv;
   if (FTZ)
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rinv) : "f"(p.r2));
   else
     rinv = rsqrtf(p.r2);
-  const float hr = fmaxf(h - p.r2 * rinv, 0.0f);
-  p.s = p.r2 >= kEps * kEps ? hr * hr * rinv : 0.0f;
+  const float hr = fmaxf(__fmaf_rn(-p.r2, rinv, h), 0.0f);
+  p.s = p.r2 >= kEps * kEps ? __fmul_rn(__fmul_rn(hr, hr), rinv) : 0.0f;
   return p;
+}
+
+// acc + a * c per component, one rounding each
+__device__ __forceinline__ float3 fma3(const float3 a, float c, const float3 acc) {
+  return make_float3(__fmaf_rn(a.x, c, acc.x), __fmaf_rn(a.y, c, acc.y), __fmaf_rn(a.z, c, acc.z));
+}
+__device__ __forceinline__ float dot3_rn(const float3 a, const float3 b) {
+  return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x)));
 }
 
 // Spiky gradient factor s with grad W(r) = spiky_c * s * r (particles.cpp:143-149);

@@ -146,12 +146,15 @@ struct SurfGrid {
 void build_table(SurfTable* t);
 const SurfTable& surf_table();
 
-// Launch shapes picked by the autotuner (threads per block per kernel family).
+// Launch shapes and kernel forms picked by the autotuner (threads per block per kernel
+// family; the neighbour passes' gather depth and list-load policy).
 struct Tuning {
   int block_predict = 256;
   int block_nbr = 128;
   int block_solve = 128;
   int block_misc = 256;
+  int gather_depth = 8;  // neighbour loads in flight per thread in the neighbour passes (4 or 8)
+  int list_stream = 0;   // 1: neighbour-list words loaded with the streaming cache policy
 };
 
 // Phases of a step for CUDA-event timing (pbf_get_phase_times).

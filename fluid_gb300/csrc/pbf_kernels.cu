@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
 // ---------------------------------------------------------------------------
 // lambda_i is stored in x*_i.w of the same buffer: within this pass every
 // thread reads only .xyz of its neighbours' x*, which no thread writes.
-template <int BLOCK>
+template <int BLOCK, int D, bool ST>
 __global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs, const uint4* __restrict__ hdr,
                                                   const uint32_t* __restrict__ words,
                                                   float* __restrict__ rho_iter0,
@@ -404,18 +404,19 @@ __global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs, const uint4* __res
   const float4 xi = xs[i];
   float qsum = 0.f, g2 = 0.f;
   float3 gs = make_float3(0.f, 0.f, 0.f);
-  // eight gathers in flight: this pass is bound by the latency of the neighbour loads
-  for_each_neighbor_pf<8>(i, n, hdr[i], words, [&](uint32_t j) -> float4 { return xs[j]; },
-                          [&](uint32_t, const float4& xj) {
+  // D gathers in flight: this pass is bound by the latency of the neighbour loads
+  for_each_neighbor_pf<D, Decode::kBits, ST>(i, n, ld_hdr<ST>(&hdr[i]), words,
+                                              [&](uint32_t j) -> float4 { return xs[j]; },
+                                              [&](uint32_t, const float4& xj) {
     const Pair p = pair_of(xi, xj, P.h, P.h2);
-    qsum += p.q * p.q * p.q;
-    gs = gs + p.r * p.s;
-    g2 += p.s * p.s * p.r2;
+    qsum = __fmaf_rn(__fmul_rn(p.q, p.q), p.q, qsum);
+    gs = fma3(p.r, p.s, gs);
+    g2 = __fmaf_rn(__fmul_rn(p.s, p.s), p.r2, g2);
   });
-  const float rho = P.poly6_c * qsum;
-  const float kg = P.spiky_c * P.inv_rho0;
-  const float denom = kg * kg * (g2 + dot3(gs, gs)) + P.epsilon;
-  const float l = -(rho * P.inv_rho0 - 1.0f) / denom;
+  const float rho = __fmul_rn(P.poly6_c, qsum);
+  const float kg = __fmul_rn(P.spiky_c, P.inv_rho0);
+  const float denom = __fmaf_rn(__fmul_rn(kg, kg), __fadd_rn(g2, dot3_rn(gs, gs)), P.epsilon);
+  const float l = -__fdiv_rn(__fmaf_rn(rho, P.inv_rho0, -1.0f), denom);
   reinterpret_cast<float*>(xs)[4 * i + 3] = l;
   if (rho_iter0) rho_iter0[i] = rho;
 }
@@ -425,7 +426,7 @@ __global__ void __launch_bounds__(BLOCK) k_lambda(float4* xs, const uint4* __res
 // also stores the requested displacement and the collision record in dp_rec. MESH =
 // false (no collider triangles) leaves the triangle tests out of the collision: 40
 // registers a thread instead of 55.
-template <int BLOCK, bool N4, bool REC, bool MESH>
+template <int BLOCK, bool N4, bool REC, bool MESH, int D, bool ST>
 __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
                                                   const float4* __restrict__ pos,
                                                   const uint4* __restrict__ hdr,
@@ -439,22 +440,24 @@ __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
   const float li = xi.w;  // lambda_i (k_lambda stores it in x*.w)
   const float wt = P.poly6_c * P.tis;
   float3 dp = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor_pf<8>(i, n, hdr[i], words, [&](uint32_t j) -> float4 { return __ldg(&xs[j]); },
-                          [&](uint32_t, const float4& xj) {
+  for_each_neighbor_pf<D, Decode::kBits, ST>(i, n, ld_hdr<ST>(&hdr[i]), words,
+                                              [&](uint32_t j) -> float4 { return __ldg(&xs[j]); },
+                                              [&](uint32_t, const float4& xj) {
     const Pair p = pair_of(xi, xj, P.h, P.h2);
-    const float a = wt * (p.q * p.q * p.q);  // W / W(dq)
+    const float a = __fmul_rn(wt, __fmul_rn(__fmul_rn(p.q, p.q), p.q));  // W / W(dq)
     float an;
     if (N4) {
-      const float a2 = a * a;
-      an = a2 * a2;
+      const float a2 = __fmul_rn(a, a);
+      an = __fmul_rn(a2, a2);
     } else {
       an = a;
-      for (int e = 1; e < P.scorr_n; ++e) an *= a;
+      for (int e = 1; e < P.scorr_n; ++e) an = __fmul_rn(an, a);
     }
-    const float coef = (li + xj.w) - P.scorr_k * an;  // lambda_i + lambda_j + s_corr
-    dp = dp + p.r * (coef * p.s);
+    const float coef = __fmaf_rn(-P.scorr_k, an, __fadd_rn(li, xj.w));  // lambda_i + lambda_j + s_corr
+    dp = fma3(p.r, __fmul_rn(coef, p.s), dp);
   });
-  dp = dp * (P.spiky_c * P.inv_rho0);
+  const float sc_dp = __fmul_rn(P.spiky_c, P.inv_rho0);
+  dp = make_float3(__fmul_rn(dp.x, sc_dp), __fmul_rn(dp.y, sc_dp), __fmul_rn(dp.z, sc_dp));
   const float4 x4 = pos[i];
   const SceneDesc& sc = scenes[scene_of_slot(x4)];
   const float4 d4 = disp[i];
@@ -471,7 +474,7 @@ __global__ void __launch_bounds__(BLOCK) k_deltap(const float4* __restrict__ xs,
 // velocity, vorticity, XSPH, reported density; then vorticity confinement
 // ---------------------------------------------------------------------------
 // |omega_i| is stored in x*_i.w of the same buffer (neighbours read only .xyz here).
-template <int BLOCK>
+template <int BLOCK, int D, bool ST>
 __global__ void __launch_bounds__(BLOCK) k_xsph(float4* xs, const float4* __restrict__ disp,
                                                 const uint4* __restrict__ hdr,
                                                 const uint32_t* __restrict__ words,
@@ -487,27 +490,31 @@ __global__ void __launch_bounds__(BLOCK) k_xsph(float4* xs, const float4* __rest
   struct XD {
     float4 x, d;
   };
-  for_each_neighbor_pf<8, Decode::kCompare>(
-      i, n, hdr[i], words, [&](uint32_t j) { return XD{xs[j], __ldg(&disp[j])}; },
+  for_each_neighbor_pf<D, Decode::kCompare, ST>(
+      i, n, ld_hdr<ST>(&hdr[i]), words, [&](uint32_t j) { return XD{xs[j], __ldg(&disp[j])}; },
       [&](uint32_t, const XD& a) {
     const Pair p = pair_of(xi, a.x, P.h, P.h2);
-    const float3 vij = f3(a.d) * inv_dt - vi;
-    const float q3 = p.q * p.q * p.q;
-    visc = visc + vij * q3;
-    qsum += q3;
-    w = w + cross3(vij, p.r * p.s);
+    const float3 vij = make_float3(__fmaf_rn(a.d.x, inv_dt, -vi.x), __fmaf_rn(a.d.y, inv_dt, -vi.y),
+                                   __fmaf_rn(a.d.z, inv_dt, -vi.z));
+    const float q3 = __fmul_rn(__fmul_rn(p.q, p.q), p.q);
+    visc = fma3(vij, q3, visc);
+    qsum = __fadd_rn(qsum, q3);
+    const float3 rs = make_float3(__fmul_rn(p.r.x, p.s), __fmul_rn(p.r.y, p.s), __fmul_rn(p.r.z, p.s));
+    w = make_float3(__fadd_rn(w.x, __fmaf_rn(vij.y, rs.z, -__fmul_rn(vij.z, rs.y))),
+                    __fadd_rn(w.y, __fmaf_rn(vij.z, rs.x, -__fmul_rn(vij.x, rs.z))),
+                    __fadd_rn(w.z, __fmaf_rn(vij.x, rs.y, -__fmul_rn(vij.y, rs.x))));
   });
-  const float rho = P.poly6_c * qsum;
-  w = w * P.spiky_c;
-  const float3 v = vi + visc * (P.xsph_c * P.poly6_c);
+  const float rho = __fmul_rn(P.poly6_c, qsum);
+  w = make_float3(__fmul_rn(w.x, P.spiky_c), __fmul_rn(w.y, P.spiky_c), __fmul_rn(w.z, P.spiky_c));
+  const float3 v = fma3(visc, __fmul_rn(P.xsph_c, P.poly6_c), vi);
   vel_out[i] = make_float4(v.x, v.y, v.z, 0.f);
-  const float wn = sqrtf(dot3(w, w));
+  const float wn = __fsqrt_rn(dot3_rn(w, w));
   omega[i] = make_float4(w.x, w.y, w.z, wn);
   reinterpret_cast<float*>(xs)[4 * i + 3] = wn;
   rho_out[i] = rho;
 }
 
-template <int BLOCK>
+template <int BLOCK, int D, bool ST>
 __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
                                                 float4* __restrict__ pos,
                                                 const float4* __restrict__ omega,
@@ -519,18 +526,24 @@ __global__ void __launch_bounds__(BLOCK) k_vort(const float4* __restrict__ xs,
   if (i >= n) return;
   const float4 xi = xs[i];
   float3 eta = make_float3(0.f, 0.f, 0.f);
-  for_each_neighbor_pf<8>(i, n, hdr[i], words, [&](uint32_t j) -> float4 { return __ldg(&xs[j]); },
-                          [&](uint32_t, const float4& xj) {
+  for_each_neighbor_pf<D, Decode::kBits, ST>(i, n, ld_hdr<ST>(&hdr[i]), words,
+                                              [&](uint32_t j) -> float4 { return __ldg(&xs[j]); },
+                                              [&](uint32_t, const float4& xj) {
     const Pair p = pair_of<true>(xi, xj, P.h, P.h2);
-    eta = eta + p.r * (xj.w * p.s);  // |omega_j| (k_xsph stores it in x*.w)
+    eta = fma3(p.r, __fmul_rn(xj.w, p.s), eta);  // |omega_j| (k_xsph stores it in x*.w)
   });
-  eta = eta * P.spiky_c;
+  eta = make_float3(__fmul_rn(eta.x, P.spiky_c), __fmul_rn(eta.y, P.spiky_c), __fmul_rn(eta.z, P.spiky_c));
   if (eta_rec) eta_rec[i] = make_float4(eta.x, eta.y, eta.z, 0.f);  // recording forward of the adjoint
   float3 v = f3(vel[i]);
-  const float en = sqrtf(dot3(eta, eta));
+  const float en = __fsqrt_rn(dot3_rn(eta, eta));
   if (en > kEps) {
     const float4 wi = omega[i];
-    v = v + cross3(eta * (1.0f / en), f3(wi)) * (dt * P.vort_eps);
+    const float ie = __fdiv_rn(1.0f, en);
+    const float3 nh = make_float3(__fmul_rn(eta.x, ie), __fmul_rn(eta.y, ie), __fmul_rn(eta.z, ie));
+    const float3 c = make_float3(__fmaf_rn(nh.y, wi.z, -__fmul_rn(nh.z, wi.y)),
+                                 __fmaf_rn(nh.z, wi.x, -__fmul_rn(nh.x, wi.z)),
+                                 __fmaf_rn(nh.x, wi.y, -__fmul_rn(nh.y, wi.x)));
+    v = fma3(c, __fmul_rn(dt, P.vort_eps), v);
   }
   const float4 p4 = pos[i];
   vel[i] = make_float4(v.x, v.y, v.z, 0.f);
@@ -772,13 +785,36 @@ __global__ void k_density_at(const float4* __restrict__ pos, const uint32_t* __r
 
 inline unsigned blocks_for(size_t n, int block) { return static_cast<unsigned>((n + block - 1) / block); }
 
+// Launches neighbour kernel KERN (a template-id, parenthesised) over n particles, BLOCK threads a block.
+#define PBF_PASS_LAUNCH(KERN, ...) KERN<<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(__VA_ARGS__)
+
+// Instantiates a neighbour pass for the tuned gather depth (D = 4 or 8 neighbour loads in
+// flight per thread) and list-load policy (ST: streaming). Neither changes the order in
+// which a particle's neighbours are summed, so every form gives the same bits.
+#define PBF_FORM_SWITCH(depth, stream, ...)                                          \
+  if ((depth) == 4) {                                                                \
+    if (stream) { constexpr int D = 4; constexpr bool ST = true; __VA_ARGS__; }      \
+    else { constexpr int D = 4; constexpr bool ST = false; __VA_ARGS__; }            \
+  } else {                                                                           \
+    if (stream) { constexpr int D = 8; constexpr bool ST = true; __VA_ARGS__; }      \
+    else { constexpr int D = 8; constexpr bool ST = false; __VA_ARGS__; }            \
+  }
+
 // One delta-p pass (B = the buffer index holding this step's cell-ordered x and delta).
+// The recording forward of the adjoint keeps the default form (8 deep, cached lists).
 template <bool N4, bool REC, bool MESH>
 void launch_deltap(const Tuning& t, const Buffers& b, int B, float4* xcur, float4* xnext, float4* dprec,
                    const DevParams& P, int n, cudaStream_t s) {
-  PBF_BLOCK_SWITCH(t.block_solve,
-                   (k_deltap<BLOCK, N4, REC, MESH><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                       xcur, b.pos[B], b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, dprec, P, n)));
+  if (REC) {
+    PBF_BLOCK_SWITCH(t.block_solve,
+                     PBF_PASS_LAUNCH((k_deltap<BLOCK, N4, REC, MESH, 8, false>), xcur, b.pos[B], b.nbr_hdr,
+                                     b.nbr_w, b.scenes, b.disp[1], xnext, dprec, P, n));
+    return;
+  }
+  PBF_FORM_SWITCH(t.gather_depth, t.list_stream,
+                  PBF_BLOCK_SWITCH(t.block_solve,
+                                   PBF_PASS_LAUNCH((k_deltap<BLOCK, N4, REC, MESH, D, ST>), xcur, b.pos[B],
+                                                   b.nbr_hdr, b.nbr_w, b.scenes, b.disp[1], xnext, dprec, P, n)));
 }
 
 // Shared front half of a step and of a resort: keys, counts, scan, slots.
@@ -833,17 +869,18 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
     if (e != cudaSuccess) return e;
   }
   if (mk) mk->mark(kPhaseGather, s);
-  PBF_BLOCK_SWITCH(t.block_nbr,
-                   k_nbr_build<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                       xs0, b.pos[B], b.cell_start, b.scenes, b.nbr_hdr, b.nbr_w, b.err, P, n));
+  PBF_BLOCK_SWITCH(t.block_nbr, PBF_PASS_LAUNCH(k_nbr_build<BLOCK>, xs0, b.pos[B], b.cell_start, b.scenes,
+                                                b.nbr_hdr, b.nbr_w, b.err, P, n));
   if (mk) mk->mark(kPhaseNeighbors, s);
   for (int it = 0; it < iters; ++it) {
     float4* xcur = rec ? tape->xs + static_cast<size_t>(it) * b.n : b.xs[it & 1];
     float4* xnext = rec ? tape->xs + static_cast<size_t>(it + 1) * b.n : b.xs[(it + 1) & 1];
     float4* dprec = rec ? tape->dp + static_cast<size_t>(it) * b.n : nullptr;
-    PBF_BLOCK_SWITCH(t.block_solve,
-                     k_lambda<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                         xcur, b.nbr_hdr, b.nbr_w, (it == 0 && P.stats) ? b.rho_iter0 : nullptr, P, n));
+    PBF_FORM_SWITCH(t.gather_depth, t.list_stream,
+                    PBF_BLOCK_SWITCH(t.block_solve,
+                                     PBF_PASS_LAUNCH((k_lambda<BLOCK, D, ST>), xcur, b.nbr_hdr,
+                                                     b.nbr_w, (it == 0 && P.stats) ? b.rho_iter0 : nullptr, P,
+                                                     n)));
     if (mk) mk->mark(kPhaseLambda, s);
     const bool n4 = P.scorr_n == 4, mesh = P.n_mesh > 0;
     if (rec) {  // the adjoint takes box colliders only; the recording keeps the general form
@@ -859,14 +896,16 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
     if (mk) mk->mark(kPhaseDeltaP, s);
   }
   float4* fin = rec ? tape->xs + static_cast<size_t>(iters) * b.n : b.xs[iters & 1];
-  PBF_BLOCK_SWITCH(t.block_solve,
-                   k_xsph<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                       fin, b.disp[1], b.nbr_hdr, b.nbr_w, b.vel[B], b.omega, b.rho, P, 1.0f / dt, n));
+  PBF_FORM_SWITCH(t.gather_depth, t.list_stream,
+                  PBF_BLOCK_SWITCH(t.block_solve,
+                                   PBF_PASS_LAUNCH((k_xsph<BLOCK, D, ST>), fin, b.disp[1],
+                                                   b.nbr_hdr, b.nbr_w, b.vel[B], b.omega, b.rho, P, 1.0f / dt, n)));
   if (mk) mk->mark(kPhaseXsph, s);
-  PBF_BLOCK_SWITCH(t.block_solve,
-                   k_vort<BLOCK><<<blocks_for(n, BLOCK), BLOCK, 0, s>>>(
-                       fin, b.pos[B], b.omega, b.nbr_hdr, b.nbr_w, b.vel[B], b.err, rec ? tape->eta : nullptr,
-                       P, dt, n));
+  PBF_FORM_SWITCH(t.gather_depth, t.list_stream,
+                  PBF_BLOCK_SWITCH(t.block_solve,
+                                   PBF_PASS_LAUNCH((k_vort<BLOCK, D, ST>), fin, b.pos[B], b.omega,
+                                                   b.nbr_hdr, b.nbr_w, b.vel[B], b.err, rec ? tape->eta : nullptr,
+                                                   P, dt, n)));
   if (mk) mk->mark(kPhaseVorticity, s);
   if (P.stats) {
     k_stats<<<kStatsBlocks, 256, 0, s>>>(b.rho, b.rho_iter0, b.nbr_hdr, b.stats_part, P.inv_rho0, n);

@@ -20,7 +20,7 @@ from .params import CParams, PbfParams
 LIB_PATH = Path(os.environ.get("PBF_LIB") or Path(__file__).resolve().parent / "_lib" / "libpbf.so")
 
 PBF_OK = 0
-ABI_VERSION = 5  # PBF_ABI_VERSION of include/pbf.h that these declarations follow
+ABI_VERSION = 6  # PBF_ABI_VERSION of include/pbf.h that these declarations follow
 STATUS = {0: "PBF_OK", 1: "PBF_ERR_INVALID", 2: "PBF_ERR_CUDA", 3: "PBF_ERR_TIMEOUT",
           4: "PBF_ERR_NONFINITE", 5: "PBF_ERR_CAPACITY", 6: "PBF_ERR_NOMEM"}
 
@@ -33,7 +33,8 @@ class PbfError(RuntimeError):
 
 class CTuning(ctypes.Structure):
     _fields_ = [("block_predict", ctypes.c_int32), ("block_nbr", ctypes.c_int32),
-                ("block_solve", ctypes.c_int32), ("block_misc", ctypes.c_int32)]
+                ("block_solve", ctypes.c_int32), ("block_misc", ctypes.c_int32),
+                ("gather_depth", ctypes.c_int32), ("list_stream", ctypes.c_int32)]
 
 
 class CStats(ctypes.Structure):

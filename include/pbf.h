@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define PBF_ABI_VERSION 5
+#define PBF_ABI_VERSION 6
 
 #if defined(__GNUC__)
 #define PBF_API __attribute__((visibility("default")))
@@ -200,22 +200,31 @@ PBF_API pbf_status pbf_reset_phase_times(pbf_handle* h);
 PBF_API int pbf_num_phases(void);
 PBF_API const char* pbf_phase_name(int phase);
 
-/* Launch shapes (threads per block) of the kernel families of a step. */
+/*
+ * Launch shapes (threads per block) of the kernel families of a step, and the
+ * forms of the neighbour kernels. No field changes any result bit: the forms
+ * visit every particle's neighbours in the same order.
+ */
 typedef struct pbf_tuning {
   int32_t block_predict;  /* prediction, cell count */
   int32_t block_nbr;      /* neighbour-set build */
   int32_t block_solve;    /* lambda, delta-p, XSPH/vorticity passes */
   int32_t block_misc;     /* scatter, cell sort, gather */
+  int32_t gather_depth;   /* neighbour loads a thread keeps in flight in the passes: 4 or 8 */
+  int32_t list_stream;    /* 1: the passes load neighbour-list words with the streaming
+                             (evict-first) cache policy, 0: through the read-only cache */
 } pbf_tuning;
 
 PBF_API pbf_status pbf_get_tuning(pbf_handle* h, pbf_tuning* out);
-/* Each block size must be 64, 128, 256 or 512. Drops captured graphs. */
+/* Each block size must be 64, 128, 256 or 512, gather_depth 4 or 8, list_stream 0 or 1.
+ * Drops captured graphs. */
 PBF_API pbf_status pbf_set_tuning(pbf_handle* h, const pbf_tuning* t);
 /*
- * Autotuner: times every candidate block size of each kernel family with
+ * Autotuner: times every candidate of each tuning dimension (the block size of each
+ * kernel family, the passes' gather depth and list policy) with
  * CUDA events over `reps` steps of dt from the current state (checkpointed
  * and restored around every trial, so the state is unchanged on return),
- * keeps the fastest shape per family and reports it in *out (may be NULL).
+ * keeps the fastest candidate per dimension and reports the result in *out (may be NULL).
  */
 PBF_API pbf_status pbf_autotune(pbf_handle* h, double dt, int reps, pbf_tuning* out);
 

@@ -34,6 +34,11 @@ def test_reference_arm_prints_one_contract_line():
     assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 3 and d["n_gpus"] == 1
     assert d["unit"] == "particle-updates/s" and d["higher_is_better"] is True
     assert d["config"]["workload"] == "colliding_blocks_1m"
+    # the line names the sample it ran, not the full scene it was drawn from
+    assert d["config"]["source_particles"] == 1048576
+    assert d["config"]["particles"] % 4096 == 0 and d["config"]["particles"] < 1048576
+    fit = d["extrapolated_1m"]
+    assert fit["kind"] == "extrapolated" and len(fit["measured"]) >= 3 and 0 < fit["value"] < d["value"]
     cb = d["cpu_baseline"]
     assert cb["kind"] == "reference" and cb["cores"] >= 1 and cb["sample"] and cb["value"] == d["value"]
     e = d["e2e"]

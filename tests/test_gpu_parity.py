@@ -308,7 +308,9 @@ def test_autotune_keeps_state_and_results(pbf):
         sim.time_step(sc.params.dt, 2)
         x0 = sim.positions()
         best = sim.autotune(sc.params.dt, reps=2)
-        assert all(v in (64, 128, 256, 512) for v in best.values())
+        assert all(best[k] in (64, 128, 256, 512) for k in ("block_predict", "block_nbr", "block_solve",
+                                                              "block_misc"))
+        assert best["gather_depth"] in (4, 8) and best["list_stream"] in (0, 1)
         assert np.array_equal(sim.positions(), x0)
         sim.time_step(sc.params.dt, 3)
         xa = sim.positions()
@@ -316,6 +318,54 @@ def test_autotune_keeps_state_and_results(pbf):
         sim.set_tuning(block_nbr=512, block_solve=64, block_predict=128, block_misc=64)
         sim.time_step(sc.params.dt, 5)
         assert np.array_equal(sim.positions(), xa)
+
+
+@pytest.mark.parametrize("scene", ["block4096", "batched", "crowded"])
+def test_kernel_forms_give_identical_bits(pbf, scene):
+    """Every tuning form (gather depth 4 and 8, cached and streaming list loads, every block
+    size) visits each particle's neighbours in the same order and rounds every operation
+    explicitly: the neighbour lists and three steps of state are bit-identical across forms."""
+    if scene == "block4096":
+        sc = scenes.block4096(5)
+        pos, vel, prm, kw = _f32(sc.pos), _f32(sc.vel), sc.params, {}
+    elif scene == "batched":
+        b = scenes.batched_256(seed=9, n_scenes=5, lo=500, hi=3000)
+        pos, vel, prm, kw = _f32(b.pos), _f32(b.vel), b.params, {"counts": b.counts, "boxes": b.boxes}
+    else:
+        rng = np.random.default_rng(8)
+        prm = scenes.physical_params(0.1, 0.05, max_neighbors=1023)
+        pos = _f32(np.stack([rng.uniform(0.41, 0.49, 600), rng.uniform(0.01, 0.09, 600),
+                             rng.uniform(0.41, 0.49, 600)], 1))
+        vel, kw = np.zeros_like(pos), {}
+    forms = [dict(gather_depth=8, list_stream=0, block_nbr=128, block_solve=128),
+             dict(gather_depth=8, list_stream=1, block_nbr=128, block_solve=128),
+             dict(gather_depth=4, list_stream=0, block_nbr=128, block_solve=128),
+             dict(gather_depth=4, list_stream=1, block_nbr=64, block_solve=256),
+             dict(gather_depth=8, list_stream=1, block_nbr=512, block_solve=512),
+             dict(gather_depth=4, list_stream=0, block_nbr=256, block_solve=64)]
+    outs = []
+    for f in forms:
+        with pbf.Simulator(pos, vel, prm.with_(flags=PBF_FLAG_STATS), **kw) as sim:
+            sim.set_tuning(**f)
+            sim.time_step(prm.dt, 1)
+            nb = sim.neighbors()
+            sim.time_step(prm.dt, 2)
+            outs.append((nb, sim.positions(), sim.velocities(), sim.densities(), sim.stats()["error_flags"]))
+    for o in outs[1:]:
+        assert np.array_equal(o[0][0], outs[0][0][0]) and np.array_equal(o[0][1], outs[0][0][1])
+        for a, b in zip(o[1:4], outs[0][1:4]):
+            assert np.array_equal(a, b)
+        assert o[4] == outs[0][4] == 0
+
+
+def test_tuning_arguments(pbf):
+    sc = scenes.block4096(1)
+    with pbf.Simulator(_f32(sc.pos), _f32(sc.vel), sc.params) as sim:
+        for bad in (dict(gather_depth=6), dict(gather_depth=0), dict(list_stream=-1), dict(block_nbr=100)):
+            with pytest.raises(pbf.PbfError):
+                sim.set_tuning(**bad)
+        t = sim.tuning()
+        assert t["gather_depth"] in (4, 8) and t["list_stream"] in (0, 1)
 
 
 def test_collider_mesh_matches_oracle(pbf, oracle_lib):
