@@ -1,6 +1,7 @@
 // C ABI of the PBF step (include/pbf.h): handle lifetime, device memory,
 // stream and CUDA-graph management, host/device transfers, introspection.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -167,6 +168,8 @@ void Handle::free_all() {
   surf_hash_bytes = 0;
   if (mesh_dev) cudaFree(mesh_dev);
   mesh_dev = nullptr;
+  if (sph_dev) cudaFree(sph_dev);
+  sph_dev = nullptr;
   render.release();
   snap_pos = snap_vel = nullptr;
   snap_id = nullptr;
@@ -614,7 +617,8 @@ pbf_status pbf_adjoint_step_device(pbf_handle* hh, double dt, const float* xyz, 
   const double d = dt > 0 ? dt : h->params.dt;
   if (!(d > 0) || !std::isfinite(d)) return h->fail(PBF_ERR_INVALID, "dt must be positive");
   if (!g_rho0) return h->fail(PBF_ERR_INVALID, "g_rho0 is NULL");
-  if (h->dp.n_mesh > 0) return h->fail(PBF_ERR_INVALID, "the adjoint step supports the box collider only");
+  if (h->dp.n_mesh > 0 || h->dp.n_sph > 0)
+    return h->fail(PBF_ERR_INVALID, "the adjoint step supports the box collider only");
   if (h->b.n && (!gx_in || !gv_in)) return h->fail(PBF_ERR_INVALID, "gx_in / gv_in is NULL");
   pbf::DeviceGuard g(h->device);
   pbf_status st = h->ensure_tape();
@@ -738,33 +742,120 @@ pbf_status pbf_estimate_densities(pbf_handle* hh, float* rho) {
   return download(h, nullptr, nullptr, rho);
 }
 
+namespace {
+
+// Bounding-volume hierarchy over the collider triangles, built once on the host: median
+// splits of the centroids along their longest extent down to leaves of kMeshLeafSize
+// triangles (depth under kMeshMaxDepth); every node box is widened by 1e-5 of the
+// largest coordinate magnitude and rounded outward to float, so the device's slab test
+// never drops a triangle its exact test would hit.
+struct MeshBuilder {
+  const std::vector<std::array<double, 9>>& tri;
+  std::vector<uint32_t> order;
+  std::vector<std::array<double, 3>> cen;
+  std::vector<float4> nodes;
+
+  explicit MeshBuilder(const std::vector<std::array<double, 9>>& t) : tri(t), order(t.size()), cen(t.size()) {
+    for (size_t k = 0; k < t.size(); ++k) {
+      order[k] = static_cast<uint32_t>(k);
+      for (int a = 0; a < 3; ++a) cen[k][a] = (t[k][a] + t[k][3 + a] + t[k][6 + a]) / 3.0;
+    }
+  }
+
+  static float down(double x) {
+    const float f = static_cast<float>(x);
+    return static_cast<double>(f) > x ? std::nextafter(f, -INFINITY) : f;
+  }
+  static float up(double x) {
+    const float f = static_cast<float>(x);
+    return static_cast<double>(f) < x ? std::nextafter(f, INFINITY) : f;
+  }
+  static float bits(int v) {
+    float f;
+    std::memcpy(&f, &v, sizeof f);
+    return f;
+  }
+
+  int build(size_t first, size_t count, int depth) {
+    const int node = static_cast<int>(nodes.size() / 2);
+    nodes.resize(nodes.size() + 2);
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    double clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    double mag = 1.0;
+    for (size_t k = first; k < first + count; ++k) {
+      const auto& q = tri[order[k]];
+      for (int v = 0; v < 3; ++v)
+        for (int a = 0; a < 3; ++a) {
+          lo[a] = std::min(lo[a], q[3 * v + a]);
+          hi[a] = std::max(hi[a], q[3 * v + a]);
+          mag = std::max(mag, std::fabs(q[3 * v + a]));
+        }
+      for (int a = 0; a < 3; ++a) {
+        clo[a] = std::min(clo[a], cen[order[k]][a]);
+        chi[a] = std::max(chi[a], cen[order[k]][a]);
+      }
+    }
+    const double margin = 1e-5 * mag;
+    int a_ = static_cast<int>(first), b_ = -static_cast<int>(count);
+    if (count > static_cast<size_t>(pbf::kMeshLeafSize) && depth + 1 < pbf::kMeshMaxDepth) {
+      int axis = 0;
+      for (int a = 1; a < 3; ++a)
+        if (chi[a] - clo[a] > chi[axis] - clo[axis]) axis = a;
+      const size_t mid = first + count / 2;
+      std::nth_element(order.begin() + first, order.begin() + mid, order.begin() + first + count,
+                       [&](uint32_t x, uint32_t y) {
+                         return cen[x][axis] < cen[y][axis] || (cen[x][axis] == cen[y][axis] && x < y);
+                       });
+      a_ = build(first, mid - first, depth + 1);
+      b_ = build(mid, first + count - mid, depth + 1);
+    }
+    nodes[2 * node] = make_float4(down(lo[0] - margin), down(lo[1] - margin), down(lo[2] - margin), bits(a_));
+    nodes[2 * node + 1] = make_float4(up(hi[0] + margin), up(hi[1] + margin), up(hi[2] + margin), bits(b_));
+    return node;
+  }
+};
+
+}  // namespace
+
 pbf_status pbf_set_collider_mesh(pbf_handle* hh, size_t n, const float* tri) {
   if (!hh) return PBF_ERR_INVALID;
   Handle* h = reinterpret_cast<Handle*>(hh);
   if (n > static_cast<size_t>(pbf::kMaxMeshTriangles))
-    return h->fail(PBF_ERR_INVALID, "at most 1024 collider triangles");
+    return h->fail(PBF_ERR_INVALID, "at most 4,194,304 collider triangles");
   if (n && !tri) return h->fail(PBF_ERR_INVALID, "tri is NULL");
-  std::vector<float4> packed(4 * n);
+  std::vector<std::array<double, 9>> q(n);
   for (size_t t = 0; t < n; ++t) {
-    double p[3][3];
-    for (int v = 0; v < 3; ++v)
-      for (int k = 0; k < 3; ++k) {
-        p[v][k] = tri[9 * t + 3 * v + k];
-        if (!std::isfinite(p[v][k])) return h->fail(PBF_ERR_INVALID, "collider triangles must be finite");
-      }
+    for (int k = 0; k < 9; ++k) {
+      q[t][k] = tri[9 * t + k];
+      if (!std::isfinite(q[t][k])) return h->fail(PBF_ERR_INVALID, "collider triangles must be finite");
+    }
     double e1[3], e2[3];
     for (int k = 0; k < 3; ++k) {
-      e1[k] = p[1][k] - p[0][k];
-      e2[k] = p[2][k] - p[0][k];
+      e1[k] = q[t][3 + k] - q[t][k];
+      e2[k] = q[t][6 + k] - q[t][k];
+    }
+    const double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    if (!(std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) > 0))
+      return h->fail(PBF_ERR_INVALID, "degenerate collider triangle");
+  }
+  MeshBuilder mb(q);
+  if (n) mb.build(0, n, 0);
+  std::vector<float4> packed(4 * n);
+  for (size_t k = 0; k < n; ++k) {  // leaf order
+    const uint32_t t = mb.order[k];
+    const auto& p = q[t];
+    double e1[3], e2[3];
+    for (int a = 0; a < 3; ++a) {
+      e1[a] = p[3 + a] - p[a];
+      e2[a] = p[6 + a] - p[a];
     }
     const double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
     const double cn = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
-    if (!(cn > 0)) return h->fail(PBF_ERR_INVALID, "degenerate collider triangle");
-    packed[4 * t] = make_float4(static_cast<float>(p[0][0]), static_cast<float>(p[0][1]), static_cast<float>(p[0][2]), 0.f);
-    packed[4 * t + 1] = make_float4(static_cast<float>(e1[0]), static_cast<float>(e1[1]), static_cast<float>(e1[2]), 0.f);
-    packed[4 * t + 2] = make_float4(static_cast<float>(e2[0]), static_cast<float>(e2[1]), static_cast<float>(e2[2]), 0.f);
-    packed[4 * t + 3] = make_float4(static_cast<float>(c[0] / cn), static_cast<float>(c[1] / cn),
-                                    static_cast<float>(c[2] / cn), 0.f);
+    packed[4 * k] = make_float4(static_cast<float>(p[0]), static_cast<float>(p[1]), static_cast<float>(p[2]), 0.f);
+    packed[4 * k + 1] = make_float4(static_cast<float>(e1[0]), static_cast<float>(e1[1]), static_cast<float>(e1[2]), 0.f);
+    packed[4 * k + 2] = make_float4(static_cast<float>(e2[0]), static_cast<float>(e2[1]), static_cast<float>(e2[2]), 0.f);
+    packed[4 * k + 3] = make_float4(static_cast<float>(c[0] / cn), static_cast<float>(c[1] / cn),
+                                    static_cast<float>(c[2] / cn), MeshBuilder::bits(static_cast<int>(t)));
   }
   pbf::DeviceGuard g(h->device);
   pbf_status st = h->cuda(cudaStreamSynchronize(h->stream), "sync");
@@ -773,17 +864,54 @@ pbf_status pbf_set_collider_mesh(pbf_handle* hh, size_t n, const float* tri) {
   h->mesh_dev = nullptr;
   h->dp.n_mesh = 0;
   h->dp.mesh = nullptr;
+  h->dp.mesh_nodes = nullptr;
   if (n) {
-    st = h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->mesh_dev), sizeof(float4) * packed.size()),
-                 "cudaMalloc(mesh)");
+    const size_t bytes = sizeof(float4) * (packed.size() + mb.nodes.size());
+    st = h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->mesh_dev), bytes), "cudaMalloc(mesh)");
     if (st != PBF_OK) return st;
     st = h->cuda(cudaMemcpy(h->mesh_dev, packed.data(), sizeof(float4) * packed.size(), cudaMemcpyHostToDevice),
                  "H2D mesh");
+    if (st == PBF_OK)
+      st = h->cuda(cudaMemcpy(h->mesh_dev + packed.size(), mb.nodes.data(), sizeof(float4) * mb.nodes.size(),
+                              cudaMemcpyHostToDevice),
+                   "H2D mesh hierarchy");
     if (st != PBF_OK) return st;
     h->dp.n_mesh = static_cast<int>(n);
     h->dp.mesh = h->mesh_dev;
+    h->dp.mesh_nodes = h->mesh_dev + packed.size();
   }
   h->drop_graphs();  // the captured steps hold the old parameters
+  return PBF_OK;
+}
+
+pbf_status pbf_set_collider_spheres(pbf_handle* hh, size_t n, const float* xyzr) {
+  if (!hh) return PBF_ERR_INVALID;
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (n > static_cast<size_t>(pbf::kMaxSpheres)) return h->fail(PBF_ERR_INVALID, "at most 1024 collider spheres");
+  if (n && !xyzr) return h->fail(PBF_ERR_INVALID, "xyzr is NULL");
+  std::vector<float4> packed(n);
+  for (size_t k = 0; k < n; ++k) {
+    for (int a = 0; a < 4; ++a)
+      if (!std::isfinite(xyzr[4 * k + a])) return h->fail(PBF_ERR_INVALID, "collider spheres must be finite");
+    if (!(xyzr[4 * k + 3] > 0.f)) return h->fail(PBF_ERR_INVALID, "collider sphere radius must be positive");
+    packed[k] = make_float4(xyzr[4 * k], xyzr[4 * k + 1], xyzr[4 * k + 2], xyzr[4 * k + 3]);
+  }
+  pbf::DeviceGuard g(h->device);
+  pbf_status st = h->cuda(cudaStreamSynchronize(h->stream), "sync");
+  if (st != PBF_OK) return st;
+  if (h->sph_dev) cudaFree(h->sph_dev);
+  h->sph_dev = nullptr;
+  h->dp.n_sph = 0;
+  h->dp.sph = nullptr;
+  if (n) {
+    st = h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->sph_dev), sizeof(float4) * n), "cudaMalloc(spheres)");
+    if (st == PBF_OK)
+      st = h->cuda(cudaMemcpy(h->sph_dev, packed.data(), sizeof(float4) * n, cudaMemcpyHostToDevice), "H2D spheres");
+    if (st != PBF_OK) return st;
+    h->dp.n_sph = static_cast<int>(n);
+    h->dp.sph = h->sph_dev;
+  }
+  h->drop_graphs();
   return PBF_OK;
 }
 

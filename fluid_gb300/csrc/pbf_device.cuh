@@ -91,31 +91,135 @@ __device__ __forceinline__ float3 predict_delta(const float4& v4, const DevParam
   return v * dt;
 }
 
-// Nearest collider-mesh triangle hit by p + s dir, s in [0, tmax] (Moller-Trumbore as
-// MarchingTriangle::intersect, static_scene/marching_triangle.cpp:21-45, with the
-// triangle's normal at all three vertices). Returns s, or tmax when nothing is hit.
+// Moller-Trumbore test of triangle m (MarchingTriangle::intersect,
+// static_scene/marching_triangle.cpp:21-45) against p + s dir, s in [0, t]: on a hit
+// (s <= t) sets t = s, *best = the triangle's index as given and *nrm its normal. Of
+// hits at the same s the one with the larger index wins, which is what a scan of the
+// triangles in index order that keeps the last hit with s <= t gives.
+__device__ __forceinline__ void tri_test(int m, const float3 p, const float3 dir, const DevParams& P, float& t,
+                                         int& best, float3* nrm) {
+  const float4 a = __ldg(&P.mesh[4 * m]), b = __ldg(&P.mesh[4 * m + 1]), c = __ldg(&P.mesh[4 * m + 2]);
+  const float3 e1 = f3(b), e2 = f3(c), sv = p - f3(a);
+  const float3 s1 = cross3(dir, e2), s2 = cross3(sv, e1);
+  const float den = dot3(s1, e1);
+  if (den == 0.0f) return;
+  const float tt = dot3(s2, e2) / den;
+  if (tt < 0.0f || tt > t) return;
+  const float u = dot3(s1, sv) / den, v = dot3(s2, dir) / den, w = 1.0f - u - v;
+  if (u < 0.0f || u > 1.0f || v < 0.0f || v > 1.0f || w < 0.0f || w > 1.0f) return;
+  const float4 nn = __ldg(&P.mesh[4 * m + 3]);
+  const int idx = __float_as_int(nn.w);
+  if (tt == t && idx < best) return;
+  t = tt;
+  best = idx;
+  *nrm = f3(nn);
+}
+
+// Whether the segment p + s dir, s in [0, t], meets the box [lo, hi] (slab test; boxes are
+// stored widened, so rounding here never drops a triangle the exact test would hit).
+__device__ __forceinline__ bool seg_box(const float3 p, const float3 dir, float t, const float4 lo, const float4 hi) {
+  float t0 = 0.0f, t1 = t;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float o = cmp3(p, a), d = cmp3(dir, a);
+    const float l = a == 0 ? lo.x : (a == 1 ? lo.y : lo.z), h = a == 0 ? hi.x : (a == 1 ? hi.y : hi.z);
+    if (d == 0.0f) {
+      if (o < l || o > h) return false;
+    } else {
+      const float inv = 1.0f / d;
+      float ta = (l - o) * inv, tb = (h - o) * inv;
+      if (ta > tb) {
+        const float x = ta;
+        ta = tb;
+        tb = x;
+      }
+      t0 = fmaxf(t0, ta);
+      t1 = fminf(t1, tb);
+      if (t0 > t1) return false;
+    }
+  }
+  return true;
+}
+
+// Nearest collider-mesh triangle hit by p + s dir, s in [0, tmax]: a walk of the
+// hierarchy (one stack entry per level, its depth bounded by the build) testing the
+// triangles of the leaves the segment meets, with the same per-triangle arithmetic and
+// the same winner as a scan of all triangles. Returns s, or tmax when nothing is hit.
 __device__ __forceinline__ float mesh_hit(const float3 p, const float3 dir, float tmax, const DevParams& P,
                                           float3* nrm, bool* hit) {
   float t = tmax;
+  int best = -1;
+  int stack[kMeshMaxDepth];
+  int sp = 0, node = 0;
+  for (;;) {
+    const float4 lo = __ldg(&P.mesh_nodes[2 * node]), hi = __ldg(&P.mesh_nodes[2 * node + 1]);
+    if (seg_box(p, dir, t, lo, hi)) {
+      const int a = __float_as_int(lo.w), b = __float_as_int(hi.w);
+      if (b < 0) {
+        for (int m = a; m < a - b; ++m) tri_test(m, p, dir, P, t, best, nrm);
+      } else {
+        if (sp < kMeshMaxDepth) stack[sp++] = b;
+        node = a;
+        continue;
+      }
+    }
+    if (sp == 0) break;
+    node = stack[--sp];
+  }
+  *hit = best >= 0;
+  return t;
+}
+
+// Nearest collider sphere hit by p + s dir, s in [0, tmax] (Sphere::test and
+// Sphere::intersect, static_scene/sphere.cpp:10-72: the nearer root in range, else the
+// farther; the normal points from the centre to the hit point). Returns s, or tmax.
+__device__ __forceinline__ float sphere_hit(const float3 p, const float3 dir, float tmax, const DevParams& P,
+                                            float3* nrm, bool* hit) {
+  float t = tmax;
   *hit = false;
-  for (int m = 0; m < P.n_mesh; ++m) {
-    const float4 a = __ldg(&P.mesh[4 * m]), b = __ldg(&P.mesh[4 * m + 1]), c = __ldg(&P.mesh[4 * m + 2]);
-    const float3 e1 = f3(b), e2 = f3(c), sv = p - f3(a);
-    const float3 s1 = cross3(dir, e2), s2 = cross3(sv, e1);
-    const float den = dot3(s1, e1);
-    if (den == 0.0f) continue;
-    const float tt = dot3(s2, e2) / den;
-    if (tt < 0.0f || tt > t) continue;
-    const float u = dot3(s1, sv) / den, v = dot3(s2, dir) / den, w = 1.0f - u - v;
-    if (u < 0.0f || u > 1.0f || v < 0.0f || v > 1.0f || w < 0.0f || w > 1.0f) continue;
+  for (int k = 0; k < P.n_sph; ++k) {
+    const float4 c4 = __ldg(&P.sph[k]);
+    const float3 m = p - f3(c4);
+    const float a = dot3(dir, dir);
+    const float b = 2.0f * dot3(m, dir);
+    const float c = dot3(m, m) - c4.w * c4.w;
+    const float delta = b * b - 4.0f * a * c;
+    if (delta < 0.0f) continue;
+    const float sq = sqrtf(delta);
+    float tt = (-b - sq) / (2.0f * a);
+    if (!(tt >= 0.0f && tt <= t)) {
+      tt = (-b + sq) / (2.0f * a);
+      if (!(tt >= 0.0f && tt <= t)) continue;
+    }
     t = tt;
     *hit = true;
-    *nrm = f3(__ldg(&P.mesh[4 * m + 3]));
+    const float3 q = (p + dir * tt) - f3(c4);
+    *nrm = q * rsqrtf(dot3(q, q));
   }
   return t;
 }
 
-// Distance to keep from a mesh triangle after a stop (the reference backs off by EPS_D =
+// The nearest of the collider's mesh triangles and spheres (on equal distance the
+// triangle); returns s, or tmax when neither is hit.
+__device__ __forceinline__ float prim_hit(const float3 p, const float3 dir, float tmax, const DevParams& P,
+                                          float3* nrm, bool* hit) {
+  float t = tmax;
+  *hit = false;
+  if (P.n_sph > 0) t = sphere_hit(p, dir, t, P, nrm, hit);
+  if (P.n_mesh > 0) {
+    float3 mn;
+    bool mh;
+    const float tm = mesh_hit(p, dir, t, P, &mn, &mh);
+    if (mh) {
+      t = tm;
+      *nrm = mn;
+      *hit = true;
+    }
+  }
+  return t;
+}
+
+// Distance to keep from a collider triangle or sphere after a stop (the reference backs off by EPS_D =
 // 1e-11 in FP64, below FP32 resolution): 4 ulps of the point's largest coordinate.
 __device__ __forceinline__ float mesh_backoff(const float3 p) {
   return 4.0f * 1.1920929e-7f * fmaxf(1.0f, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
@@ -171,10 +275,11 @@ __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 
   uint32_t rc = kCollFree;
   int wall;
   const float t = wall_hit(p, dir, l, sc, P.open_mask, &wall);
-  if (MESH && P.n_mesh > 0) {  // a collider triangle nearer than the wall or clip plane stops the move instead
+  if (MESH && (P.n_mesh > 0 || P.n_sph > 0)) {  // a collider triangle or sphere nearer than the wall or
+                                                  // clip plane stops the move instead
     float3 mn;
     bool mh;
-    const float tm = mesh_hit(p, dir, t, P, &mn, &mh);
+    const float tm = prim_hit(p, dir, t, P, &mn, &mh);
     if (mh && tm < t) {
       float3 nd = d + dir * fmaxf(tm - mesh_backoff(p), 0.0f);
       // slide as clamp_response does (particles.cpp:118-124): half the remaining length along
@@ -190,7 +295,7 @@ __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 
           const float t2 = wall_hit(p1, dir2, l2, sc, P.open_mask, &wall2);
           float3 mn2;
           bool mh2;
-          const float tm2 = mesh_hit(p1, dir2, t2, P, &mn2, &mh2);
+          const float tm2 = prim_hit(p1, dir2, t2, P, &mn2, &mh2);
           if (mh2 && tm2 < t2) {
             nd = nd + dir2 * fmaxf(tm2 - mesh_backoff(p1), 0.0f);
           } else {
@@ -237,10 +342,11 @@ __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 
           int wall2;
           const float3 p1 = x + nd;
           const float t2 = wall_hit(p1, dir2, l2, sc, P.open_mask, &wall2);
-          if (MESH && P.n_mesh > 0) {  // the slide stops at a collider triangle before the wall
+          if (MESH && (P.n_mesh > 0 || P.n_sph > 0)) {  // the slide stops at a collider triangle or
+                                                        // sphere before the wall
             float3 mn2;
             bool mh2;
-            const float tm2 = mesh_hit(p1, dir2, t2, P, &mn2, &mh2);
+            const float tm2 = prim_hit(p1, dir2, t2, P, &mn2, &mh2);
             if (mh2 && tm2 < t2) {
               d = nd + dir2 * fmaxf(tm2 - mesh_backoff(p1), 0.0f);
               if (REC) *code = kCollNone;  // not recorded: the adjoint takes box colliders only

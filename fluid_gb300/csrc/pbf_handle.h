@@ -61,7 +61,8 @@ struct Handle {
   SurfTable* surf_table_dev = nullptr;  // marching-cubes table (first pbf_surface)
   void* surf_hash = nullptr;            // grow-only scratch of the surface's vertex-normal table
   size_t surf_hash_bytes = 0;
-  float4* mesh_dev = nullptr;           // collider triangles (pbf_set_collider_mesh)
+  float4* mesh_dev = nullptr;           // collider triangles and their hierarchy (pbf_set_collider_mesh)
+  float4* sph_dev = nullptr;            // collider spheres (pbf_set_collider_spheres)
   RenderState render;                   // path tracer (pbf_render_set_scene, pbf_render)
   double phase_ms[kNumPhases] = {};
   uint64_t phase_launches[kNumPhases] = {};

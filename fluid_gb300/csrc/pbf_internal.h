@@ -52,9 +52,18 @@ struct DevParams {
   int scorr_n, n_clip, clip_axis[2], open_mask, max_words;
   int stats;
   int n_mesh;                // collider triangles besides the box walls (pbf_set_collider_mesh)
-  const float4* mesh;        // 4 float4 per triangle: p1, p2 - p1, p3 - p1, normal
+  const float4* mesh;        // 4 float4 per triangle, in hierarchy leaf order: p1, p2 - p1,
+                             // p3 - p1, normal (w: the triangle's index as given, int bits)
+  const float4* mesh_nodes;  // bounding-volume hierarchy over the triangles, 2 float4 per node:
+                             // lo (w: a), hi (w: b) as int bits; b < 0: leaf of triangles
+                             // [a, a - b), else children a and b; node 0 is the root
+  int n_sph;                 // collider spheres (pbf_set_collider_spheres)
+  const float4* sph;         // centre xyz, radius w
 };
-constexpr int kMaxMeshTriangles = 1024;
+constexpr int kMaxMeshTriangles = 1 << 22;
+constexpr int kMaxSpheres = 1024;
+constexpr int kMeshLeafSize = 4;     // triangles per hierarchy leaf (at most)
+constexpr int kMeshMaxDepth = 40;    // hierarchy depth bound (the walk's stack holds one entry per level)
 
 // Step statistics accumulated on the device (reset every step).
 struct DevStats {

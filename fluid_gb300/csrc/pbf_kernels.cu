@@ -882,7 +882,7 @@ cudaError_t launch_step(const Buffers& b, const DevParams& P, const Tuning& t, i
                                                      b.nbr_w, (it == 0 && P.stats) ? b.rho_iter0 : nullptr, P,
                                                      n)));
     if (mk) mk->mark(kPhaseLambda, s);
-    const bool n4 = P.scorr_n == 4, mesh = P.n_mesh > 0;
+    const bool n4 = P.scorr_n == 4, mesh = P.n_mesh > 0 || P.n_sph > 0;
     if (rec) {  // the adjoint takes box colliders only; the recording keeps the general form
       if (n4) launch_deltap<true, true, true>(t, b, B, xcur, xnext, dprec, P, n, s);
       else launch_deltap<false, true, true>(t, b, B, xcur, xnext, dprec, P, n, s);

@@ -16,18 +16,21 @@
 //   p.ps[i]->velocity, getDensityBasedColor(), p.estimateDensityAt(pos)
 //   p.updateSurface(); p.surface; p.getSurfacePrims(iso, step)   // marching cubes
 //   p.setColliderMesh(vertices)                                   // the BVH's triangles
+//   p.setColliderSpheres(centres, radii)                           // the BVH's spheres
+//   p.paramsString()                                              // the constants, as printed
 //
 // Differences, by design: the collider is the axis-aligned box of the pbf_params plus the
-// triangles given to setColliderMesh (the reference casts rays against a BVH of the
-// scene's primitives; `bvh` is kept as an opaque, unused pointer); the XSPH pass is
-// order-independent; positions, velocities and densities are FP32 on the device and
-// mirrored into V after
-// every step; Particle::neighbors stays empty (neighbour sets live on the device,
-// see pbf_get_neighbors). Errors throw std::runtime_error with pbf_last_error().
+// triangles and spheres given to setColliderMesh / setColliderSpheres (the reference casts
+// rays against a BVH of the scene's primitives; `bvh` is kept as an opaque, unused
+// pointer); the XSPH pass is order-independent; positions, velocities and densities are
+// FP32 on the device and mirrored into V after every step; Particle::neighbors stays empty
+// (neighbour sets live on the device, see pbf_get_neighbors). Errors throw
+// std::runtime_error with pbf_last_error().
 #pragma once
 
 #include <cstdio>
 #include <iostream>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -172,6 +175,8 @@ class Particles {
   }
 
   // particles.cpp:387-395: isolevel 0.95 rest density, step 0.5 H, once per time step.
+  // The reference's updateSurface then takes one step of DEFAULT_DELTA_T (:397); this one
+  // does not (its callers step themselves); tests/dropin/particles.h keeps that step.
   void updateSurface() {
     if (surfaceUpToTimestep) return;
     surface = getSurfacePrims(0.95 * rest_density, 0.5 * prm_.h);
@@ -188,6 +193,43 @@ class Particles {
       mesh_[3 * k + 2] = static_cast<float>(vertices[k].z);
     }
     if (h_ && !dirty_) check(pbf_set_collider_mesh(h_, mesh_.size() / 9, mesh_.data()));
+  }
+
+  // Solid spheres the particles collide with (the reference's Sphere primitives in its
+  // scene's BVH, static_scene/sphere.cpp): one centre and one radius each.
+  void setColliderSpheres(const std::vector<V>& centres, const std::vector<double>& radii) {
+    if (centres.size() != radii.size()) throw std::invalid_argument("one radius per sphere centre");
+    spheres_.assign(4 * centres.size(), 0.f);
+    for (size_t k = 0; k < centres.size(); ++k) {
+      spheres_[4 * k] = static_cast<float>(centres[k].x);
+      spheres_[4 * k + 1] = static_cast<float>(centres[k].y);
+      spheres_[4 * k + 2] = static_cast<float>(centres[k].z);
+      spheres_[4 * k + 3] = static_cast<float>(radii[k]);
+    }
+    if (h_ && !dirty_) check(pbf_set_collider_spheres(h_, spheres_.size() / 4, spheres_.data()));
+  }
+
+  // particles.cpp:420-438: the step's and the surface's parameters, printed as the
+  // reference prints them (its labels, default stream formatting); the visualisation
+  // radius, bounce factor and marching-cube ratios are the reference's constants.
+  std::string paramsString() const {
+    std::ostringstream ss;
+    ss << "Fluid simulation parameters: " << std::endl
+       << "\tTime step: " << prm_.dt << std::endl
+       << "\tSPH Density estimate radius H: " << prm_.h << std::endl
+       << "\tNewton steps: " << prm_.iters << std::endl
+       << "\tConstraint relaxation epsilon: " << prm_.epsilon << std::endl
+       << "\tTensile artificial pressure coefficient K: " << prm_.scorr_k << std::endl
+       << "\tTensile artificial pressure exponent N: " << prm_.scorr_n << std::endl
+       << "\tVorticity confinement coefficient epsilon: " << prm_.vort_eps << std::endl
+       << "\tViscosity coefficient C: " << prm_.xsph_c << std::endl
+       << "\tParticle visualization radius: " << 0.05 << std::endl
+       << "\tCollision response velocity factor: " << 0.6 << std::endl
+       << "Marching cube parameters: " << std::endl
+       << "\tIso-level / rest density ratio: " << 0.95 << std::endl
+       << "\tGradient estimateion epsilon: " << 0.001 << std::endl
+       << "\tStepsize / H ratio: " << 0.5 << std::endl;
+    return ss.str();
   }
 
   const pbf_params& params() const { return prm_; }
@@ -211,7 +253,8 @@ class Particles {
   bool dirty_ = true;
   bool verbose_ = false;
   int device_ = 0;
-  std::vector<float> mesh_;  // collider triangles, 9 floats each
+  std::vector<float> mesh_;     // collider triangles, 9 floats each
+  std::vector<float> spheres_;  // collider spheres: centre, radius
 
   void check(pbf_status st) const {
     if (st != PBF_OK) throw std::runtime_error(std::string("pbf: ") + pbf_last_error(h_));
@@ -241,6 +284,7 @@ class Particles {
     h_ = h;
     dirty_ = false;
     if (!mesh_.empty()) check(pbf_set_collider_mesh(h_, mesh_.size() / 9, mesh_.data()));
+    if (!spheres_.empty()) check(pbf_set_collider_spheres(h_, spheres_.size() / 4, spheres_.data()));
   }
 
   // Mirror device state into the Particle objects (original order).

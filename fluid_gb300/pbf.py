@@ -134,6 +134,7 @@ def _declare(L):
         "pbf_surface": (st, [P, ctypes.c_double, ctypes.c_double, P, P, P, P, sz, P]),
         "pbf_mc_table": (None, [P, P, P]),
         "pbf_set_collider_mesh": (st, [P, sz, P]),
+        "pbf_set_collider_spheres": (st, [P, sz, P]),
         "pbf_get_state": (st, [P, P, P, P]),
         "pbf_render_params_default": (None, [P]),
         "pbf_camera_frame": (st, [P, ctypes.c_uint32, ctypes.c_uint32, P]),
@@ -320,6 +321,14 @@ class Simulator:
             return
         t = np.ascontiguousarray(tri, dtype=np.float32).reshape(-1, 9)
         self._check(lib().pbf_set_collider_mesh(self._h, t.shape[0], _ptr(t)))
+
+    def set_collider_spheres(self, xyzr=None):
+        """Collider spheres: (m, 4) centre x, y, z and radius (None or empty removes them)."""
+        if xyzr is None or len(xyzr) == 0:
+            self._check(lib().pbf_set_collider_spheres(self._h, 0, None))
+            return
+        q = np.ascontiguousarray(xyzr, dtype=np.float32).reshape(-1, 4)
+        self._check(lib().pbf_set_collider_spheres(self._h, q.shape[0], _ptr(q)))
 
     def surface(self, iso: float | None = None, step: float | None = None, lo=None, hi=None):
         """Particles::getSurfacePrims (particles.cpp:352-385) on the current state: the

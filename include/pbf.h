@@ -301,15 +301,27 @@ PBF_API pbf_status pbf_surface(pbf_handle* h, double isolevel, double step, cons
 /*
  * pbf_set_collider_mesh -- triangles the particles collide with besides the box walls,
  * as the reference's colliders are the triangles of its scene's BVH (clamp and
- * clamp_response, particles.cpp:51-132). tri: n triangles of 9 floats (p1, p2, p3, host
- * memory); each triangle's normal is unit((p2 - p1) x (p3 - p1)), used for the slide of
- * the predicted move. A move stops at the nearest wall, clip plane or triangle; after a
- * triangle stop the particle keeps 4 FP32 ulps from it (the reference keeps EPS_D =
- * 1e-11, below FP32 resolution). n = 0 removes the mesh. At most 1024 triangles, each
- * tested by every ray (no hierarchy). pbf_adjoint_step_device refuses a handle with a
- * mesh (its collision reverse is for axis-aligned walls).
+ * clamp_response, particles.cpp:51-132; BVHAccel::intersect, bvh.cpp:142-192). tri: n
+ * triangles of 9 floats (p1, p2, p3, host memory); each triangle's normal is
+ * unit((p2 - p1) x (p3 - p1)), used for the slide of the predicted move. A move stops at
+ * the nearest wall, clip plane, triangle or sphere; after a triangle or sphere stop the
+ * particle keeps 4 FP32 ulps from it (the reference keeps EPS_D = 1e-11, below FP32
+ * resolution). The triangles go into a bounding-volume hierarchy built here, on the
+ * host; a move tests the triangles of the leaves its segment meets, and of hits at the
+ * same distance the triangle given last wins (as in a scan of all of them). n = 0
+ * removes the mesh. At most 4,194,304 triangles. pbf_adjoint_step_device refuses a
+ * handle with a mesh or spheres (its collision reverse is for axis-aligned walls).
  */
 PBF_API pbf_status pbf_set_collider_mesh(pbf_handle* h, size_t n, const float* tri);
+
+/*
+ * pbf_set_collider_spheres -- solid spheres the particles collide with, the reference's
+ * Sphere primitives (static_scene/sphere.cpp:10-72: the nearer intersection in range,
+ * else the farther; the normal from the centre to the hit point). xyzr: n spheres of 4
+ * floats (centre x, y, z, radius > 0; host memory). n = 0 removes them. At most 1024,
+ * each tested by every move.
+ */
+PBF_API pbf_status pbf_set_collider_spheres(pbf_handle* h, size_t n, const float* xyzr);
 
 /*
  * pbf_mc_table -- the triangulation table pbf_surface uses (no GPU needed): for each of

@@ -74,6 +74,8 @@ def lib(fp32: bool = False, adjoint: bool = False):
         L.orc_max_threads.restype = ctypes.c_int
         L.orc_set_mesh.argtypes = [ctypes.c_int64, P]
         L.orc_set_mesh.restype = ctypes.c_int
+        L.orc_set_spheres.argtypes = [ctypes.c_int64, P]
+        L.orc_set_spheres.restype = ctypes.c_int
         L.orc_surface.argtypes = [P, ctypes.c_int64, P, ctypes.c_double, ctypes.c_double, P, P, P, P, P, P, P,
                                   ctypes.c_int64, ctypes.c_int]
         L.orc_surface.restype = ctypes.c_int64
@@ -243,7 +245,19 @@ def set_mesh(tri=None, fp32: bool = False) -> None:
         return
     t = np.ascontiguousarray(tri, dtype=np.float64).reshape(-1, 9)
     if L.orc_set_mesh(t.shape[0], _ptr(t)) != 0:
-        raise ValueError("at most 1024 collider triangles")
+        raise ValueError("at most 65536 collider triangles")
+
+
+def set_spheres(xyzr=None, fp32: bool = False) -> None:
+    """Collider spheres ((m, 4) centre and radius, None to clear) for the following calls
+    (process-wide in the restatement, like the mesh)."""
+    L = lib(fp32)
+    if xyzr is None or len(xyzr) == 0:
+        L.orc_set_spheres(0, None)
+        return
+    q = np.ascontiguousarray(xyzr, dtype=np.float64).reshape(-1, 4)
+    if L.orc_set_spheres(q.shape[0], _ptr(q)) != 0:
+        raise ValueError("at most 1024 collider spheres")
 
 
 def surface(pos, params: PbfParams, ntri, tri, iso: float | None = None, step: float | None = None,

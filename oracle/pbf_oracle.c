@@ -22,6 +22,9 @@
  *     reference's clamp (particles.cpp:76) uses BVHAccel::intersect(const
  *     Ray&), which returns the first hit in BVH order (src/bvh.cpp:142-160);
  *     the two differ only when one displacement crosses two walls.
+ *   - collider spheres (orc_set_spheres) are the reference's Sphere primitives
+ *     (src/static_scene/sphere.cpp:10-72), tested after the triangles in the same
+ *     nearest-hit scan;
  *   - gravity is a 3-vector applied per non-zero component (the reference
  *     subtracts 10*dt from v.y, particles.cpp:180).
  * Parallel over particles with OpenMP; every phase is order-independent so the
@@ -78,8 +81,9 @@ static inline real intpow(real b, int e) {
   return r;
 }
 
-#define ORC_MAX_MESH 1024
+#define ORC_MAX_MESH 65536
 #define ORC_MAX_TRI (12 + ORC_MAX_MESH)
+#define ORC_MAX_SPH 1024
 
 typedef struct {
   real h, h2, h6, h9, tis;
@@ -92,6 +96,9 @@ typedef struct {
   int ntri;
   v3 tp[ORC_MAX_TRI][3];  /* the box walls (up to 12), then the collider mesh */
   v3 tn[ORC_MAX_TRI];
+  int nsph;
+  v3 so[ORC_MAX_SPH];     /* collider spheres: centre, radius */
+  real sr[ORC_MAX_SPH];
 } ctx_t;
 
 /* poly6_kernel, particles.cpp:134-141 */
@@ -161,10 +168,40 @@ static int tri_hit(const ctx_t* c, int t, ray_t* r, v3* nrm) {
   return 1;
 }
 
-/* Nearest hit over all triangles; updates r->max_t, *nrm. */
+/* Sphere::test and Sphere::intersect(const Ray&, Intersection*), static_scene/sphere.cpp:10-72:
+ * the nearer root if it lies in [min_t, max_t], else the farther; the normal is the unit
+ * vector from the centre to the hit point. */
+static int sph_hit(const ctx_t* c, int s, ray_t* r, v3* nrm) {
+  const v3 o = c->so[s];
+  const real r2 = c->sr[s] * c->sr[s];
+  real a = dot(r->d, r->d);
+  v3 m = vsub(r->o, o);
+  real b = 2 * dot(m, r->d);
+  real cc = dot(m, m) - r2;
+  real delta = b * b - 4 * a * cc;
+  if (delta < 0) return 0;
+  real t1;
+  real t = (-b - sqrt(delta)) / (2 * a);
+  if ((t >= r->min_t) && (t <= r->max_t)) {
+    t1 = t;
+  } else {
+    t = (-b + sqrt(delta)) / (2 * a);
+    if ((t >= r->min_t) && (t <= r->max_t)) {
+      t1 = t;
+    } else {
+      return 0;
+    }
+  }
+  r->max_t = t1;
+  if (nrm) *nrm = unit(vsub(vadd(r->o, svmul(t1, r->d)), o));
+  return 1;
+}
+
+/* Nearest hit over all triangles, then all spheres; updates r->max_t, *nrm. */
 static int scene_hit(const ctx_t* c, ray_t* r, v3* nrm) {
   int hit = 0;
   for (int t = 0; t < c->ntri; t++) hit |= tri_hit(c, t, r, nrm);
+  for (int s = 0; s < c->nsph; s++) hit |= sph_hit(c, s, r, nrm);
   return hit;
 }
 
@@ -341,7 +378,24 @@ int orc_set_mesh(int64_t n, const double* tri) {
   return 0;
 }
 
+/* Collider spheres (orc_set_spheres): the reference's Sphere primitives in the same BVH.
+ * Process-wide, like the mesh. */
+static int64_t g_sph_n = 0;
+static double g_sph[4 * ORC_MAX_SPH];
+
+int orc_set_spheres(int64_t n, const double* xyzr) {
+  if (n < 0 || n > ORC_MAX_SPH) return -1;
+  g_sph_n = n;
+  if (n) memcpy(g_sph, xyzr, sizeof(double) * 4 * (size_t)n);
+  return 0;
+}
+
 static void add_mesh(ctx_t* c) {
+  c->nsph = (int)g_sph_n;
+  for (int64_t s = 0; s < g_sph_n; s++) {
+    c->so[s] = V(g_sph[4 * s], g_sph[4 * s + 1], g_sph[4 * s + 2]);
+    c->sr[s] = g_sph[4 * s + 3];
+  }
   for (int64_t m = 0; m < g_mesh_n; m++) {
     const double* q = g_mesh + 9 * m;
     v3 p1 = V(q[0], q[1], q[2]), p2 = V(q[3], q[4], q[5]), p3 = V(q[6], q[7], q[8]);

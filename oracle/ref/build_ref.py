@@ -44,6 +44,7 @@ REF_TUS = [
     "src/bvh.cpp",
     "src/bbox.cpp",
     "src/static_scene/marching_triangle.cpp",
+    "src/static_scene/sphere.cpp",
     "src/marching.cpp",
     "src/bsdf.cpp",
     "src/sampler.cpp",

@@ -29,7 +29,11 @@
 // (appended: i64 ntri, f64 xyz[9 ntri], f64 nrm[9 ntri], i64 cube[ntri]),
 // 32 = collider mesh: the input continues with i64 m, f64 tri[9 m]; each
 // triangle joins the box in the BVH as a MarchingTriangle with the normal
-// ((p2 - p1) x (p3 - p1)).unit() at its three vertices.
+// ((p2 - p1) x (p3 - p1)).unit() at its three vertices,
+// 64 = collider spheres: the input continues with i64 m, f64 xyzr[4 m]; each sphere
+// joins the BVH as the reference's Sphere primitive (static_scene/sphere.cpp).
+// --params-string: construct Particles with the default constants (its constructor
+// prints paramsString()) and exit.
 // open_mask: bit per box face to leave out (0 x-lo, 1 x-hi, 2 y-lo, 3 y-hi,
 // 4 z-lo, 5 z-hi).
 #include <chrono>
@@ -47,6 +51,8 @@
 #include "ref_params.h"
 #include "ref_surface.h"
 #include "static_scene/marching_triangle.h"
+#include "static_scene/object.h"
+#include "static_scene/sphere.h"
 
 double pbf_ref_dt = 0.016;
 double pbf_ref_h = 0.3;
@@ -63,6 +69,21 @@ void pbf_ref_reinit_statics();
 }
 
 using namespace CGL;
+
+// The reference defines SphereObject's members in static_scene/object.cpp, next to the
+// polygon-mesh object whose code needs the half-edge mesh library; this driver links the
+// reference's Sphere primitive (sphere.cpp) without object.cpp, so the three members a
+// Sphere's material lookup reaches are defined here: keep the centre, radius and
+// material; list the one Sphere primitive; hand out the material.
+namespace CGL {
+namespace StaticScene {
+SphereObject::SphereObject(const Vector3D& o_, double r_, BSDF* bsdf_) : o(o_), r(r_), bsdf(bsdf_) {}
+std::vector<Primitive*> SphereObject::get_primitives() const {
+  return std::vector<Primitive*>(1, new Sphere(this, o, r));
+}
+BSDF* SphereObject::get_bsdf() const { return bsdf; }
+}  // namespace StaticScene
+}  // namespace CGL
 
 namespace {
 
@@ -150,8 +171,15 @@ void step_jacobi(Particles& P, double dt) {
 }  // namespace
 
 int main(int argc, char** argv) {
+  if (argc == 2 && std::strcmp(argv[1], "--params-string") == 0) {
+    // the reference's constructor prints Particles::paramsString() (particles.h:114-116)
+    // with the reference's default constants
+    Particles* P = new Particles(1000.0);
+    (void)P;
+    return 0;
+  }
   if (argc != 3) {
-    std::fprintf(stderr, "usage: %s <in.bin> <out.bin>\n", argv[0]);
+    std::fprintf(stderr, "usage: %s <in.bin> <out.bin> | --params-string\n", argv[0]);
     return 2;
   }
   std::ifstream in(argv[1], std::ios::binary);
@@ -209,6 +237,18 @@ int main(int argc, char** argv) {
       Vector3D p1(q[0], q[1], q[2]), p2(q[3], q[4], q[5]), p3(q[6], q[7], q[8]);
       Vector3D nn = cross(p2 - p1, p3 - p1).unit();
       prims.push_back(new MarchingTriangle(p1, p2, p3, nn, nn, nn, nullptr));
+    }
+  }
+  if (flags & 64) {  // collider spheres: the reference's Sphere primitives in the same BVH
+    int64_t m = 0;
+    rd(in, &m, 1);
+    std::vector<double> q(4 * m);
+    rd(in, q.data(), q.size());
+    for (int64_t k = 0; k < m; k++) {
+      const Vector3D o(q[4 * k], q[4 * k + 1], q[4 * k + 2]);
+      const SphereObject* obj = new SphereObject(o, q[4 * k + 3], nullptr);
+      std::vector<Primitive*> sp = obj->get_primitives();
+      prims.insert(prims.end(), sp.begin(), sp.end());
     }
   }
   BVHAccel* bvh = new BVHAccel(prims);

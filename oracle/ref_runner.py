@@ -24,7 +24,7 @@ def available() -> bool:
 
 def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool = False,
         load_density: bool = False, restart: bool = False, timeout: float | None = None,
-        surface: bool = False, mesh=None) -> dict:
+        surface: bool = False, mesh=None, spheres=None) -> dict:
     """Run ``steps`` reference steps. ``params`` is a fluid_gb300.params.PbfParams.
 
     ``restart``: every step starts again from (pos, vel); ``seconds`` then times
@@ -32,7 +32,8 @@ def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool 
     reference's surface after the steps (Particles::getSurfacePrims with
     updateSurface's arguments): ``surf_xyz`` / ``surf_nrm`` (T, 3, 3), ``surf_cube``.
     ``mesh``: (m, 9) collider triangles added to the box (the reference's BVH holds them
-    as MarchingTriangles with the normal ((p2 - p1) x (p3 - p1)).unit()).
+    as MarchingTriangles with the normal ((p2 - p1) x (p3 - p1)).unit()). ``spheres``:
+    (m, 4) centres and radii, the reference's Sphere primitives in the same BVH.
 
     The reference hard-codes gravity on -y, the clip planes z=1 / y=1.49 and the
     clamp box (particles.cpp:57-83, 180); params that disagree are rejected.
@@ -54,7 +55,7 @@ def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool 
     vel = np.ascontiguousarray(vel, dtype=np.float64)
     n = pos.shape[0]
     flags = ((2 if neighbors else 0) | (4 if load_density else 0) | (8 if restart else 0) | (16 if surface else 0)
-             | (32 if mesh is not None else 0))
+             | (32 if mesh is not None else 0) | (64 if spheres is not None else 0))
     with tempfile.TemporaryDirectory() as td:
         fin = Path(td) / "in.bin"
         fout = Path(td) / "out.bin"
@@ -72,6 +73,10 @@ def run(pos, vel, params, steps: int = 1, mode: str = "jacobi", neighbors: bool 
                 m = np.ascontiguousarray(mesh, dtype=np.float64).reshape(-1, 9)
                 f.write(struct.pack("<q", m.shape[0]))
                 f.write(m.tobytes())
+            if spheres is not None:
+                q = np.ascontiguousarray(spheres, dtype=np.float64).reshape(-1, 4)
+                f.write(struct.pack("<q", q.shape[0]))
+                f.write(q.tobytes())
         subprocess.run([str(DRIVER), str(fin), str(fout)], check=True, timeout=timeout)
         buf = fout.read_bytes()
     assert buf[:8] == b"PBFREFO1"
