@@ -15,9 +15,10 @@ import pytest
 from tests.golden.make_golden import params_from_json
 
 # reference-step vectors of make_golden.py (the finite-difference fixture of the adjoint
-# workload, the surface and the render fixtures are read by their own tests)
+# workload, the surface and the render fixtures and the bunny scene's triangles are read
+# by their own tests)
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                if not os.path.basename(p).startswith(("adjoint_", "surface_", "render_")))
+                if not os.path.basename(p).startswith(("adjoint_", "surface_", "render_", "cbbunny")))
 
 
 def _case_id(path):
@@ -28,13 +29,16 @@ def _case_id(path):
 def golden(request, oracle_lib):
     g = np.load(request.param)
     oracle_lib.set_mesh(g["mesh"] if "mesh" in g.files else None)  # collider triangles of the case
+    oracle_lib.set_spheres(g["spheres"] if "spheres" in g.files else None)  # and its spheres
     yield g
     oracle_lib.set_mesh(None)
+    oracle_lib.set_spheres(None)
 
 
 def test_golden_files_present():
     names = {_case_id(p) for p in GOLDEN}
-    assert {"block4096_mass_1step", "p_default_1step", "block512_mass_20step"} <= names
+    assert {"block4096_mass_1step", "p_default_1step", "block512_mass_20step", "sphere_block512_2step",
+            "wavyfloor2048_block512_2step"} <= names
 
 
 def test_oracle_matches_reference_bitwise(golden, oracle_lib):
