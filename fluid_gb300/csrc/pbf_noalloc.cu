@@ -189,6 +189,24 @@ extern "C" pbf_status pbf_density_noalloc(const pbf_params* params, size_t n, co
                                         " cells of size h, more than PBF_NOALLOC_MAX_CELLS (" +
                                         std::to_string(kNaMaxCells) + ")");
   if (n == 0) return PBF_OK;
+  // xyz and rho must be memory of the current device (a host pointer here would make the
+  // kernels fault or, where the GPU can reach host memory, read and write the wrong memory)
+  int cur_dev = 0;
+  cudaError_t e0 = cudaGetDevice(&cur_dev);
+  if (e0 != cudaSuccess) return na_fail(PBF_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e0));
+  const void* ptrs[2] = {xyz, rho};
+  for (const void* q : ptrs) {
+    cudaPointerAttributes at;
+    e0 = cudaPointerGetAttributes(&at, q);
+    if (e0 != cudaSuccess) {
+      cudaGetLastError();
+      return na_fail(PBF_ERR_INVALID, "pbf_density_noalloc: xyz and rho must be device memory");
+    }
+    const bool ok = (at.type == cudaMemoryTypeDevice && at.device == cur_dev) || at.type == cudaMemoryTypeManaged;
+    if (!ok)
+      return na_fail(PBF_ERR_INVALID, "pbf_density_noalloc: xyz and rho must be device (or managed) memory of "
+                                      "the current device");
+  }
   unsigned char* base = nullptr;
   cudaError_t e = scratch_for_current_device(&base);
   if (e != cudaSuccess) return na_fail(PBF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));

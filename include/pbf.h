@@ -236,25 +236,6 @@ PBF_API int pbf_num_scenes(const pbf_handle* h);
 PBF_API const char* pbf_last_error(const pbf_handle* h);
 
 /*
- * pbf_density_noalloc -- no counterpart in the reference.
- *
- * The density estimate of pbf_estimate_densities (Particles::estimateDensities,
- * self term included) for callers that cannot allocate device memory: ones whose
- * device memory belongs to another framework's allocator, or that must not let
- * cudaMalloc/cudaFree synchronize the device. It creates no handle and allocates
- * nothing: xyz ((n, 3) float32) and rho (n float32) are DEVICE pointers owned by
- * the caller, the collider box and kernel radius come from params, and the work
- * is enqueued on `stream` (a cudaStream_t, NULL for the legacy default stream)
- * without waiting. Its cell-sort scratch is one static device array of about
- * 3.9 MB inside the library, held by every GPU that loads it until the process
- * exits. The first call on a device looks up that array's device address, so make
- * the first call on each device outside any stream capture. All calls share the
- * array: calls whose work could overlap on the GPU race and must be serialized.
- * Limits: n <= PBF_NOALLOC_MAX_PARTICLES and at most PBF_NOALLOC_MAX_CELLS grid
- * cells of size h over the box; larger inputs return PBF_ERR_INVALID with the
- * reason in pbf_last_error(NULL).
- */
-/*
  * pbf_adjoint_step_device -- no counterpart in the reference (which has no
  * gradients); the reverse mode of one Particles::timeStep (particles.cpp:250-297).
  *
@@ -437,6 +418,29 @@ PBF_API pbf_status pbf_render_set_scene(pbf_handle* h, const float* tri_xyz, con
 PBF_API pbf_status pbf_render(pbf_handle* h, const pbf_camera* cam, const pbf_render_params* p, float* hdr,
                               uint8_t* rgba, pbf_render_stats* stats);
 
+/*
+ * pbf_density_noalloc -- no counterpart in the reference.
+ *
+ * The density estimate of pbf_estimate_densities (Particles::estimateDensities,
+ * self term included) for callers that cannot allocate device memory: ones whose
+ * device memory belongs to another framework's allocator, or that must not let
+ * cudaMalloc/cudaFree synchronize the device. It creates no handle and allocates
+ * nothing: xyz ((n, 3) float32) and rho (n float32) are DEVICE pointers owned by
+ * the caller (device or managed memory of the current device; anything else, a host
+ * pointer included, is rejected with PBF_ERR_INVALID before any work), the collider
+ * box and kernel radius come from params, and the work is enqueued on `stream` (a
+ * cudaStream_t, NULL for the legacy default stream) without waiting. Its cell-sort
+ * scratch is one static device array of about 3.9 MB inside the library, held by
+ * every GPU that loads it until the process exits. The first call on a device looks
+ * up that array's device address and keeps it for the process, so make the first call
+ * on each device outside any stream capture, and do not call it again after a
+ * cudaDeviceReset of that device. All calls share the array: calls whose work could
+ * overlap on the GPU race and must be serialized. Limits: n <= PBF_NOALLOC_MAX_PARTICLES
+ * and at most PBF_NOALLOC_MAX_CELLS grid cells of size h over the box; larger inputs
+ * return PBF_ERR_INVALID with the reason in pbf_last_error(NULL). A cell holding more
+ * than 256 particles keeps the order its particles were counted in, so for such dense
+ * inputs the sums' order, and hence their last bits, may vary from call to call.
+ */
 #define PBF_NOALLOC_MAX_PARTICLES 65536
 #define PBF_NOALLOC_MAX_CELLS 262144
 PBF_API pbf_status pbf_density_noalloc(const pbf_params* params, size_t n,

@@ -2,8 +2,9 @@
 
 Two stages, both writing only under ``oracle/_ref/`` (git-ignored):
 
-1. ``stage()`` — needs the reference checkout (``PBF_REFERENCE_DIR``, default the
-   read-only mount). Copies the reference files the step needs, unmodified, into
+1. ``stage(reference)`` — needs the reference checkout: its directory is an argument
+   (``--reference DIR`` on the command line) or ``PBF_REFERENCE_DIR``; without either,
+   staging stops with an error. Copies the reference files the step needs, unmodified, into
    ``oracle/_ref/src/`` and writes ``particles_param.cpp``: the reference's
    ``src/particles.cpp`` with its parameter ``#define`` block (lines 20-44) and the
    gravity literal (line 180) rewritten mechanically into references to the runtime
@@ -18,7 +19,7 @@ Two stages, both writing only under ``oracle/_ref/`` (git-ignored):
    ``g++ -O3 -std=gnu++11 -ffp-contract=off`` (contraction off so x86-64 and aarch64
    round identically).
 
-Usage: ``python oracle/ref/build_ref.py [--stage-only|--compile-only]``.
+Usage: ``python oracle/ref/build_ref.py [--reference DIR] [--stage-only|--compile-only]``.
 """
 from __future__ import annotations
 
@@ -37,7 +38,10 @@ STAGE = OUT / "src"
 DRIVER = OUT / "pbf_ref_driver"
 RENDER = OUT / "pbf_ref_render"
 
-REFERENCE = Path(os.environ.get("PBF_REFERENCE_DIR", "/root/reference"))
+def reference_dir() -> Path | None:
+    """The reference checkout named by ``PBF_REFERENCE_DIR``, or None."""
+    d = os.environ.get("PBF_REFERENCE_DIR")
+    return Path(d) if d else None
 
 # Translation units of the reference that the step links against.
 REF_TUS = [
@@ -108,7 +112,10 @@ def rewrite_particles(text: str) -> str:
     return '#include "ref_params.h"\n' + text
 
 
-def stage(reference: Path = REFERENCE) -> None:
+def stage(reference: Path | None = None) -> None:
+    reference = reference or reference_dir()
+    if reference is None:
+        raise FileNotFoundError("no reference checkout given: pass its directory or set PBF_REFERENCE_DIR")
     if not (reference / "src" / "particles.cpp").is_file():
         raise FileNotFoundError(f"reference checkout not found at {reference}")
     if STAGE.exists():
@@ -167,7 +174,8 @@ def compile(jobs: int = 8, cxx: str = "g++") -> Path:
 
 def main(argv: list[str]) -> int:
     if "--compile-only" not in argv:
-        stage()
+        ref = Path(argv[argv.index("--reference") + 1]) if "--reference" in argv else None
+        stage(ref)
     if "--stage-only" not in argv:
         print(compile())
     return 0

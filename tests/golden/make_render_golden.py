@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import dataclasses
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -67,7 +68,10 @@ def save(name: str, scene, cam, pos, params: PbfParams, W: int, H: int, ns_aa: i
 
 
 def main(argv):
-    reference = Path(argv[1]) if len(argv) > 1 else Path("/root/reference")
+    ref_dir = argv[1] if len(argv) > 1 else os.environ.get("PBF_REFERENCE_DIR")
+    if not ref_dir:
+        raise SystemExit(f"usage: {Path(argv[0]).name} <reference_dir> (or set PBF_REFERENCE_DIR)")
+    reference = Path(ref_dir)
     if not ref_runner.render_available():
         raise SystemExit("build the reference renderer first: python oracle/ref/build_ref.py")
     pos, _, rho0 = load_reference_xml(reference / "particles" / "p.xml")

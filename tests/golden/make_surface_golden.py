@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import dataclasses
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -35,7 +36,10 @@ def save(name: str, pos, vel, params: PbfParams, steps: int) -> None:
 
 
 def main(argv):
-    reference = Path(argv[1]) if len(argv) > 1 else Path("/root/reference")
+    ref_dir = argv[1] if len(argv) > 1 else os.environ.get("PBF_REFERENCE_DIR")
+    if not ref_dir:
+        raise SystemExit(f"usage: {Path(argv[0]).name} <reference_dir> (or set PBF_REFERENCE_DIR)")
+    reference = Path(ref_dir)
     if not ref_runner.available():
         raise SystemExit("build the reference driver first: python oracle/ref/build_ref.py")
     pos, vel, rho0 = load_reference_xml(reference / "particles" / "p.xml")

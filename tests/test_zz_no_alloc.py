@@ -61,17 +61,69 @@ def _cases():
             (sc.params, sc.pos.astype(np.float32))]
 
 
-def test_noalloc_matches_handle_path_on_consecutive_calls(pbf):
+def test_noalloc_matches_handle_path_on_consecutive_calls(pbf, oracle_lib):
     cases = _cases()
     order = [0, 1, 0]  # the third call runs on what the second left in the scratch array
     for k in order:
         prm, pos = cases[k]
         got = _noalloc(pbf, prm, pos)
         want = _with_handle(pbf, prm, pos)
-        err = rel_err(got, want)
-        print(f"case {k}: n={len(pos)} rel err vs pbf_estimate_densities {err:.2e}")
+        ref = oracle_lib.estimate_densities(pos.astype(np.float64), prm)  # the FP64 restatement
+        err, err64 = rel_err(got, want), rel_err(got, ref)
+        print(f"case {k}: n={len(pos)} rel err vs pbf_estimate_densities {err:.2e}, vs FP64 {err64:.2e}")
         assert np.all(np.isfinite(got))
-        assert err < TOL
+        assert err < TOL and err64 < TOL
+
+
+def _largest_case():
+    """65,536 particles (the particle limit) with h such that the unit box needs 64^3 =
+    262,144 cells of size h (the cell limit): the scratch layout's offsets and the scan's
+    tile count at their largest."""
+    h = 0.0162
+    prm = scenes.physical_params(h, h / 2)
+    pos = scenes.lattice(64, 32, 32, h / 2, corner=(0.2, 0.0, 0.3))
+    pos += scenes.uniform(29, pos.size, -1e-4, 1e-4).reshape(pos.shape)
+    return prm, pos.astype(np.float32)
+
+
+def test_noalloc_at_its_limits(pbf, oracle_lib):
+    from tests.helpers import scene_grid
+
+    prm, pos = _largest_case()
+    _, _, dims = scene_grid(prm, prm.box_lo, prm.box_hi)
+    assert len(pos) == 65536 and int(np.prod(dims)) == 262144
+    for _ in range(2):
+        got = _noalloc(pbf, prm, pos)
+        want = _with_handle(pbf, prm, pos)
+        ref = oracle_lib.estimate_densities(pos.astype(np.float64), prm)
+        err, err64 = rel_err(got, want), rel_err(got, ref)
+        print(f"limits: rel err vs pbf_estimate_densities {err:.2e}, vs FP64 {err64:.2e}")
+        assert err < TOL and err64 < TOL
+
+
+def test_noalloc_dense_cell(pbf):
+    """300 particles in about one cell (more than the 256 whose order the call fixes):
+    within the tolerance of the handle path, call after call."""
+    rng = np.random.default_rng(8)
+    prm = scenes.physical_params(0.1, 0.05)
+    pos = np.stack([rng.uniform(0.41, 0.49, 300), rng.uniform(0.01, 0.09, 300),
+                    rng.uniform(0.41, 0.49, 300)], 1).astype(np.float32)
+    want = _with_handle(pbf, prm, pos)
+    for _ in range(2):
+        assert rel_err(_noalloc(pbf, prm, pos), want) < TOL
+
+
+def test_noalloc_empty_and_host_pointers(pbf):
+    lib = pbf.lib()
+    prm = scenes.block4096(1).params
+    cp = prm.to_c()
+    assert lib.pbf_density_noalloc(ctypes.byref(cp), 0, None, None, None) == 0
+    # host memory is refused before any device work
+    x = np.zeros((10, 3), dtype=np.float32)
+    r = np.zeros(10, dtype=np.float32)
+    rc = lib.pbf_density_noalloc(ctypes.byref(cp), 10, x.ctypes.data_as(ctypes.c_void_p),
+                                 r.ctypes.data_as(ctypes.c_void_p), None)
+    assert rc == 1 and b"device" in lib.pbf_last_error(None)
 
 
 def test_noalloc_rejects_inputs_beyond_its_limits(pbf):
