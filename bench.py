@@ -53,9 +53,9 @@ UNIT = "particle-updates/s"
 ALGO_BYTES = {"predict": 64 + 24, "sort": 104, "gather": 0, "lambda": 20, "deltap": 36,
               "xsph": 84, "vorticity": 64, "neighbors": 16, "scan": 0, "stats": 0}
 # DRAM bytes per particle per launch measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) on the 1M colliding-blocks scene; see profiles/.
-# Source: profiles/k_deltap_k_lambda_k_nbr_build_colliding_blocks_1m.md.
-NCU_TRAFFIC_PER_PARTICLE: dict[str, float] = {"deltap": 141.9, "lambda": 99.1, "neighbors": 62.2}
+# dram__bytes_write.sum) on the 1M colliding-blocks scene: profiles/k_deltap_colliding_blocks_1m.md
+# (k_deltap) and profiles/neighbour_pass_forms_colliding_blocks_1m.md (k_lambda, k_nbr_build).
+NCU_TRAFFIC_PER_PARTICLE: dict[str, float] = {"deltap": 141.8, "lambda": 99.1, "neighbors": 62.2}
 
 
 def peaks():
