@@ -637,15 +637,16 @@ struct Pair {
   float3 r;
   float r2, q, s;
 };
-// FTZ selects the flush-to-zero form of the approximate reciprocal square root. The two
-// forms differ only for a subnormal r2, far below EPS_D^2, where s is 0 either way (and
-// both give +inf at r2 = 0, where hr is 0), so the pair values are the same; the vorticity
-// pass measured faster with it (0.066 against 0.071 ms per step on the 1M colliding
-// blocks), the other passes did not.
+// FTZ selects the flush-to-zero form of the approximate reciprocal square root, which
+// needs no rescaling of subnormal inputs. The two forms differ only for a subnormal r2,
+// far below EPS_D^2, where s is 0 either way (and both give +inf at r2 = 0, where hr is 0),
+// so the pair values are the same. Every pass uses it: measured with the current kernels on
+// the 1M colliding blocks, lambda 0.222 against 0.235 ms a step, delta-p 0.274 against
+// 0.279, XSPH 0.090 against 0.093 (the vorticity pass already used it).
 // Every rounding is explicit (_rn intrinsics, fused where written as an fma), so the
 // compiler cannot contract differently in differently unrolled loops: every form of a
 // neighbour pass gives the same bits.
-template <bool FTZ = false>
+template <bool FTZ = true>
 __device__ __forceinline__ Pair pair_of(const float4& xi, const float4& xj, float h, float h2) {
   Pair p;
   p.r = make_float3(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z));
