@@ -108,10 +108,13 @@ bool make_dev_params(const pbf_params& p, DevParams* d, double* cell_out, std::s
     d->clamp_hi[k] = static_cast<float>(p.clamp_hi[k]);
   }
   d->n_clip = p.n_clip;
+  double clip_scale = 1.0;
   for (int c = 0; c < p.n_clip; ++c) {
     d->clip_axis[c] = p.clip_axis[c];
     d->clip_value[c] = static_cast<float>(p.clip_value[c]);
+    clip_scale = std::max(clip_scale, std::fabs(p.clip_value[c]));
   }
+  d->clip_margin = static_cast<float>(kInteriorMargin * clip_scale);
   d->scorr_n = p.scorr_n;
   d->open_mask = p.box_open_mask;
   d->max_words = (max_nbr + 1) / 2;
@@ -143,6 +146,22 @@ bool make_scene(const pbf_params& p, double cell, const float* lo, const float* 
       return false;
     }
     sc->dim[a] = static_cast<int>(dim);
+  }
+  // Interior box (collide's shortcut): inside the closed walls and the clamp box by a margin
+  // of kInteriorMargin times the largest coordinate among them (at least 1). A move whose
+  // ends both lie inside it stops at no wall by more than the FP32 rounding of the stop
+  // distances, and no coordinate is clamped. A box left empty (in_lo >= in_hi) takes no move.
+  double scale = 1.0;
+  for (int a = 0; a < 3; ++a)
+    scale = std::max({scale, std::fabs(static_cast<double>(lo[a])), std::fabs(static_cast<double>(hi[a])),
+                      std::fabs(p.clamp_lo[a]), std::fabs(p.clamp_hi[a])});
+  const double m = kInteriorMargin * scale;
+  for (int a = 0; a < 3; ++a) {
+    double ilo = p.clamp_lo[a], ihi = p.clamp_hi[a];
+    if (!(p.box_open_mask & (1 << (2 * a)))) ilo = std::max(ilo, static_cast<double>(lo[a]));
+    if (!(p.box_open_mask & (1 << (2 * a + 1)))) ihi = std::min(ihi, static_cast<double>(hi[a]));
+    sc->in_lo[a] = static_cast<float>(ilo + m);
+    sc->in_hi[a] = static_cast<float>(ihi - m);
   }
   return true;
 }

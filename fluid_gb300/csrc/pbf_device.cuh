@@ -242,6 +242,30 @@ __device__ __forceinline__ uint32_t coll_index(uint32_t c) { return (c >> 4) & 7
 __device__ __forceinline__ uint32_t coll_wall2(uint32_t c) { return (c >> 8) & 7u; }
 __device__ __forceinline__ uint32_t coll_clamped(uint32_t c) { return (c >> 12) & 7u; }
 
+// Shortcut of collide(): a move longer than EPS_D (by 0.1%, so the rounding of sqrt cannot
+// decide it) that starts and ends inside the scene's interior box and keeps clip_margin
+// from every clip plane meets no wall and no plane and leaves every coordinate inside the
+// clamp box: the general path would add delta unchanged, which the shortcut does without
+// the stop distances' divisions. The margins are about 1,000 ulps of the coordinates' scale, far
+// above the rounding of those distances, so the two paths give the same bits. NaN or
+// infinite coordinates fail the comparisons and take the general path.
+template <bool MESH>
+__device__ __forceinline__ bool clear_move(const float3 p, const float3 delta, float s2, const SceneDesc& sc,
+                                           const DevParams& P) {
+  if (MESH && (P.n_mesh > 0 || P.n_sph > 0)) return false;
+  if (!(s2 > kEps * kEps * 1.001f)) return false;
+  const float3 e = p + delta;
+  bool ok = fminf(p.x, e.x) > sc.in_lo[0] && fmaxf(p.x, e.x) < sc.in_hi[0] &&
+            fminf(p.y, e.y) > sc.in_lo[1] && fmaxf(p.y, e.y) < sc.in_hi[1] &&
+            fminf(p.z, e.z) > sc.in_lo[2] && fmaxf(p.z, e.z) < sc.in_hi[2];
+  for (int c = 0; c < P.n_clip; ++c) {
+    const int a = P.clip_axis[c];
+    const float u = cmp3(p, a), w = cmp3(e, a), v = P.clip_value[c];
+    ok = ok && (fminf(u, w) > v + P.clip_margin || fmaxf(u, w) < v - P.clip_margin);
+  }
+  return ok;
+}
+
 // Move x* = x + d by `delta` against the collider, in displacement form: d is
 // updated, x is fixed. Follows clamp (slide = false, particles.cpp:51-84) and
 // clamp_response (slide = true, particles.cpp:87-132): clip planes first, the
@@ -251,11 +275,18 @@ __device__ __forceinline__ uint32_t coll_clamped(uint32_t c) { return (c >> 12) 
 // REC additionally writes the collision record to *code (same arithmetic).
 // MESH = false compiles the collider-triangle tests out (for launches with no triangles:
 // they hold registers a neighbour pass would otherwise spend on occupancy).
+// Moves that clear_move accepts take its shortcut.
 template <bool REC = false, bool MESH = true>
 __device__ __forceinline__ void collide(const float3 x, float3& d, const float3 delta, bool slide,
                                         const SceneDesc& sc, const DevParams& P, uint32_t* code = nullptr) {
   const float3 p = x + d;
-  float l = sqrtf(delta.x * delta.x + delta.y * delta.y + delta.z * delta.z);
+  const float s2 = delta.x * delta.x + delta.y * delta.y + delta.z * delta.z;
+  if (clear_move<MESH>(p, delta, s2, sc, P)) {
+    d = d + delta;
+    if (REC) *code = kCollFree;
+    return;
+  }
+  float l = sqrtf(s2);
   if (!(l > kEps)) {  // particles.cpp:53-55 / 90-92: no move, no clamp
     if (REC) *code = kCollNone;
     return;
@@ -495,6 +526,10 @@ constexpr uint32_t kOffsetMask = (1u << kOffsetBits) - 1u;
 
 __device__ __forceinline__ int nbr_total(const uint4& h) { return static_cast<int>(h.w); }
 
+// A list entry is a 2-bit slab tag g over a 14-bit offset into slab g's three rows. The
+// header holds slab 0's first slot in x and, in y and z, slab 1's and slab 2's first slots
+// less slab 0's and less the tag bits (g << 14), all modulo 2^32, so the slot is
+// x + entry + (0, y or z by tag): the entry needs no masking.
 // Two forms of the same decode (slab tags are 0, 1 and 2, so both give the same slot).
 // The compiler schedules a pass's gathers differently around them; measured per pass on
 // the 1M colliding blocks (ms per step): lambda 0.238 / 0.256 and delta-p 0.282 / 0.315
@@ -503,14 +538,14 @@ enum class Decode { kBits, kCompare };
 
 template <Decode DC = Decode::kBits>
 __device__ __forceinline__ uint32_t nbr_decode(const uint4& h, uint32_t e) {
-  uint32_t base;
+  uint32_t adj;
   if (DC == Decode::kBits) {
-    base = (e & (2u << kOffsetBits)) ? h.z : ((e & (1u << kOffsetBits)) ? h.y : h.x);
+    adj = (e & (2u << kOffsetBits)) ? h.z : ((e & (1u << kOffsetBits)) ? h.y : 0u);
   } else {
     const uint32_t g = e >> kOffsetBits;
-    base = g == 0u ? h.x : (g == 1u ? h.y : h.z);
+    adj = g == 0u ? 0u : (g == 1u ? h.y : h.z);
   }
-  return base + (e & kOffsetMask);
+  return h.x + e + adj;
 }
 
 // Calls f(j) for every neighbour slot j of slot i, ascending.

@@ -27,6 +27,9 @@ namespace pbf {
 constexpr int kMaxRowCandidates = 4096;  // bound on the candidates scanned in one 3-cell row
 constexpr int kNeighborAlert = 18;      // NUM_NEIGHBOR_ALERT_THRESHOLD, particles.cpp:32
 constexpr float kEps = 1e-11f;          // EPS_D, CGL/include/CGL/misc.h:11
+// Margin of the collider's interior box and clip planes, relative to the largest coordinate
+// of the walls, the clamp box or the planes (at least 1): about 1,000 FP32 ulps of it.
+constexpr double kInteriorMargin = 1e-4;
 
 // Per-scene collider and grid (device table, one entry per scene).
 struct SceneDesc {
@@ -35,7 +38,8 @@ struct SceneDesc {
   int dim[3];               // grid cells per axis
   uint32_t cell_off;        // first global cell id
   uint32_t p_off, p_cnt;    // particle range in original order
-  uint32_t pad;
+  float in_lo[3], in_hi[3];  // interior box: the closed walls and the clamp box, shrunk by a
+                             // margin (a move that stays inside it touches neither)
 };
 
 // Uniform physics parameters in FP32, derived on the host from pbf_params.
@@ -49,6 +53,7 @@ struct DevParams {
   float g[3];
   float clip_value[2];
   float clamp_lo[3], clamp_hi[3];
+  float clip_margin;  // a move that keeps this far from every clip plane crosses none
   int scorr_n, n_clip, clip_axis[2], open_mask, max_words;
   int stats;
   int n_mesh;                // collider triangles besides the box walls (pbf_set_collider_mesh)

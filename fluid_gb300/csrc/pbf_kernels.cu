@@ -385,7 +385,9 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
     }
   }
   if (total & 1) *wptr = word;
-  hdr[i] = make_uint4(gbase[0], gbase[1], gbase[2], static_cast<uint32_t>(total));
+  // the slab bases relative to slab 0's, less the tag bits (nbr_decode)
+  hdr[i] = make_uint4(gbase[0], gbase[1] - gbase[0] - (1u << kOffsetBits),
+                      gbase[2] - gbase[0] - (2u << kOffsetBits), static_cast<uint32_t>(total));
   if (flags) atomicOr(err, flags);
 }
 
