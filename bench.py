@@ -700,6 +700,16 @@ def bench_ours(args, scene, world, rank, local):
     achieved = algo / per_launch_s / 1e9
     traffic = NCU_TRAFFIC_PER_PARTICLE.get(dom)
     step_bytes = (340 + 56 * prm.iters) * n
+    # the same figures for every phase with algorithmic bytes (the dominant one included)
+    per_kernel = {}
+    for k, (ms, cnt) in phases.items():
+        if ALGO_BYTES.get(k, 0) > 0 and cnt > 0:
+            sec = ms / cnt / 1e3
+            per_kernel[k] = {"launches_per_step": cnt / args.steps, "avg_launch_ms": sec * 1e3,
+                             "algo_bytes_per_launch": ALGO_BYTES[k] * n,
+                             "achieved": ALGO_BYTES[k] * n / sec / 1e9,
+                             "frac": ALGO_BYTES[k] * n / sec / 1e9 / peak,
+                             "share_of_phase_pass": ms / sum(prof_ms)}
     launches = int(sum(v[1] for v in phases.values()))
 
     # end to end through the C ABI with pinned host buffers
@@ -750,7 +760,8 @@ def bench_ours(args, scene, world, rank, local):
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": None if traffic is None else traffic * n,
                      "algo_bytes_per_launch": algo, "avg_launch_ms": per_launch_s * 1e3,
-                     "step_frac": step_bytes / (total_ms / args.steps / 1e3) / 1e9 / peak},
+                     "step_frac": step_bytes / (total_ms / args.steps / 1e3) / 1e9 / peak,
+                     "kernels": per_kernel},
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items()},
         "phases_pass": {"launch": "stream-ordered with events between phases (no graph)",
                         "ms_per_step": sum(prof_ms) / args.steps},

@@ -212,7 +212,7 @@ pbf_status Handle::alloc_all() {
       {(void**)&b.omega, f4}, {(void**)&b.xkey, u4}, {(void**)&b.rho, u4}, {(void**)&b.rho_iter0, u4},
       {(void**)&b.id[0], u4}, {(void**)&b.id[1], u4}, {(void**)&b.key, u4}, {(void**)&b.rank, u4},
       {(void**)&b.perm, u4}, {(void**)&b.nbr_hdr, sizeof(uint4) * n},
-      {(void**)&b.nbr_w, u4 * static_cast<size_t>(b.max_words)},
+      {(void**)&b.nbr_w, u4 * static_cast<size_t>((b.max_words + 3) / 4 * 4)},  // groups of 4 words
       {(void**)&b.cell_count, sizeof(uint32_t) * b.n_cells},
       {(void**)&b.cell_start, sizeof(uint32_t) * (b.n_cells + 1)},
       {(void**)&b.scan_tmp, sizeof(uint32_t) * ((b.n_cells + 1023) / 1024 + 1)},

@@ -531,9 +531,10 @@ __device__ __forceinline__ int nbr_total(const uint4& h) { return static_cast<in
 // less slab 0's and less the tag bits (g << 14), all modulo 2^32, so the slot is
 // x + entry + (0, y or z by tag): the entry needs no masking.
 // Two forms of the same decode (slab tags are 0, 1 and 2, so both give the same slot).
-// The compiler schedules a pass's gathers differently around them; measured per pass on
-// the 1M colliding blocks (ms per step): lambda 0.238 / 0.256 and delta-p 0.282 / 0.315
-// with kBits / kCompare, XSPH 0.113 / 0.104.
+// The compiler schedules a pass's gathers differently around them; every pass measured
+// fastest with kBits on the 1M colliding blocks (ms per step, kBits / kCompare): lambda
+// 0.238 / 0.256 and delta-p 0.282 / 0.315 with word-major lists, XSPH 0.084 / 0.100 with
+// the grouped list words.
 enum class Decode { kBits, kCompare };
 
 template <Decode DC = Decode::kBits>
@@ -548,34 +549,39 @@ __device__ __forceinline__ uint32_t nbr_decode(const uint4& h, uint32_t e) {
   return h.x + e + adj;
 }
 
+// List words are grouped by four: word w of slot i is words[list_word(i, n, w)], i.e. the
+// layout is [W/4][N][4] (W = words per slot rounded up to 4). One 16-byte load brings a
+// slot 8 entries, the 32 slots of a warp read 512 contiguous bytes, and consecutive warps
+// read consecutive lines.
+__device__ __forceinline__ size_t list_word(int i, int n, int w) {
+  return static_cast<size_t>(w >> 2) * (4 * static_cast<size_t>(n)) + 4 * static_cast<size_t>(i) +
+         static_cast<uint32_t>(w & 3);
+}
+
 // Calls f(j) for every neighbour slot j of slot i, ascending.
 template <typename F>
 __device__ __forceinline__ void for_each_neighbor(int i, int n, const uint4 h,
                                                   const uint32_t* __restrict__ words, F&& f) {
   const int total = nbr_total(h);
-  int k = 0;
-  for (; k + 1 < total; k += 2) {
-    const uint32_t w = __ldg(&words[static_cast<size_t>(k >> 1) * n + i]);
+  for (int k = 0; k < total; k += 2) {
+    const uint32_t w = __ldg(&words[list_word(i, n, k >> 1)]);
     f(nbr_decode(h, w & 0xffffu));
-    f(nbr_decode(h, w >> 16));
-  }
-  if (k < total) {
-    const uint32_t w = __ldg(&words[static_cast<size_t>(k >> 1) * n + i]);
-    f(nbr_decode(h, w & 0xffffu));
+    if (k + 1 < total) f(nbr_decode(h, w >> 16));
   }
 }
 
 // As for_each_neighbor, with each neighbour's data gathered ahead of the computation:
 // load(j) returns what f needs of neighbour j; per round D list entries are decoded and
 // their loads issued before f runs on any of them, so every thread keeps D independent
-// gathers in flight. With D = 8 the next round's list words are loaded before this
-// round's computation, so their latency overlaps it. Calls f(j, load(j)) in the same
-// (ascending) order. D = 2, 4 or 8; DC picks the decode form.
+// gathers in flight. A round of 8 entries is one 16-byte group of list words; with D = 8
+// the next group is loaded before this round's computation, so its latency overlaps it.
+// The last group, with fewer than 8 entries left, is taken from the same registers. Calls
+// f(j, load(j)) in the same (ascending) order. D = 4 or 8; DC picks the decode form.
 // List words are read once per pass: ST = true loads them with the streaming policy
 // (ld.global.cs, evict-first in L1 and L2), so they displace less of the neighbours' x*
 // that the pass gathers repeatedly.
 template <bool ST>
-__device__ __forceinline__ uint32_t ld_list(const uint32_t* p) {
+__device__ __forceinline__ uint4 ld_quad(const uint4* p) {
   return ST ? __ldcs(p) : __ldg(p);
 }
 template <bool ST>
@@ -586,25 +592,22 @@ __device__ __forceinline__ uint4 ld_hdr(const uint4* p) {
 template <int D, Decode DC = Decode::kBits, bool ST = false, typename L, typename F>
 __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h,
                                                      const uint32_t* __restrict__ words, L&& load, F&& f) {
+  static_assert(D == 4 || D == 8, "gather depth 4 or 8");
   const int total = nbr_total(h);
+  if (total <= 0) return;
   const size_t sn = static_cast<size_t>(n);
-  const uint32_t* wp = words + i;
+  const uint4* qp = reinterpret_cast<const uint4*>(words) + i;
+  uint4 q = ld_quad<ST>(qp);
   int k = 0;
-  if (D == 8) {
-    uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u;
-    if (total >= 8) {
-      w0 = ld_list<ST>(wp); w1 = ld_list<ST>(wp + sn); w2 = ld_list<ST>(wp + 2 * sn); w3 = ld_list<ST>(wp + 3 * sn);
-    }
-    for (; k + 7 < total; k += 8) {
-      wp += 4 * sn;
-      uint32_t n0 = 0u, n1 = 0u, n2 = 0u, n3 = 0u;
-      if (k + 15 < total) {
-        n0 = ld_list<ST>(wp); n1 = ld_list<ST>(wp + sn); n2 = ld_list<ST>(wp + 2 * sn); n3 = ld_list<ST>(wp + 3 * sn);
-      }
-      const uint32_t j0 = nbr_decode<DC>(h, w0 & 0xffffu), j1 = nbr_decode<DC>(h, w0 >> 16);
-      const uint32_t j2 = nbr_decode<DC>(h, w1 & 0xffffu), j3 = nbr_decode<DC>(h, w1 >> 16);
-      const uint32_t j4 = nbr_decode<DC>(h, w2 & 0xffffu), j5 = nbr_decode<DC>(h, w2 >> 16);
-      const uint32_t j6 = nbr_decode<DC>(h, w3 & 0xffffu), j7 = nbr_decode<DC>(h, w3 >> 16);
+  for (; k + 7 < total; k += 8) {
+    qp += sn;
+    uint4 nq = make_uint4(0u, 0u, 0u, 0u);
+    if (D == 8 && k + 8 < total) nq = ld_quad<ST>(qp);
+    const uint32_t j0 = nbr_decode<DC>(h, q.x & 0xffffu), j1 = nbr_decode<DC>(h, q.x >> 16);
+    const uint32_t j2 = nbr_decode<DC>(h, q.y & 0xffffu), j3 = nbr_decode<DC>(h, q.y >> 16);
+    if (D == 8) {
+      const uint32_t j4 = nbr_decode<DC>(h, q.z & 0xffffu), j5 = nbr_decode<DC>(h, q.z >> 16);
+      const uint32_t j6 = nbr_decode<DC>(h, q.w & 0xffffu), j7 = nbr_decode<DC>(h, q.w >> 16);
       const auto a0 = load(j0);
       const auto a1 = load(j1);
       const auto a2 = load(j2);
@@ -621,15 +624,8 @@ __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h
       f(j5, a5);
       f(j6, a6);
       f(j7, a7);
-      w0 = n0; w1 = n1; w2 = n2; w3 = n3;
-    }
-  }
-  if (D >= 4) {
-    for (; k + 3 < total; k += 4) {
-      const uint32_t w0 = ld_list<ST>(wp), w1 = ld_list<ST>(wp + sn);
-      wp += 2 * sn;
-      const uint32_t j0 = nbr_decode<DC>(h, w0 & 0xffffu), j1 = nbr_decode<DC>(h, w0 >> 16);
-      const uint32_t j2 = nbr_decode<DC>(h, w1 & 0xffffu), j3 = nbr_decode<DC>(h, w1 >> 16);
+      q = nq;
+    } else {
       const auto a0 = load(j0);
       const auto a1 = load(j1);
       const auto a2 = load(j2);
@@ -638,19 +634,46 @@ __device__ __forceinline__ void for_each_neighbor_pf(int i, int n, const uint4 h
       f(j1, a1);
       f(j2, a2);
       f(j3, a3);
+      const uint32_t j4 = nbr_decode<DC>(h, q.z & 0xffffu), j5 = nbr_decode<DC>(h, q.z >> 16);
+      const uint32_t j6 = nbr_decode<DC>(h, q.w & 0xffffu), j7 = nbr_decode<DC>(h, q.w >> 16);
+      const auto a4 = load(j4);
+      const auto a5 = load(j5);
+      const auto a6 = load(j6);
+      const auto a7 = load(j7);
+      f(j4, a4);
+      f(j5, a5);
+      f(j6, a6);
+      f(j7, a7);
+      if (k + 8 < total) q = ld_quad<ST>(qp);
     }
   }
-  for (; k + 1 < total; k += 2) {
-    const uint32_t w = ld_list<ST>(wp);
-    wp += sn;
-    const uint32_t j0 = nbr_decode<DC>(h, w & 0xffffu), j1 = nbr_decode<DC>(h, w >> 16);
+  // fewer than 8 entries left, all in q
+  if (k + 3 < total) {
+    const uint32_t j0 = nbr_decode<DC>(h, q.x & 0xffffu), j1 = nbr_decode<DC>(h, q.x >> 16);
+    const uint32_t j2 = nbr_decode<DC>(h, q.y & 0xffffu), j3 = nbr_decode<DC>(h, q.y >> 16);
+    const auto a0 = load(j0);
+    const auto a1 = load(j1);
+    const auto a2 = load(j2);
+    const auto a3 = load(j3);
+    f(j0, a0);
+    f(j1, a1);
+    f(j2, a2);
+    f(j3, a3);
+    k += 4;
+    q.x = q.z;
+    q.y = q.w;
+  }
+  if (k + 1 < total) {
+    const uint32_t j0 = nbr_decode<DC>(h, q.x & 0xffffu), j1 = nbr_decode<DC>(h, q.x >> 16);
     const auto a0 = load(j0);
     const auto a1 = load(j1);
     f(j0, a0);
     f(j1, a1);
+    k += 2;
+    q.x = q.y;
   }
   if (k < total) {
-    const uint32_t j0 = nbr_decode<DC>(h, ld_list<ST>(wp) & 0xffffu);
+    const uint32_t j0 = nbr_decode<DC>(h, q.x & 0xffffu);
     f(j0, load(j0));
   }
 }

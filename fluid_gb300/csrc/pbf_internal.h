@@ -10,8 +10,9 @@
 //   lam    float   lambda                                    4 B
 //   rho    float   reported density                          4 B
 //   id     u32     original particle index                   4 B
-//   nbr_hdr uint4  first candidate slot of the 3 z-slabs, neighbour count
-//   nbr_w   u32    [words][N] neighbour entries, 2 x u16 per word, word-major
+//   nbr_hdr uint4  first candidate slot of z-slab 0, the other two slabs' first slots
+//                  relative to it (less the entries' tag bits), neighbour count
+//   nbr_w   u32    [words/4][N][4] neighbour entries, 2 x u16 per word, in groups of 4 words
 //   cell_count / cell_start u32 [C] / [C+1]
 #pragma once
 

@@ -299,7 +299,17 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
   uint32_t gbase[3] = {0u, 0u, 0u};
   int total = 0;
   uint32_t word = 0;
-  uint32_t* wptr = words + i;
+  // list words in groups of 4 (list_word): wptr walks the slot's words, one word at a time
+  // within a group and on to the next group after every fourth. (Collecting a group in
+  // registers or in shared memory and storing it as one 16-byte write measured slower:
+  // the appends run divergently, and the extra instructions and the smaller L1 cost more
+  // than the coalesced stores save.)
+  uint32_t* wptr = words + 4 * static_cast<size_t>(i);
+  const size_t wstep = 4 * static_cast<size_t>(n) - 3;
+  auto put = [&](int wi, uint32_t wv) {
+    *wptr = wv;
+    wptr += ((wi & 3) == 3) ? wstep : 1;
+  };
   unsigned flags = 0;
   // position inside the own cell, in cells, and the reach in cells with its margin
   const float fy = (xi.y - sc.origin[1]) * P.inv_cell - static_cast<float>(cc.y);
@@ -372,8 +382,7 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
                 word = e;
               } else {
                 word |= e << 16;
-                *wptr = word;
-                wptr += n;
+                put(total >> 1, word);
               }
               ++total;
             } else {
@@ -384,7 +393,7 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
       }
     }
   }
-  if (total & 1) *wptr = word;
+  if (total & 1) put(total >> 1, word);
   // the slab bases relative to slab 0's, less the tag bits (nbr_decode)
   hdr[i] = make_uint4(gbase[0], gbase[1] - gbase[0] - (1u << kOffsetBits),
                       gbase[2] - gbase[0] - (2u << kOffsetBits), static_cast<uint32_t>(total));
@@ -492,7 +501,7 @@ __global__ void __launch_bounds__(BLOCK) k_xsph(float4* xs, const float4* __rest
   struct XD {
     float4 x, d;
   };
-  for_each_neighbor_pf<D, Decode::kCompare, ST>(
+  for_each_neighbor_pf<D, Decode::kBits, ST>(
       i, n, ld_hdr<ST>(&hdr[i]), words, [&](uint32_t j) { return XD{xs[j], __ldg(&disp[j])}; },
       [&](uint32_t, const XD& a) {
     const Pair p = pair_of(xi, a.x, P.h, P.h2);
