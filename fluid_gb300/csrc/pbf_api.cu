@@ -174,7 +174,7 @@ void Handle::free_all() {
   }
   void* ptrs[] = {b.pos[0], b.pos[1], b.disp[0], b.disp[1], b.xs[0], b.xs[1], b.vel[0], b.vel[1],
                   b.omega, b.pred, b.xkey, b.rho, b.rho_iter0, b.id[0], b.id[1], b.key, b.rank,
-                  b.perm, b.nbr_hdr, b.nbr_w, b.cell_count, b.cell_start, b.scan_tmp, b.big_cells, b.big_count, b.scenes, b.stats_part,
+                  b.perm, b.perm_atomic, b.nbr_hdr, b.nbr_w, b.cell_count, b.cell_start, b.scan_tmp, b.big_cells, b.big_count, b.scenes, b.stats_part,
                   b.stats, b.err, b.io, b.io2, scratch, snap_pos, snap_vel, snap_id};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -211,7 +211,7 @@ pbf_status Handle::alloc_all() {
       {(void**)&b.xs[0], f4}, {(void**)&b.xs[1], f4}, {(void**)&b.vel[0], f4}, {(void**)&b.vel[1], f4},
       {(void**)&b.omega, f4}, {(void**)&b.xkey, u4}, {(void**)&b.rho, u4}, {(void**)&b.rho_iter0, u4},
       {(void**)&b.id[0], u4}, {(void**)&b.id[1], u4}, {(void**)&b.key, u4}, {(void**)&b.rank, u4},
-      {(void**)&b.perm, u4}, {(void**)&b.nbr_hdr, sizeof(uint4) * n},
+      {(void**)&b.perm, u4}, {(void**)&b.perm_atomic, u4}, {(void**)&b.nbr_hdr, sizeof(uint4) * n},
       {(void**)&b.nbr_w, u4 * static_cast<size_t>((b.max_words + 3) / 4 * 4)},  // groups of 4 words
       {(void**)&b.cell_count, sizeof(uint32_t) * b.n_cells},
       {(void**)&b.cell_start, sizeof(uint32_t) * (b.n_cells + 1)},
@@ -367,7 +367,7 @@ pbf_status Handle::enqueue_steps(float dt, int nsteps) {
   const bool use_graph = (params.flags & PBF_FLAG_GRAPH) != 0;
   const bool keep_pred = b.pred != nullptr;
   const int it = params.iters;
-  // kernels per phase: k_predict; k_scan_tiles/sums/add; k_scatter, k_cellsort, k_cellsort_big;
+  // kernels per phase: k_predict; k_scan_tiles/sums/add; k_scatter, k_cellrank, k_cellsort_big;
   // k_gather; k_nbr_build; k_lambda and k_deltap per iteration; k_xsph; k_vort; k_stats and
   // k_stats_final when statistics are on
   const uint64_t per_step[kNumPhases] = {1, 3, 3, 1, 1, static_cast<uint64_t>(it), static_cast<uint64_t>(it),

@@ -101,7 +101,8 @@ struct Buffers {
   uint32_t* id[2] = {nullptr, nullptr};
   uint32_t* key = nullptr;
   uint32_t* rank = nullptr;
-  uint32_t* perm = nullptr;
+  uint32_t* perm = nullptr;         // slot -> pre-sort slot, cells ordered by x
+  uint32_t* perm_atomic = nullptr;  // the same in the per-cell atomic order of the counts
   uint4* nbr_hdr = nullptr;
   uint32_t* nbr_w = nullptr;
   uint32_t* cell_count = nullptr;

@@ -6,8 +6,8 @@
 //   k_predict     gravity + predicted move + collision, cell key, per-cell
 //                 count and rank (particles.cpp:175-183, 87-132)
 //   k_scan_*      exclusive prefix sum of the cell counts
-//   k_scatter     slot = cell start + rank
-//   k_cellsort    order each cell's slots by x, then original index (determinism)
+//   k_scatter     slot = cell start + rank (atomic order within a cell)
+//   k_cellrank    order each cell's slots by x, then original index (determinism)
 //   k_gather      reorder x, delta, id into cell order; x* = x + delta
 //   k_nbr_build   neighbour sets |x*_i - x*_j|^2 <= H2 over the 27 cells,
 //                 stored row-compressed (particles.cpp:258-265)
@@ -182,34 +182,36 @@ __global__ void k_scatter(const uint32_t* __restrict__ key, const uint32_t* __re
 // neighbour sum) is independent of atomic timing, and since cells along x are adjacent
 // slot ranges, every row of cells is sorted by x, which lets the neighbour build stop a
 // row at the first candidate beyond the reach. Cells up to kSmallCell particles are
-// insertion-sorted by one thread; larger ones go to a worklist for k_cellsort_big.
+// ranked by k_cellrank; larger ones go to a worklist for k_cellsort_big.
 // The x keys (order_bits of x*.x) are written by k_predict, indexed by the pre-sort slot.
 __device__ __forceinline__ uint64_t slot_order_key(const uint32_t* __restrict__ xkey, const uint32_t* __restrict__ id,
                                                    uint32_t v) {
   return (static_cast<uint64_t>(xkey[v]) << 32) | id[v];
 }
 
-__global__ void k_cellsort(const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ perm,
-                           const uint32_t* __restrict__ xkey, const uint32_t* __restrict__ id, uint32_t* __restrict__ big_cells,
-                           uint32_t* __restrict__ big_count, uint32_t m) {
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= m) return;
+// One thread per slot s of the scatter's (atomic) order: the entry moves to its cell's
+// start plus its rank, the number of the cell's entries with a smaller key (keys are
+// distinct). A cell's threads are neighbours, so its keys are read from L1. Cells over
+// kSmallCell particles are copied in atomic order and listed for k_cellsort_big (their
+// first slot's thread adds them).
+__global__ void k_cellrank(const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ atomic_order,
+                           const uint32_t* __restrict__ key, const uint32_t* __restrict__ xkey,
+                           const uint32_t* __restrict__ id, uint32_t* __restrict__ perm,
+                           uint32_t* __restrict__ big_cells, uint32_t* __restrict__ big_count, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint32_t v = atomic_order[s];
+  const uint32_t c = key[v];
   const uint32_t b = cell_start[c], e = cell_start[c + 1];
-  if (e - b < 2) return;
   if (e - b > kSmallCell) {
-    big_cells[atomicAdd(big_count, 1u)] = c;
+    perm[s] = v;
+    if (static_cast<uint32_t>(s) == b) big_cells[atomicAdd(big_count, 1u)] = c;
     return;
   }
-  for (uint32_t x = b + 1; x < e; ++x) {
-    const uint32_t v = perm[x];
-    const uint64_t kv = slot_order_key(xkey, id, v);
-    uint32_t y = x;
-    while (y > b && slot_order_key(xkey, id, perm[y - 1]) > kv) {
-      perm[y] = perm[y - 1];
-      --y;
-    }
-    perm[y] = v;
-  }
+  const uint64_t kv = slot_order_key(xkey, id, v);
+  uint32_t r = 0;
+  for (uint32_t u = b; u < e; ++u) r += slot_order_key(xkey, id, atomic_order[u]) < kv ? 1u : 0u;
+  perm[b + r] = v;
 }
 
 // Rank sort of the worklist's cells, one block per cell: the rank of an element is the
@@ -280,7 +282,7 @@ __global__ void k_gather(const uint32_t* __restrict__ perm, const float4* __rest
 // Each of the 9 candidate rows (3 z-slabs x 3 y-rows) is skipped when its cells lie
 // beyond h in y/z, and otherwise trimmed in x to the cells that reach [x - w, x + w],
 // w = sqrt(h^2 - d_yz^2): about 20 of the 27 cells on average. Within the trimmed row
-// (sorted by x, see k_cellsort) only candidates with |dx| <= w are tested. All tests keep
+// (sorted by x, see k_cellrank) only candidates with |dx| <= w are tested. All tests keep
 // a margin of 1e-3 cell, far above the FP32 rounding of the cell binning and of the
 // predicate, so no pair within h is dropped.
 template <int BLOCK>
@@ -847,9 +849,9 @@ cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& 
   k_scan_sums<<<1, 1024, 0, s>>>(b.scan_tmp, tiles, b.cell_start, m, b.big_count);
   k_scan_add<<<tiles, kScanThreads, 0, s>>>(b.cell_start, b.scan_tmp, m);
   if (mk) mk->mark(kPhaseScan, s);
-  k_scatter<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(b.key, b.rank, b.cell_start, b.perm, n);
-  k_cellsort<<<blocks_for(m, t.block_misc), t.block_misc, 0, s>>>(b.cell_start, b.perm, b.xkey, b.id[cur],
-                                                                   b.big_cells, b.big_count, m);
+  k_scatter<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(b.key, b.rank, b.cell_start, b.perm_atomic, n);
+  k_cellrank<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(b.cell_start, b.perm_atomic, b.key, b.xkey,
+                                                                   b.id[cur], b.perm, b.big_cells, b.big_count, n);
   k_cellsort_big<<<kBigSortBlocks, kBigSortThreads, 0, s>>>(b.cell_start, b.perm, b.xkey, b.id[cur], b.big_cells,
                                                              b.big_count);
   if (mk) mk->mark(kPhaseSort, s);
