@@ -231,6 +231,9 @@ pbf_status Handle::alloc_all() {
     pbf_status st = cuda(cudaMalloc((void**)&b.pred, f4), "cudaMalloc");
     if (st != PBF_OK) return st;
   }
+  pbf_status st = cuda(cudaMemsetAsync(b.scan_tmp, 0, sizeof(uint32_t) * ((b.n_cells + 1023) / 1024 + 1), stream),
+                       "cudaMemsetAsync");  // the scan's ticket word (after the tile sums) starts at zero
+  if (st != PBF_OK) return st;
   return cuda(cudaMemsetAsync(b.err, 0, sizeof(unsigned), stream), "cudaMemsetAsync");
 }
 
@@ -367,10 +370,11 @@ pbf_status Handle::enqueue_steps(float dt, int nsteps) {
   const bool use_graph = (params.flags & PBF_FLAG_GRAPH) != 0;
   const bool keep_pred = b.pred != nullptr;
   const int it = params.iters;
-  // kernels per phase: k_predict; k_scan_tiles/sums/add; k_scatter, k_cellrank, k_cellsort_big;
+  // kernels per phase: k_predict; k_scan_tiles (with the tile sums' scan), k_scan_add; k_scatter,
+  // k_cellrank, k_cellsort_big;
   // k_gather; k_nbr_build; k_lambda and k_deltap per iteration; k_xsph; k_vort; k_stats and
   // k_stats_final when statistics are on
-  const uint64_t per_step[kNumPhases] = {1, 3, 3, 1, 1, static_cast<uint64_t>(it), static_cast<uint64_t>(it),
+  const uint64_t per_step[kNumPhases] = {1, 2, 3, 1, 1, static_cast<uint64_t>(it), static_cast<uint64_t>(it),
                                          1, 1, dp.stats ? 2u : 0u};
   for (int k = 0; k < nsteps; ++k) {
     if (use_graph && graph_dt != dt) {

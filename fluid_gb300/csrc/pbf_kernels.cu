@@ -28,16 +28,10 @@ namespace {
 constexpr int kScanItems = 4;
 constexpr int kScanThreads = 256;
 constexpr int kScanTile = kScanItems * kScanThreads;
-constexpr uint32_t kSmallCell = 32;       // cells up to this size: insertion sort by one thread
+constexpr uint32_t kSmallCell = 32;       // cells up to this size: ranked slot by slot (k_cellrank)
 constexpr uint32_t kMaxSortedCell = 4096;  // larger cells: rank sort by one block (in shared memory)
 constexpr int kBigSortThreads = 256;
 constexpr int kBigSortBlocks = 64;
-
-__device__ __forceinline__ unsigned lanemask_lt() {
-  unsigned m;
-  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-  return m;
-}
 
 __device__ __forceinline__ int scene_of_slot(const float4& p) { return __float_as_int(p.w); }
 
@@ -77,15 +71,22 @@ __global__ void k_predict(const float4* __restrict__ pos, const float4* __restri
     key_out[i] = key;
     xkey_out[i] = order_bits(xp.x);
   }
-  // warp-aggregated per-cell rank
-  const unsigned active = __ballot_sync(0xffffffffu, live);
-  if (!live) return;
-  const unsigned peers = __match_any_sync(active, key);
-  const int leader = __ffs(peers) - 1;
+  // per-cell rank, one atomic per run of equal keys among consecutive lanes (the slots are
+  // still mostly in the cell order of the last step; measured 38 against 42 us a step for
+  // one atomic per distinct key of the warp by __match_any_sync on scrambled cells). Dead
+  // lanes carry the key 0xffffffff, a run of their own.
+  const unsigned lane = lane_id();
+  const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+  const bool head = lane == 0 || prev != key;
+  const unsigned heads = __ballot_sync(0xffffffffu, head);
+  const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);  // lanes 0..lane
+  const int start = 31 - __clz(heads & upto);                            // this lane's run head
+  const unsigned above = heads & ~upto;
+  const int next = above ? __ffs(above) - 1 : 32;                        // the next run's head
   uint32_t base = 0;
-  if (static_cast<int>(lane_id()) == leader) base = atomicAdd(&cell_count[key], __popc(peers));
-  base = __shfl_sync(peers, base, leader);
-  rank_out[i] = base + __popc(peers & lanemask_lt());
+  if (head && live) base = atomicAdd(&cell_count[key], static_cast<uint32_t>(next - static_cast<int>(lane)));
+  base = __shfl_sync(0xffffffffu, base, start);
+  if (live) rank_out[i] = base + (lane - static_cast<unsigned>(start));
 }
 
 // ---------------------------------------------------------------------------
@@ -119,10 +120,33 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
   return warp_off + x - v;
 }
 
+// Exclusive scan of the tile sums in place (carry over rounds of blockDim.x); start[m] =
+// the total. zero_word (or null): a counter the following phases need at zero (the cell
+// sort's worklist). The sums are read through L2: they may come from other blocks.
+__device__ __forceinline__ void scan_tile_sums(uint32_t* __restrict__ tile_sum, uint32_t tiles,
+                                               uint32_t* __restrict__ start, uint32_t m,
+                                               uint32_t* __restrict__ zero_word) {
+  if (zero_word && threadIdx.x == 0) *zero_word = 0u;
+  uint32_t carry = 0;
+  for (uint32_t b = 0; b < tiles; b += blockDim.x) {
+    const uint32_t idx = b + threadIdx.x;
+    const uint32_t v = idx < tiles ? __ldcg(&tile_sum[idx]) : 0u;
+    uint32_t total;
+    const uint32_t ex = block_exclusive_scan(v, &total);
+    if (idx < tiles) tile_sum[idx] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) start[m] = carry;
+}
+
+// Scan of each tile of kScanTile counts. With a ticket (a zeroed word), the last block to
+// finish also scans the tile sums (no block waits: each block counts itself in after its
+// sum is visible, and the one that counts last does the work, then clears the ticket).
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* __restrict__ count,
                                                               uint32_t* __restrict__ start,
                                                               uint32_t* __restrict__ tile_sum,
-                                                              uint32_t m) {
+                                                              uint32_t m, uint32_t* __restrict__ ticket,
+                                                              uint32_t* __restrict__ zero_word) {
   const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
   uint32_t v[kScanItems];
   uint32_t s = 0;
@@ -138,24 +162,28 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* __r
     if (base + k < m) start[base + k] = off;
     off += v[k];
   }
-  if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+  if (!ticket) {
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+    return;
+  }
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    tile_sum[blockIdx.x] = total;
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __threadfence();
+  }
+  __syncthreads();
+  if (last) {
+    scan_tile_sums(tile_sum, gridDim.x, start, m, zero_word);
+    if (threadIdx.x == 0) *ticket = 0u;
+  }
 }
 
-// zero_word (or null): a counter the following phases need at zero (the cell sort's worklist)
 __global__ void __launch_bounds__(1024) k_scan_sums(uint32_t* __restrict__ tile_sum, uint32_t tiles,
                                                      uint32_t* __restrict__ start, uint32_t m,
                                                      uint32_t* __restrict__ zero_word) {
-  if (zero_word && threadIdx.x == 0) *zero_word = 0u;
-  uint32_t carry = 0;
-  for (uint32_t b = 0; b < tiles; b += blockDim.x) {
-    const uint32_t idx = b + threadIdx.x;
-    const uint32_t v = idx < tiles ? tile_sum[idx] : 0u;
-    uint32_t total;
-    const uint32_t ex = block_exclusive_scan(v, &total);
-    if (idx < tiles) tile_sum[idx] = carry + ex;
-    carry += total;
-  }
-  if (threadIdx.x == 0) start[m] = carry;
+  scan_tile_sums(tile_sum, tiles, start, m, zero_word);
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_add(uint32_t* __restrict__ start,
@@ -322,6 +350,8 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
   const float ux = (xi.x - sc.origin[0]) * P.inv_cell;
   const float cell_w = 1.0f / P.inv_cell;
   const int y0 = cc.y > 0 ? cc.y - 1 : 0;
+  const float2 nxy = make_float2(-xi.x, -xi.y);
+  const float nz = -xi.z;
 #pragma unroll
   for (int g = 0; g < 3; ++g) {
     const int z = cc.z + g - 1;
@@ -358,7 +388,9 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
       // one reaching below x - W) finds the first candidate at or above x - W, and the
       // first one above x + W ends the row (W = w cells, margin included; with NaN
       // coordinates in the cell the search may start early, never late). The predicate
-      // reuses the x difference: the same _rn arithmetic as dist2_rn.
+      // reuses the x difference: the same roundings as dist2_rn. (One loop over a slab's
+      // three rows, lanes moving on to the next row when theirs ends, measured slower:
+      // 0.243 against 0.234 ms, 48 registers a thread against 40.)
       const float W = w * cell_w;
       const uint32_t first_end = __ldg(&cell_start[row + xa + 1]);
       for (int half = 0; half < 2; ++half) {
@@ -371,10 +403,13 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
         }
         for (uint32_t j = a; j < b; ++j) {
           const float4 xj = __ldg(&xs[j]);
-          const float ndx = __fsub_rn(xi.x, xj.x);
-          if (ndx < -W) break;
-          const float ndy = __fsub_rn(xi.y, xj.y), ndz = __fsub_rn(xi.z, xj.z);
-          if (__fadd_rn(__fadd_rn(__fmul_rn(ndx, ndx), __fmul_rn(ndy, ndy)), __fmul_rn(ndz, ndz)) <= P.h2) {
+          // x and y of x*_j - x*_i as one packed FP32x2 add against -x*_i (negation is
+          // exact: the same roundings as x*_i - x*_j up to sign) and one packed square
+          const float2 dxy = __fadd2_rn(make_float2(xj.x, xj.y), nxy);
+          if (dxy.x > W) break;
+          const float2 sq = __fmul2_rn(dxy, dxy);
+          const float dz = __fadd_rn(xj.z, nz);
+          if (__fadd_rn(__fadd_rn(sq.x, sq.y), __fmul_rn(dz, dz)) <= P.h2) {
             const uint32_t off = j - gb;
             if (off > kOffsetMask) {
               flags |= PBF_ERRBIT_ROW_CAPACITY;
@@ -845,8 +880,9 @@ cudaError_t sort_into_cells(const Buffers& b, const DevParams& P, const Tuning& 
         b.pos[cur], b.vel[cur], b.disp[0], b.key, b.xkey, b.rank, b.cell_count, b.scenes, P, dt, move ? 1 : 0, n);
   if (mk) mk->mark(kPhasePredict, s);
   const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
-  k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(b.cell_count, b.cell_start, b.scan_tmp, m);
-  k_scan_sums<<<1, 1024, 0, s>>>(b.scan_tmp, tiles, b.cell_start, m, b.big_count);
+  // scan_tmp holds the tile sums and, after them, the ticket of k_scan_tiles' last block
+  k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(b.cell_count, b.cell_start, b.scan_tmp, m, b.scan_tmp + tiles,
+                                               b.big_count);
   k_scan_add<<<tiles, kScanThreads, 0, s>>>(b.cell_start, b.scan_tmp, m);
   if (mk) mk->mark(kPhaseScan, s);
   k_scatter<<<blocks_for(n, t.block_misc), t.block_misc, 0, s>>>(b.key, b.rank, b.cell_start, b.perm_atomic, n);
@@ -996,7 +1032,7 @@ cudaError_t launch_neighbor_ids(const Buffers& b, int cur, const uint32_t* offse
 cudaError_t launch_exclusive_scan(const uint32_t* count, uint32_t* start, uint32_t* tile_sums, uint32_t m,
                                   cudaStream_t s) {
   const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
-  k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(count, start, tile_sums, m);
+  k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(count, start, tile_sums, m, nullptr, nullptr);
   k_scan_sums<<<1, 1024, 0, s>>>(tile_sums, tiles, start, m, nullptr);
   k_scan_add<<<tiles, kScanThreads, 0, s>>>(start, tile_sums, m);
   return cudaGetLastError();
