@@ -53,10 +53,10 @@ UNIT = "particle-updates/s"
 ALGO_BYTES = {"predict": 64 + 24, "sort": 104, "gather": 0, "lambda": 20, "deltap": 36,
               "xsph": 84, "vorticity": 64, "neighbors": 16, "scan": 0, "stats": 0}
 # DRAM bytes per particle per launch measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) on the 1M colliding-blocks scene: profiles/k_deltap_colliding_blocks_1m.md
-# (k_deltap) and profiles/neighbour_pass_forms_colliding_blocks_1m.md (k_lambda, k_nbr_build).
+# dram__bytes_write.sum) on the 1M colliding-blocks scene: profiles/k_deltap_colliding_blocks_1m.md,
+# profiles/k_lambda_colliding_blocks_1m.md and profiles/k_nbr_build_colliding_blocks_1m.md.
 PER_ITERATION = ("lambda", "deltap")  # phases launched once per Jacobi iteration
-NCU_TRAFFIC_PER_PARTICLE: dict[str, float] = {"deltap": 141.8, "lambda": 99.1, "neighbors": 62.2}
+NCU_TRAFFIC_PER_PARTICLE: dict[str, float] = {"deltap": 141.8, "lambda": 99.8, "neighbors": 83.2}
 
 
 def peaks():
