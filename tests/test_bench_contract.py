@@ -67,3 +67,33 @@ def test_reference_arm_under_torchrun_prints_once():
     assert len(lines) == 1, out.stdout[-2000:]
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
+@pytest.mark.gpu
+def test_gpu_arm_prints_one_contract_line():
+    """The default arm on a GB300: one JSON line with the contract's keys, the roofline of
+    the dominant kernel and of every phase, the end-to-end figure with its copies counted,
+    and the number of this library's launches in the timed region."""
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--steps", "3", "--warmup", "3",
+                          "--no-cpu-baseline", "--no-autotune", "--no-batched", "--no-adjoint", "--no-surface",
+                          "--no-render"], capture_output=True, text=True, timeout=900, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, out.stdout[-2000:]
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "dtype", "data", "config", "roofline", "e2e", "gpu_launches", "clocks"):
+        assert key in d, key
+    assert d["steps"] == 3 and d["warmup"] == 3 and d["n_gpus"] == 1 and d["value"] > 0
+    assert d["config"]["workload"] == "colliding_blocks_1m" and d["config"]["particles"] == 1048576
+    r = d["roofline"]
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s" and r["peak"] > 0
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-9
+    assert r["kernel"] in r["kernels"]
+    for k in ("lambda", "deltap", "neighbors", "xsph", "vorticity"):
+        assert 0 < r["kernels"][k]["frac"] < 1.5, (k, r["kernels"][k])
+    assert r["kernels"]["deltap"]["per"] == "launch" and r["kernels"]["deltap"]["launches_per_step"] == 4
+    e = d["e2e"]
+    assert e["h2d_bytes_per_step"] == e["d2h_bytes_per_step"] == 1048576 * 24
+    assert 0 < e["value"] < d["value"]
+    assert d["gpu_launches"] == 3 * 20  # kernels a step with statistics on, over the timed steps
