@@ -30,6 +30,7 @@ pytestmark = pytest.mark.gpu
 
 TOL_1STEP = 1e-5
 SENS_FACTOR = 3.0
+TWIN_FACTOR = 2.0
 FIELDS = ("pos", "vel", "density")
 
 
@@ -82,11 +83,18 @@ def _check_sets_and_cells(oracle_lib, g, prm, lo=None, hi=None):
     return int(off[-1])
 
 
-def _compare_one_step(name, oracle_lib, pos, vel, prm, g, strict=()):
+def _compare_one_step(name, oracle_lib, pos, vel, prm, g, strict=(), twin=False):
     """GPU vs FP64 on the same FP32 inputs, with the oracle's own neighbour search; the
     bar is 1e-5, or SENS_FACTOR x the FP64 sensitivity where that is larger (never for the
-    fields in ``strict``)."""
+    fields in ``strict``). With ``twin``, every field's bar is also at least TWIN_FACTOR x
+    the distance of the oracle's exact FP32 restatement from FP64: on a lattice whose pairs
+    sit at exactly h, FP32 and FP64 rounding put different pairs in the neighbour sets,
+    which the fixed-set sensitivity does not see."""
     ref = oracle_lib.step(pos, vel, prm, 1)
+    floor = {}
+    if twin:
+        r32 = oracle_lib.step(pos, vel, prm, 1, fp32=True)
+        floor = {k: TWIN_FACTOR * rel_err(r32[k], ref[k]) for k in FIELDS}
     got = {k: rel_err(g[k], ref[k]) for k in FIELDS}
     sens = _sensitivity(oracle_lib, pos, vel, prm, g["nbr"], oracle_lib.step(pos, vel, prm, 1,
                                                                              given_neighbors=g["nbr"]))
@@ -94,8 +102,11 @@ def _compare_one_step(name, oracle_lib, pos, vel, prm, g, strict=()):
     print(f"{name}: GPU vs FP64 normwise " + ", ".join(f"{k} {got[k]:.2e}" for k in FIELDS)
           + "; elementwise p99/max " + ", ".join(f"{k} {el[k][0]:.1e}/{el[k][1]:.1e}" for k in FIELDS)
           + "; FP64 sensitivity to FP32 input rounding " + ", ".join(f"{k} {sens[k]:.2e}" for k in FIELDS))
+    if floor:
+        print(f"{name}: FP32 restatement vs FP64 " + ", ".join(f"{k} {floor[k] / TWIN_FACTOR:.2e}" for k in FIELDS))
     for k in FIELDS:
         bar = TOL_1STEP if k in strict else max(TOL_1STEP, SENS_FACTOR * sens[k])
+        bar = max(bar, floor.get(k, 0.0))
         assert got[k] < bar, (k, got[k], bar)
     return got, sens
 
@@ -139,20 +150,20 @@ def test_dam_break_262k_one_step(pbf, oracle_lib):
 
 def test_batched_256_scenes_against_oracle(pbf, oracle_lib):
     """The full 256-scene batch (2,048-32,768 particles per scene, 2.8M in all) in one handle,
-    one step; eleven scenes spanning the count range (smallest, largest and the deciles
-    between) are each compared with the FP64 oracle stepping that scene alone, with their
-    neighbour sets checked against the FP32 predicate."""
+    one step; every scene is compared with the FP64 oracle stepping that scene alone, with
+    its neighbour sets checked against the FP32 predicate and no pair crossing scenes. The
+    scenes are jittered lattices of spacing h/2, so some pairs sit at distance h within FP32
+    rounding: on 24 of the 256 scenes the oracle's own FP32 restatement differs from FP64 by
+    more than 1e-5 (up to 6e-4 in velocity), and there the bar is twice that distance."""
     b = scenes.batched_256()
     pos, vel = _f32(b.pos), _f32(b.vel)
     g = _gpu_step(pbf, pos, vel, b.params, counts=b.counts, boxes=b.boxes)
     assert g["stats"]["error_flags"] == 0
     counts = np.asarray(b.counts)
     starts = np.concatenate([[0], np.cumsum(counts)])
-    order = np.argsort(counts, kind="stable")
-    pick = sorted({int(order[int(round(q * (len(order) - 1)))]) for q in np.linspace(0, 1, 11)})
-    assert len(pick) >= 8
+    assert len(counts) == 256
     off, ids = g["nbr"]
-    for s in pick:
+    for s in range(len(counts)):
         a, e = int(starts[s]), int(starts[s + 1])
         so = off[a:e + 1] - off[a]
         si = ids[off[a]:off[e]].astype(np.int64) - a
@@ -162,7 +173,7 @@ def test_batched_256_scenes_against_oracle(pbf, oracle_lib):
         sub = {k: g[k][a:e] for k in FIELDS}
         sub["nbr"] = (so, si)
         _compare_one_step(f"batched scene {s} ({e - a} particles)", oracle_lib, pos[a:e], vel[a:e], b.params, sub,
-                          strict=("pos", "density"))
+                          strict=("pos", "density"), twin=True)
 
 
 def _ensemble(oracle_lib, pos, vel, prm, steps, members, seed=0):
