@@ -222,6 +222,16 @@ def test_block4096_rollout_60_steps(pbf, oracle_lib):
     _rollout_band("block4096", pbf, oracle_lib, sc.pos, sc.vel, sc.params, 60, 3)
 
 
+def test_colliding_blocks_1m_rollout_2_steps(pbf, oracle_lib):
+    """The configured 1M colliding blocks over 2 steps, the last one within the scene's
+    neighbour capacity: with the configured tensile k the reference's formulation blows the
+    blocks apart in the first step and then collapses them into clumps (FP64: at most 32
+    neighbours at step 1, 113 at step 2, 565 at step 3, 2067 at step 5, 5362 at step 10,
+    against a capacity of 128), so its configured 200 steps cannot run."""
+    sc = scenes.colliding_blocks_1m()
+    _rollout_band("colliding_blocks_1m", pbf, oracle_lib, sc.pos, sc.vel, sc.params, 2, 2)
+
+
 def test_dam_break_262k_rollout_8_steps(pbf, oracle_lib):
     """The dam break over 8 steps. With 4 Jacobi iterations the reference's formulation lets
     this fluid clump (FP64: max neighbours 93 at step 8, 140 at step 11, 728 at step 20,
