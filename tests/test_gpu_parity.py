@@ -301,6 +301,27 @@ def test_neighbor_capacity_is_reported(pbf):
         assert e.value.status == 5
 
 
+def test_list_capacity_does_not_change_results(pbf):
+    """A slot's list words lie in groups of four: a capacity just above the largest list (its
+    last group partly used), an odd one and a large one give the same bits."""
+    sc = scenes.block4096(2)
+    pos, vel = _f32(sc.pos), _f32(sc.vel)
+    with pbf.Simulator(pos, vel, sc.params.with_(max_neighbors=256, flags=PBF_FLAG_STATS)) as sim:
+        sim.time_step(sc.params.dt, 1)
+        mx = sim.stats()["max_neighbors"]
+    assert mx > 8
+    outs = []
+    for cap in (mx, mx + 1, mx + 7, 256):
+        with pbf.Simulator(pos, vel, sc.params.with_(max_neighbors=cap, flags=PBF_FLAG_STATS)) as sim:
+            sim.time_step(sc.params.dt, 1)
+            assert sim.stats()["error_flags"] == 0, cap
+            outs.append((sim.positions(), sim.velocities(), sim.densities(), sim.neighbors()))
+    for o in outs[1:]:
+        for a, b in zip(o[:3], outs[0][:3]):
+            assert np.array_equal(a, b)
+        assert np.array_equal(o[3][0], outs[0][3][0]) and np.array_equal(o[3][1], outs[0][3][1])
+
+
 def test_autotune_keeps_state_and_results(pbf):
     """The autotuner restores the state it timed on; launch shapes never change results."""
     sc = scenes.block4096(3)
