@@ -273,6 +273,21 @@ def test_batched_equals_separate(pbf):
         off += c
 
 
+def test_batch_with_empty_scenes(pbf):
+    """Scenes without particles (first, in the middle, last) take no slots: the batch steps
+    the others to the same bits as a batch of only them."""
+    b = scenes.batched_256(seed=4, n_scenes=3, lo=500, hi=2000)
+    pos, vel = _f32(b.pos), _f32(b.vel)
+    with pbf.Simulator(pos, vel, b.params, counts=b.counts, boxes=b.boxes) as sim:
+        sim.time_step(b.params.dt, 2)
+        x0, v0 = sim.positions(), sim.velocities()
+    counts = [0, b.counts[0], 0, 0, b.counts[1], b.counts[2], 0]
+    boxes = [b.boxes[0], b.boxes[0], b.boxes[1], b.boxes[2], b.boxes[1], b.boxes[2], b.boxes[2]]
+    with pbf.Simulator(pos, vel, b.params, counts=counts, boxes=boxes) as sim:
+        sim.time_step(b.params.dt, 2)
+        assert np.array_equal(sim.positions(), x0) and np.array_equal(sim.velocities(), v0)
+
+
 def test_empty_and_tiny(pbf):
     prm = scenes.physical_params(0.1, 0.05)
     with pbf.Simulator(np.zeros((0, 3)), None, prm) as sim:
