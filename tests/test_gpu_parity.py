@@ -337,6 +337,37 @@ def test_list_capacity_does_not_change_results(pbf):
         assert np.array_equal(o[3][0], outs[0][3][0]) and np.array_equal(o[3][1], outs[0][3][1])
 
 
+def _capacity_params(h, s, hi):
+    return scenes.physical_params(h, s, box_lo=(0.0, 0.0, 0.0), box_hi=hi, clip_planes=(),
+                                  clamp_lo=(0.0, 0.0, 0.0), clamp_hi=hi)
+
+
+def test_slab_offset_limit_is_reported(pbf):
+    """A list entry holds a 14-bit offset into its slab's three rows of cells. Rows of 990
+    cells at ~16 particles a cell (15,000 slots a row) overflow it: the step must fail with
+    PBF_ERR_CAPACITY, not store a wrapped offset."""
+    h, s = 0.01, 0.004
+    p = scenes.lattice(2470, 7, 7, s, corner=(0.002, 0.002, 0.002))
+    prm = _capacity_params(h, s, (9.9, 0.032, 0.032))
+    with pbf.Simulator(_f32(p), np.zeros_like(p), prm) as sim:
+        with pytest.raises(pbf.PbfError) as e:
+            sim.time_step(prm.dt, 1)
+    assert e.value.status == 5 and "row" in str(e.value)
+
+
+def test_row_candidate_limit_is_reported(pbf):
+    """5,000 particles inside one cell: more candidates in a row than the build scans
+    (4,096); the step must fail with PBF_ERR_CAPACITY."""
+    h, s = 0.1, 0.05
+    rng = np.random.default_rng(3)
+    p = rng.uniform(0.52, 0.58, (5000, 3))
+    prm = _capacity_params(h, s, (1.0, 1.0, 1.0)).with_(max_neighbors=1024)
+    with pbf.Simulator(_f32(p), np.zeros_like(p), prm) as sim:
+        with pytest.raises(pbf.PbfError) as e:
+            sim.time_step(prm.dt, 1)
+    assert e.value.status == 5
+
+
 def test_autotune_keeps_state_and_results(pbf):
     """The autotuner restores the state it timed on; launch shapes never change results."""
     sc = scenes.block4096(3)
