@@ -328,18 +328,14 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
   const int cap = P.max_words * 2;
   uint32_t gbase[3] = {0u, 0u, 0u};
   int total = 0;
-  uint32_t word = 0;
-  // list words in groups of 4 (list_word): wptr walks the slot's words, one word at a time
-  // within a group and on to the next group after every fourth. (Collecting a group in
-  // registers or in shared memory and storing it as one 16-byte write measured slower:
-  // the appends run divergently, and the extra instructions and the smaller L1 cost more
-  // than the coalesced stores save.)
-  uint32_t* wptr = words + 4 * static_cast<size_t>(i);
-  const size_t wstep = 4 * static_cast<size_t>(n) - 3;
-  auto put = [&](int wi, uint32_t wv) {
-    *wptr = wv;
-    wptr += ((wi & 3) == 3) ? wstep : 1;
-  };
+  // List entries are stored one 16-bit half-word at a time: entry k of the slot is
+  // half-word k % 8 of its group k / 8 (list_word's word k / 2, low half first), so an
+  // append is one straight path with no word to assemble. (Pairing entries into words before
+  // storing: 0.232 against 0.210 ms; collecting a group in registers or in shared memory and
+  // storing it as one 16-byte write measured slower still: the appends run divergently, and
+  // extra instructions and a smaller L1 cost more than coalesced stores save.)
+  uint16_t* eptr = reinterpret_cast<uint16_t*>(words) + 8 * static_cast<size_t>(i);
+  const size_t estep = 8 * static_cast<size_t>(n) - 7;
   unsigned flags = 0;
   // position inside the own cell, in cells, and the reach in cells with its margin
   const float fy = (xi.y - sc.origin[1]) * P.inv_cell - static_cast<float>(cc.y);
@@ -411,26 +407,18 @@ __global__ void __launch_bounds__(BLOCK) k_nbr_build(const float4* __restrict__ 
           const float dz = __fadd_rn(xj.z, nz);
           if (__fadd_rn(__fadd_rn(sq.x, sq.y), __fmul_rn(dz, dz)) <= P.h2) {
             const uint32_t off = j - gb;
-            if (off > kOffsetMask) {
-              flags |= PBF_ERRBIT_ROW_CAPACITY;
-            } else if (total < cap) {
-              const uint32_t e = gbits | off;
-              if ((total & 1) == 0) {
-                word = e;
-              } else {
-                word |= e << 16;
-                put(total >> 1, word);
-              }
+            if (off <= kOffsetMask && total < cap) {
+              *eptr = static_cast<uint16_t>(gbits | off);
+              eptr += ((total & 7) == 7) ? estep : 1;
               ++total;
             } else {
-              flags |= PBF_ERRBIT_NEIGHBOR_CAPACITY;
+              flags |= off > kOffsetMask ? PBF_ERRBIT_ROW_CAPACITY : PBF_ERRBIT_NEIGHBOR_CAPACITY;
             }
           }
         }
       }
     }
   }
-  if (total & 1) put(total >> 1, word);
   // the slab bases relative to slab 0's, less the tag bits (nbr_decode)
   hdr[i] = make_uint4(gbase[0], gbase[1] - gbase[0] - (1u << kOffsetBits),
                       gbase[2] - gbase[0] - (2u << kOffsetBits), static_cast<uint32_t>(total));
