@@ -56,7 +56,7 @@ ALGO_BYTES = {"predict": 64 + 24, "sort": 104, "gather": 0, "lambda": 20, "delta
 # dram__bytes_write.sum) on the 1M colliding-blocks scene: profiles/k_deltap_colliding_blocks_1m.md,
 # profiles/k_lambda_colliding_blocks_1m.md and profiles/k_nbr_build_colliding_blocks_1m.md.
 PER_ITERATION = ("lambda", "deltap")  # phases launched once per Jacobi iteration
-NCU_TRAFFIC_PER_PARTICLE: dict[str, float] = {"deltap": 141.8, "lambda": 99.8, "neighbors": 83.2}
+NCU_TRAFFIC_PER_PARTICLE: dict[str, float] = {"deltap": 141.8, "lambda": 99.8, "neighbors": 86.0}
 
 
 def peaks():
